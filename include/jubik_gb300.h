@@ -1,0 +1,181 @@
+/*
+ * jubik_gb300.h -- C ABI of the GB300 (sm_103a) implementation of J-UBIK's
+ * spatially-variant instrument response and its Poisson likelihood.
+ *
+ * Conventions
+ *  - Every function returns an int status: JUBIK_OK (0) or a negative code;
+ *    jubik_last_error() gives a message for the calling thread.  Nothing
+ *    aborts or throws across this boundary.
+ *  - Array arguments are DEVICE pointers owned by the caller, C-contiguous,
+ *    of the plan's dtype (float or double) unless stated otherwise.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default).
+ *  - A plan owns its device workspace; calls on one plan must not overlap
+ *    (the plan is not thread-safe across concurrent calls).
+ *  - Shapes: M telescope modules, E energy bins, field nx x ny, n patches
+ *    per axis (stride dx = nx / n), margin m; window K = 2 dx; FFT side
+ *    P = K + 2 m (jubik/convolve.py:43-44, :87-101).
+ */
+#ifndef JUBIK_GB300_H
+#define JUBIK_GB300_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define JUBIK_API __attribute__((visibility("default")))
+#else
+#define JUBIK_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define JUBIK_ABI_VERSION 1
+
+enum jubik_status {
+  JUBIK_OK = 0,
+  JUBIK_ERR_INVALID_ARGUMENT = -1, /* the reference raises ValueError here */
+  JUBIK_ERR_UNSUPPORTED = -2,      /* shape outside what the kernels cover */
+  JUBIK_ERR_CUDA = -3,
+  JUBIK_ERR_ALLOC = -4,
+  JUBIK_ERR_STATE = -5 /* e.g. PSF / exposure / data not set yet */
+};
+
+enum jubik_dtype { JUBIK_F32 = 0, JUBIK_F64 = 1 };
+
+enum jubik_path {
+  JUBIK_PATH_AUTO = 0,  /* fused when the FFT side and dtype allow it */
+  JUBIK_PATH_FUSED = 1, /* one kernel per patch unit: FFT, PSF product, overlap-add */
+  JUBIK_PATH_PLAIN = 2  /* unfused: batched FFT kernels + gather kernels */
+};
+
+enum jubik_psf_layout {
+  JUBIK_PSF_PRECUT = 0, /* (M, n*n, E, K, K): the window convolve.py:107-111 cuts */
+  JUBIK_PSF_FULL = 1    /* (M, n*n, E, nx, ny): full-field kernels as passed to
+                           linpatch_convolve (convolve.py:66, erosita_response.py:209) */
+};
+
+typedef struct jubik_plan jubik_plan;
+
+typedef struct {
+  int32_t n_modules;  /* M: the vmapped module axis, erosita_response.py:209-212 */
+  int32_t n_energies; /* E */
+  int32_t nx, ny;     /* spatial field shape (Domain.shape[-2:], data.py:19-29) */
+  int32_t n_patches;  /* n_patches_per_axis */
+  int32_t margin;     /* margin (>= 1; the reference crops [m:-m]) */
+  int32_t dtype;      /* jubik_dtype */
+  int32_t path;       /* jubik_path */
+  double pixel_area;  /* x * pixel_area before the PSF, erosita_response.py:307,350 */
+} jubik_plan_desc;
+
+/* Library info. */
+JUBIK_API int jubik_abi_version(void);
+JUBIK_API const char* jubik_last_error(void);
+/* 1 if the fused single-kernel path covers FFT side P in dtype. */
+JUBIK_API int jubik_fused_supported(int32_t P, int32_t dtype);
+/* 1 if the plain batched FFT covers length L. */
+JUBIK_API int jubik_fft_length_supported(int32_t L);
+
+/* Plan lifetime.  Replaces the per-call set-up inside linpatch_convolve
+ * (jubik/convolve.py:66-131) and the response builders
+ * (erosita_response.py:217-358, chandra_response.py:20-149). */
+JUBIK_API int jubik_plan_create(const jubik_plan_desc* desc, jubik_plan** out);
+JUBIK_API int jubik_plan_destroy(jubik_plan* plan);
+/* Device bytes held by the plan's workspace. */
+JUBIK_API int jubik_plan_workspace_bytes(const jubik_plan* plan, int64_t* bytes);
+/* Effective path of the plan (JUBIK_PATH_FUSED or JUBIK_PATH_PLAIN). */
+JUBIK_API int jubik_plan_path(const jubik_plan* plan, int32_t* path);
+
+/* PSF kernels -> normalised spectra, computed once per plan (FP64 FFTs,
+ * rounded once to the plan dtype).  Restates the kernel preparation of
+ * jubik/convolve.py:104-131 (fftshift, cut, pad, ifftshift, / sum*dvol).
+ * psf has the plan dtype; e_broadcast = 1 when the psf has no E axis
+ * (the broadcast branch of convolve.py:167-171). */
+JUBIK_API int jubik_plan_set_psf(jubik_plan* plan, const void* psf, int32_t layout, int32_t e_broadcast,
+                       void* stream);
+
+/* Exposure and readout mask.  exposure (M,E,nx,ny) in plan dtype or NULL
+ * for ones (response.py:12-45, already thresholded and multiplied by any
+ * effective area); readmask (M,E,nx,ny) uint8, nonzero = read out, or NULL
+ * for all (the ~mask of response.py:87,110).  Readout order is C order per
+ * module, modules concatenated. */
+JUBIK_API int jubik_plan_set_exposure(jubik_plan* plan, const void* exposure, const uint8_t* readmask,
+                            void* stream);
+/* Host: number of read-out pixels per module (length M) and in total. */
+JUBIK_API int jubik_plan_readout_sizes(const jubik_plan* plan, int64_t* per_module, int64_t* total);
+/* Host: readout index map, total entries of flat (M,E,nx,ny) indices (device ptr). */
+JUBIK_API int jubik_plan_readout_index(const jubik_plan* plan, const int64_t** device_index);
+
+/* Poisson counts in readout order (int32, length total), the masked_data
+ * of erosita_likelihood.py:89 / chandra_likelihood.py:37. */
+JUBIK_API int jubik_plan_set_data(jubik_plan* plan, const int32_t* counts, void* stream);
+
+/* PSF operator: out (M,E,nx,ny) = linpatch_convolve(x, domain, kernel[m], n, margin)
+ * for every module m (jubik/convolve.py:66-145 vmapped as in
+ * erosita_response.py:209-212).  x: (E,nx,ny).  No pixel_area. */
+JUBIK_API int jubik_psf_forward(jubik_plan* plan, const void* x, void* out, void* stream);
+/* Its transpose: out_x (E,nx,ny) = sum_m linpatch_convolve^T(cot[m]). */
+JUBIK_API int jubik_psf_adjoint(jubik_plan* plan, const void* cot, void* out_x, void* stream);
+
+/* Full response R(x) = mask(exposure(psf(x * pixel_area)))
+ * (erosita_response.py:349-350, chandra_response.py:138-142).
+ * out_readout: total elements, readout order. */
+JUBIK_API int jubik_response_forward(jubik_plan* plan, const void* x, void* out_readout, void* stream);
+/* JVP of the (linear) response: R(t). */
+JUBIK_API int jubik_response_jvp(jubik_plan* plan, const void* t, void* out_readout, void* stream);
+/* VJP: out_x = R^T cot (pixel_area * psf^T(exposure * mask^T(cot))). */
+JUBIK_API int jubik_response_vjp(jubik_plan* plan, const void* cot_readout, void* out_x, void* stream);
+
+/* Poisson energy and gradient through the response, one fused pass:
+ * lam = R(x); energy = sum(lam) - sum(d * log(lam)) (NIFTy.re Poissonian,
+ * demos/x-ray-imaging.py:312-315), accumulated in FP64; grad_x = R^T(1 - d/lam).
+ * energy: device double[1]; grad_x may be NULL (energy only).  lam is kept
+ * in the plan for jubik_metric_apply. */
+JUBIK_API int jubik_poisson_energy_grad(jubik_plan* plan, const void* x, double* energy, void* grad_x,
+                              void* stream);
+/* MGVI metric product out = R^T diag(1/lam) R v, lam = R(x).  x == NULL
+ * reuses lam from the last jubik_poisson_energy_grad call. */
+JUBIK_API int jubik_metric_apply(jubik_plan* plan, const void* x, const void* v, void* out,
+                       void* stream);
+
+/* Stand-alone Poisson likelihood on readout vectors (jft.Poissonian(data)):
+ * energy (device double[1]) = sum(lam - d log lam); grad (may be NULL) = 1 - d/lam. */
+JUBIK_API int jubik_poisson_energy(const void* lam, const int32_t* data, int64_t n, int32_t dtype,
+                         double* energy, void* grad, void* stream);
+/* Elementwise Poisson helpers: op 0 metric t/lam, 1 left-sqrt-metric t/sqrt(lam),
+ * 2 normalised residual (d - lam)/sqrt(lam) (b unused, uses data),
+ * 3 exposure product a*b (response.py:44). */
+JUBIK_API int jubik_elementwise(int32_t op, const void* a, const void* b, const int32_t* data, int64_t n,
+                      int32_t dtype, void* out, void* stream);
+
+/* Readout (response.py:110) and its transpose with an explicit index map
+ * (flat int64 indices into the image, ascending).  gather: out[i] = img[idx[i]]
+ * (eps may be NULL or multiplies); scatter: img[idx[i]] = eps[idx[i]]*vec[i]
+ * (img must be zeroed by the caller). */
+JUBIK_API int jubik_readout_gather(const void* img, const void* eps, const int64_t* idx, int64_t nread,
+                         int32_t dtype, void* out, void* stream);
+JUBIK_API int jubik_readout_scatter(const void* vec, const void* eps, const int64_t* idx, int64_t nread,
+                          int32_t dtype, void* img, void* stream);
+
+/* slice_patches (jubik/convolve.py:28-63) over x (batch, nx, ny):
+ * out (n*n, batch, 2dx+2dr, 2dy+2dr).  Bit-exact gather. */
+JUBIK_API int jubik_slice_patches(const void* x, int64_t batch, int32_t nx, int32_t ny, int32_t n,
+                        int32_t additional_margin, int32_t dtype, void* out, void* stream);
+/* Its transpose (jax.linear_transpose at convolve.py:138-143): overlap-add of
+ * patches (n*n, batch, 2dx+2dr, 2dy+2dr) into out (batch, nx, ny). */
+JUBIK_API int jubik_slice_patches_adjoint(const void* patches, int64_t batch, int32_t nx, int32_t ny,
+                                int32_t n, int32_t additional_margin, int32_t dtype, void* out,
+                                void* stream);
+
+/* convolve (jubik/convolve.py:148-176) over the last two axes:
+ * out (bs, h, w) = dvol * Re(ifft2(fft2(kernel) * fft2(signal))), kernel
+ * (bk, h, w) with bk == bs, or bk dividing bs (kernel broadcast over the
+ * trailing signal batch, the branch of convolve.py:167-171). */
+JUBIK_API int jubik_convolve2d(const void* kernel, int64_t bk, const void* signal, int64_t bs, int32_t h,
+                     int32_t w, double dvol, int32_t dtype, void* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* JUBIK_GB300_H */

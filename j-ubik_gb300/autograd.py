@@ -1,0 +1,55 @@
+"""torch.autograd wrappers of the GB300 response kernels.
+
+The response is linear in the sky, so its JVP is the forward kernel on the
+tangent and its VJP is the hand-written adjoint kernel (correlation with the
+PSF, transposed overlap-add, transposed exposure and readout).  The Poisson
+energy returns its gradient from the same fused forward+adjoint pass.
+"""
+from __future__ import annotations
+
+import torch
+
+
+class PsfOpFn(torch.autograd.Function):
+    """x (E,nx,ny) -> (M,E,nx,ny): linpatch_convolve for every module."""
+
+    @staticmethod
+    def forward(ctx, x, plan):
+        ctx.plan = plan
+        return plan.psf_forward(x)
+
+    @staticmethod
+    def backward(ctx, g):
+        return ctx.plan.psf_adjoint(g.contiguous()), None
+
+
+class ResponseFn(torch.autograd.Function):
+    """x (E,nx,ny) -> flat readout of R(x)."""
+
+    @staticmethod
+    def forward(ctx, x, plan):
+        ctx.plan = plan
+        return plan.response(x)
+
+    @staticmethod
+    def backward(ctx, g):
+        return ctx.plan.response_vjp(g.contiguous()), None
+
+    @staticmethod
+    def jvp(ctx, t, _):
+        return ctx.plan.response(t)
+
+
+class PoissonEnergyFn(torch.autograd.Function):
+    """x -> H(R(x)) (float64 scalar); dH/dx from the fused pass."""
+
+    @staticmethod
+    def forward(ctx, x, plan):
+        e, g = plan.energy_and_grad(x, need_grad=True)
+        ctx.save_for_backward(g)
+        return e
+
+    @staticmethod
+    def backward(ctx, ge):
+        (g,) = ctx.saved_tensors
+        return (ge.to(g.dtype) * g), None

@@ -1,0 +1,768 @@
+// C ABI of libjubik_gb300: plans, workspace, dispatch of the fused and the
+// unfused (plain) paths, readout index map, likelihood entry points.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "internal.h"
+#include "jubik_common.cuh"
+
+namespace jubik {
+
+namespace {
+thread_local char g_err[1024] = "";
+}
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+int cuda_status(cudaError_t err, const char* what) {
+  if (err == cudaSuccess) return JUBIK_OK;
+  set_error("%s: %s", what, cudaGetErrorString(err));
+  return err == cudaErrorMemoryAllocation ? JUBIK_ERR_ALLOC : JUBIK_ERR_CUDA;
+}
+
+namespace {
+
+constexpr int kScanBlock = 1024;  // elements per scan block
+
+// per-block counts of the read-out mask
+__global__ void k_mask_counts(const uint8_t* __restrict__ mask, int64_t n, int32_t* counts) {
+  __shared__ int32_t red[256];
+  const int64_t base = (int64_t)blockIdx.x * kScanBlock;
+  int32_t c = 0;
+  for (int i = threadIdx.x; i < kScanBlock; i += blockDim.x) {
+    const int64_t p = base + i;
+    if (p < n && mask[p]) ++c;
+  }
+  red[threadIdx.x] = c;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) counts[blockIdx.x] = red[0];
+}
+
+// exclusive scan of the block counts (single thread; one-off set-up work)
+__global__ void k_scan_counts(const int32_t* counts, int64_t nb, int64_t* offsets) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int64_t acc = 0;
+  for (int64_t i = 0; i < nb; ++i) {
+    offsets[i] = acc;
+    acc += counts[i];
+  }
+  offsets[nb] = acc;
+}
+
+// C-order compaction: ridx[p] = readout position or -1; list[pos] = p
+__global__ void k_mask_compact(const uint8_t* __restrict__ mask, int64_t n,
+                               const int64_t* __restrict__ offsets, int32_t* __restrict__ ridx,
+                               int64_t* __restrict__ list) {
+  __shared__ int32_t flags[kScanBlock];
+  const int64_t base = (int64_t)blockIdx.x * kScanBlock;
+  for (int i = threadIdx.x; i < kScanBlock; i += blockDim.x) {
+    const int64_t p = base + i;
+    flags[i] = (p < n && mask[p]) ? 1 : 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {  // serial prefix inside the block (1024 entries)
+    int32_t acc = 0;
+    for (int i = 0; i < kScanBlock; ++i) {
+      const int32_t f = flags[i];
+      flags[i] = f ? acc : -1;
+      acc += f;
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kScanBlock; i += blockDim.x) {
+    const int64_t p = base + i;
+    if (p >= n) continue;
+    const int32_t loc = flags[i];
+    if (loc < 0) {
+      ridx[p] = -1;
+    } else {
+      const int64_t pos = offsets[blockIdx.x] + loc;
+      ridx[p] = (int32_t)pos;
+      list[pos] = p;
+    }
+  }
+}
+
+__global__ void k_iota(int32_t* ridx, int64_t* list, int64_t n) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    ridx[p] = (int32_t)p;
+    list[p] = p;
+  }
+}
+
+template <typename T>
+__global__ void k_to_cplx(const T* __restrict__ a, int64_t n, cx<T>* __restrict__ z) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    z[i] = mkc<T>(a[i], (T)0);
+}
+
+template <typename T>
+__global__ void k_mul_bcast(const cx<T>* __restrict__ zk, int64_t bk, cx<T>* __restrict__ zs,
+                            int64_t bs, int64_t hw) {
+  const int64_t total = bs * hw;
+  const int64_t rep = bs / bk;  // signal planes per kernel plane
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t plane = i / hw, r = i - plane * hw;
+    zs[i] = cmul<T>(zk[(plane / rep) * hw + r], zs[i]);
+  }
+}
+
+template <typename T>
+__global__ void k_real_out(const cx<T>* __restrict__ z, int64_t n, T scale, T* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = scale * z[i].x;
+}
+
+inline unsigned blocks_for(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  if (b > 1048576) b = 1048576;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+
+// numpy.linspace(0, 1, h) for the bilinear weights of jubik/convolve.py:18-25:
+// step = 1/(h-1), a_i = i*step, last element exactly 1.
+std::vector<double> bilinear_vector(int K) {
+  const int h = K / 2;
+  std::vector<double> a(h);
+  if (h == 1) {
+    a[0] = 0.0;
+  } else {
+    const double step = 1.0 / (double)(h - 1);
+    for (int i = 0; i < h; ++i) a[i] = (double)i * step;
+    a[h - 1] = 1.0;
+  }
+  std::vector<double> b(K);
+  for (int i = 0; i < h; ++i) {
+    b[i] = a[i];
+    b[K - 1 - i] = a[i];
+  }
+  return b;
+}
+
+template <typename T>
+int convolve2d_run(const void* kernel, int64_t bk, const void* signal, int64_t bs, int64_t hw,
+                   double dvol, const Fft1D& fh, const Fft1D& fw, void* zk, void* zs, void* out,
+                   cudaStream_t s) {
+  k_to_cplx<T><<<blocks_for(bk * hw), 256, 0, s>>>((const T*)kernel, bk * hw, (cx<T>*)zk);
+  k_to_cplx<T><<<blocks_for(bs * hw), 256, 0, s>>>((const T*)signal, bs * hw, (cx<T>*)zs);
+  JUBIK_TRY(fft2_batched<T>(fh, fw, zk, bk, false, s));
+  JUBIK_TRY(fft2_batched<T>(fh, fw, zs, bs, false, s));
+  k_mul_bcast<T><<<blocks_for(bs * hw), 256, 0, s>>>((const cx<T>*)zk, bk, (cx<T>*)zs, bs, hw);
+  JUBIK_TRY(fft2_batched<T>(fh, fw, zs, bs, true, s));
+  k_real_out<T><<<blocks_for(bs * hw), 256, 0, s>>>((const cx<T>*)zs, bs * hw,
+                                                    (T)(dvol / (double)hw), (T*)out);
+  return cuda_status(cudaGetLastError(), "convolve2d");
+}
+
+}  // namespace
+}  // namespace jubik
+
+using namespace jubik;
+
+struct jubik_plan {
+  jubik_plan_desc desc{};
+  Geom g;
+  int path = JUBIK_PATH_PLAIN;
+  int dtype = JUBIK_F32;
+  size_t esz = 4;
+  int device = 0;
+  size_t bytes = 0;
+  // constants
+  void* wt = nullptr;  // (K) bilinear weights
+  void* tw = nullptr;  // (P) fused twiddles
+  Fft1D fft;           // plain transforms of length P
+  // PSF spectra
+  void* hmain = nullptr;
+  void* hnyq = nullptr;
+  void* hfull = nullptr;
+  // images (M,E,nx,ny)
+  void* conv = nullptr;
+  void* conv_v = nullptr;
+  void* resid = nullptr;
+  void* lam = nullptr;
+  void* eps = nullptr;
+  int32_t* ridx = nullptr;
+  int64_t* rlist = nullptr;
+  int32_t* data = nullptr;
+  double* partials = nullptr;
+  unsigned int* counter = nullptr;
+  // unfused work buffers
+  void* zs = nullptr;
+  void* zu = nullptr;
+  int zu_modules = 0;
+  // state
+  bool psf_set = false, exposure_set = false, data_set = false, lam_valid = false;
+  std::vector<int64_t> readout_sizes;
+  int64_t readout_total = 0;
+  std::vector<void*> allocs;
+
+  int alloc(void** p, size_t n) {
+    if (n == 0) n = 16;
+    cudaError_t e = cudaMalloc(p, n);
+    if (e != cudaSuccess) return cuda_status(e, "cudaMalloc (plan workspace)");
+    allocs.push_back(*p);
+    bytes += n;
+    return JUBIK_OK;
+  }
+  ~jubik_plan() {
+    for (void* p : allocs) cudaFree(p);
+    fft1d_free(&fft);
+  }
+};
+
+namespace {
+
+inline cudaStream_t S(void* s) { return (cudaStream_t)s; }
+
+int check_plan(const jubik_plan* p) {
+  if (!p) {
+    set_error("plan is NULL");
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  return JUBIK_OK;
+}
+
+int64_t image_elems(const jubik_plan* p) { return (int64_t)p->g.M * p->g.E * p->g.pixels(); }
+
+// forward of the PSF operator: out (M,E,nx,ny) = scale * sum_k patch convolutions
+int do_forward(jubik_plan* p, const void* x, void* out, double scale, cudaStream_t s) {
+  const Geom& g = p->g;
+  if (p->path == JUBIK_PATH_FUSED) {
+    JUBIK_TRY_CUDA(cudaMemsetAsync(out, 0, image_elems(p) * p->esz, s));
+    FusedLaunch a{x, out, p->hmain, p->hnyq, p->tw, p->wt, scale};
+    return fused_forward(g, p->dtype, a, s);
+  }
+  const bool f32 = p->dtype == JUBIK_F32;
+  const int64_t n2p = (int64_t)g.n * g.n;
+  JUBIK_TRY(f32 ? plain_sky_patches<float>(g, x, p->wt, p->zs, s)
+                : plain_sky_patches<double>(g, x, p->wt, p->zs, s));
+  JUBIK_TRY(f32 ? fft2_batched<float>(p->fft, p->fft, p->zs, g.E * n2p, false, s)
+                : fft2_batched<double>(p->fft, p->fft, p->zs, g.E * n2p, false, s));
+  for (int m0 = 0; m0 < g.M; m0 += p->zu_modules) {
+    const int nm = std::min(p->zu_modules, g.M - m0);
+    JUBIK_TRY(f32 ? plain_mul_modules<float>(g, p->zs, p->hfull, m0, nm, p->zu, s)
+                  : plain_mul_modules<double>(g, p->zs, p->hfull, m0, nm, p->zu, s));
+    JUBIK_TRY(f32 ? fft2_batched<float>(p->fft, p->fft, p->zu, (int64_t)nm * g.E * n2p, true, s)
+                  : fft2_batched<double>(p->fft, p->fft, p->zu, (int64_t)nm * g.E * n2p, true, s));
+    JUBIK_TRY(f32 ? plain_overlap_gather<float>(g, p->zu, m0, nm, scale, out, s)
+                  : plain_overlap_gather<double>(g, p->zu, m0, nm, scale, out, s));
+  }
+  return JUBIK_OK;
+}
+
+// transpose: out_x (E,nx,ny) = scale * sum_m psf_m^T cot[m]
+int do_adjoint(jubik_plan* p, const void* cot, void* out_x, double scale, cudaStream_t s) {
+  const Geom& g = p->g;
+  if (p->path == JUBIK_PATH_FUSED) {
+    JUBIK_TRY_CUDA(cudaMemsetAsync(out_x, 0, (size_t)g.E * g.pixels() * p->esz, s));
+    FusedLaunch a{cot, out_x, p->hmain, p->hnyq, p->tw, p->wt, scale};
+    return fused_adjoint(g, p->dtype, a, s);
+  }
+  const bool f32 = p->dtype == JUBIK_F32;
+  const int64_t n2p = (int64_t)g.n * g.n;
+  for (int m0 = 0; m0 < g.M; m0 += p->zu_modules) {
+    const int nm = std::min(p->zu_modules, g.M - m0);
+    JUBIK_TRY(f32 ? plain_cot_patches<float>(g, cot, m0, nm, p->zu, s)
+                  : plain_cot_patches<double>(g, cot, m0, nm, p->zu, s));
+    JUBIK_TRY(f32 ? fft2_batched<float>(p->fft, p->fft, p->zu, (int64_t)nm * g.E * n2p, false, s)
+                  : fft2_batched<double>(p->fft, p->fft, p->zu, (int64_t)nm * g.E * n2p, false,
+                                         s));
+    JUBIK_TRY(f32 ? plain_mulconj_accum<float>(g, p->zu, p->hfull, m0, nm, m0 == 0, p->zs, s)
+                  : plain_mulconj_accum<double>(g, p->zu, p->hfull, m0, nm, m0 == 0, p->zs, s));
+  }
+  JUBIK_TRY(f32 ? fft2_batched<float>(p->fft, p->fft, p->zs, g.E * n2p, true, s)
+                : fft2_batched<double>(p->fft, p->fft, p->zs, g.E * n2p, true, s));
+  return f32 ? plain_grad_gather<float>(g, p->zs, p->wt, scale, out_x, s)
+             : plain_grad_gather<double>(g, p->zs, p->wt, scale, out_x, s);
+}
+
+int need(bool ok, const char* what) {
+  if (!ok) {
+    set_error("%s not set on this plan", what);
+    return JUBIK_ERR_STATE;
+  }
+  return JUBIK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int jubik_abi_version(void) { return JUBIK_ABI_VERSION; }
+
+const char* jubik_last_error(void) { return g_err; }
+
+int jubik_fused_supported(int32_t P, int32_t dtype) { return fused_supported(P, dtype) ? 1 : 0; }
+
+int jubik_fft_length_supported(int32_t L) { return fft_length_supported(L) ? 1 : 0; }
+
+int jubik_plan_create(const jubik_plan_desc* d, jubik_plan** out) {
+  if (!d || !out) {
+    set_error("NULL argument");
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  *out = nullptr;
+  if (d->dtype != JUBIK_F32 && d->dtype != JUBIK_F64) {
+    set_error("dtype must be JUBIK_F32 or JUBIK_F64");
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  if (d->n_modules < 1 || d->n_energies < 1 || d->nx < 1 || d->ny < 1 || d->n_patches < 1) {
+    set_error("modules, energies, field and n_patches must be >= 1");
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  if (d->margin < 1) {
+    set_error("margin must be >= 1 (the reference crops [margin:-margin])");
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  Geom g;
+  g.M = d->n_modules;
+  g.E = d->n_energies;
+  g.nx = d->nx;
+  g.ny = d->ny;
+  g.n = d->n_patches;
+  g.dx = d->nx / d->n_patches;
+  const int dy = d->ny / d->n_patches;
+  if (g.dx < 1 || dy != g.dx) {
+    set_error("patch stride must be >= 1 and equal on both axes (got %d and %d): the "
+              "bilinear weights of convolve.py:18-25 are square",
+              g.dx, dy);
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  g.margin = d->margin;
+  g.half = g.dx / 2;
+  g.K = 2 * g.dx;
+  g.P = g.K + 2 * g.margin;
+  g.sr_max = g.nx + 2 * g.half - g.K;
+  g.sc_max = g.ny + 2 * g.half - g.K;
+  if (g.sr_max < 0 || g.sc_max < 0) {
+    set_error("patch window does not fit the padded field");
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  if (!fft_length_supported(g.P)) {
+    set_error("FFT side P=%d unsupported", g.P);
+    return JUBIK_ERR_UNSUPPORTED;
+  }
+  jubik_plan* p = new (std::nothrow) jubik_plan();
+  if (!p) {
+    set_error("host allocation failed");
+    return JUBIK_ERR_ALLOC;
+  }
+  p->desc = *d;
+  p->g = g;
+  p->dtype = d->dtype;
+  p->esz = d->dtype == JUBIK_F32 ? 4 : 8;
+  cudaGetDevice(&p->device);
+  const bool fused_ok = fused_supported(g.P, d->dtype);
+  if (d->path == JUBIK_PATH_FUSED && !fused_ok) {
+    delete p;
+    set_error("fused path does not cover P=%d in this dtype", g.P);
+    return JUBIK_ERR_UNSUPPORTED;
+  }
+  p->path = (d->path == JUBIK_PATH_PLAIN || !fused_ok) ? JUBIK_PATH_PLAIN : JUBIK_PATH_FUSED;
+
+  int st = JUBIK_OK;
+  auto fail = [&](int s) {
+    delete p;
+    return s;
+  };
+  const size_t csz = 2 * p->esz;
+  const int64_t units = g.units();
+  const int64_t img = (int64_t)g.M * g.E * g.pixels();
+  // constants
+  {
+    std::vector<double> b = bilinear_vector(g.K);
+    if ((st = p->alloc(&p->wt, g.K * p->esz))) return fail(st);
+    if (p->dtype == JUBIK_F32) {
+      std::vector<float> bf(b.begin(), b.end());
+      if ((st = cuda_status(cudaMemcpy(p->wt, bf.data(), g.K * 4, cudaMemcpyHostToDevice),
+                            "upload weights")))
+        return fail(st);
+    } else {
+      if ((st = cuda_status(cudaMemcpy(p->wt, b.data(), g.K * 8, cudaMemcpyHostToDevice),
+                            "upload weights")))
+        return fail(st);
+    }
+  }
+  if ((st = fft1d_init(&p->fft, g.P))) return fail(st);
+  p->tw = p->dtype == JUBIK_F32 ? p->fft.tw32 : p->fft.tw64;
+  if (p->path == JUBIK_PATH_FUSED) {
+    if ((st = p->alloc(&p->hmain, (size_t)units * g.P * (g.P / 2) * csz))) return fail(st);
+    if ((st = p->alloc(&p->hnyq, (size_t)units * g.P * csz))) return fail(st);
+  } else {
+    if ((st = p->alloc(&p->hfull, (size_t)units * g.P * g.P * csz))) return fail(st);
+    const int64_t n2p = (int64_t)g.n * g.n;
+    if ((st = p->alloc(&p->zs, (size_t)g.E * n2p * g.P * g.P * csz))) return fail(st);
+    // bound the per-chunk unit buffer to ~2 GiB
+    const size_t per_module = (size_t)g.E * n2p * g.P * g.P * csz;
+    p->zu_modules = (int)std::max<size_t>(1, std::min<size_t>(g.M, (2ull << 30) / per_module));
+    if ((st = p->alloc(&p->zu, per_module * p->zu_modules))) return fail(st);
+  }
+  if ((st = p->alloc(&p->conv, img * p->esz))) return fail(st);
+  if ((st = p->alloc(&p->conv_v, img * p->esz))) return fail(st);
+  if ((st = p->alloc(&p->resid, img * p->esz))) return fail(st);
+  if ((st = p->alloc(&p->lam, img * p->esz))) return fail(st);
+  if ((st = p->alloc((void**)&p->ridx, img * sizeof(int32_t)))) return fail(st);
+  if ((st = p->alloc((void**)&p->rlist, img * sizeof(int64_t)))) return fail(st);
+  if ((st = p->alloc((void**)&p->partials, 2 * energy_partials_count() * sizeof(double))))
+    return fail(st);
+  if ((st = p->alloc((void**)&p->counter, sizeof(unsigned int)))) return fail(st);
+  if ((st = cuda_status(cudaMemset(p->counter, 0, sizeof(unsigned int)), "memset counter")))
+    return fail(st);
+  if (img > 0x7fffffffLL) {
+    delete p;
+    set_error("more than 2^31 image pixels per plan");
+    return JUBIK_ERR_UNSUPPORTED;
+  }
+  // default: everything read out, unit exposure
+  k_iota<<<blocks_for(img), 256>>>(p->ridx, p->rlist, img);
+  if ((st = cuda_status(cudaGetLastError(), "k_iota"))) return fail(st);
+  if ((st = cuda_status(cudaDeviceSynchronize(), "plan set-up"))) return fail(st);
+  p->readout_sizes.assign(g.M, (int64_t)g.E * g.pixels());
+  p->readout_total = img;
+  *out = p;
+  return JUBIK_OK;
+}
+
+int jubik_plan_destroy(jubik_plan* plan) {
+  if (!plan) return JUBIK_OK;
+  cudaDeviceSynchronize();
+  delete plan;
+  return JUBIK_OK;
+}
+
+int jubik_plan_workspace_bytes(const jubik_plan* plan, int64_t* bytes) {
+  JUBIK_TRY(check_plan(plan));
+  if (bytes) *bytes = (int64_t)plan->bytes;
+  return JUBIK_OK;
+}
+
+int jubik_plan_path(const jubik_plan* plan, int32_t* path) {
+  JUBIK_TRY(check_plan(plan));
+  if (path) *path = plan->path;
+  return JUBIK_OK;
+}
+
+int jubik_plan_set_psf(jubik_plan* p, const void* psf, int32_t layout, int32_t e_broadcast,
+                       void* stream) {
+  JUBIK_TRY(check_plan(p));
+  if (!psf || (layout != JUBIK_PSF_PRECUT && layout != JUBIK_PSF_FULL)) {
+    set_error("psf must be non-NULL with a valid layout");
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  const Geom& g = p->g;
+  if (layout == JUBIK_PSF_FULL) {
+    const int kcx = (g.nx - 2 * g.dx) / 2, kcy = (g.ny - 2 * g.dx) / 2;
+    if (kcx <= 0 || kcy <= 0 || g.nx - 2 * kcx != g.K || g.ny - 2 * kcy != g.K) {
+      set_error("the kernel cut [%d:-%d] of convolve.py:107-111 does not give a %d x %d window "
+                "(needs n_patches >= 3 and an even field-minus-window)",
+                kcx, kcx, g.K, g.K);
+      return JUBIK_ERR_INVALID_ARGUMENT;
+    }
+  }
+  cudaStream_t s = S(stream);
+  const int64_t units = g.units();
+  const size_t per = (size_t)g.P * g.P * sizeof(double2);
+  int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(units, (int64_t)((512ull << 20) / per)));
+  void* buf = nullptr;
+  double* sums = nullptr;
+  JUBIK_TRY_CUDA(cudaMallocAsync(&buf, per * chunk, s));
+  JUBIK_TRY_CUDA(cudaMallocAsync((void**)&sums, sizeof(double) * chunk, s));
+  int st = JUBIK_OK;
+  for (int64_t u0 = 0; u0 < units && st == JUBIK_OK; u0 += chunk) {
+    const int64_t nu = std::min(chunk, units - u0);
+    st = p->dtype == JUBIK_F32
+             ? psf_to_cplx<float>(g, psf, layout, e_broadcast, u0, nu, sums, buf, s)
+             : psf_to_cplx<double>(g, psf, layout, e_broadcast, u0, nu, sums, buf, s);
+    if (st) break;
+    st = fft2_batched<double>(p->fft, p->fft, buf, nu, false, s);
+    if (st) break;
+    st = p->dtype == JUBIK_F32
+             ? spectra_store<float>(g, buf, u0, nu, p->hfull, p->hmain, p->hnyq, s)
+             : spectra_store<double>(g, buf, u0, nu, p->hfull, p->hmain, p->hnyq, s);
+  }
+  cudaFreeAsync(buf, s);
+  cudaFreeAsync(sums, s);
+  JUBIK_TRY(st);
+  p->psf_set = true;
+  p->lam_valid = false;
+  return cuda_status(cudaGetLastError(), "set_psf");
+}
+
+int jubik_plan_set_exposure(jubik_plan* p, const void* exposure, const uint8_t* readmask,
+                            void* stream) {
+  JUBIK_TRY(check_plan(p));
+  cudaStream_t s = S(stream);
+  const Geom& g = p->g;
+  const int64_t img = image_elems(p);
+  if (exposure) {
+    if (!p->eps) JUBIK_TRY(p->alloc(&p->eps, img * p->esz));
+    JUBIK_TRY_CUDA(cudaMemcpyAsync(p->eps, exposure, img * p->esz, cudaMemcpyDeviceToDevice, s));
+  } else if (p->eps) {
+    // back to unit exposure
+    for (auto it = p->allocs.begin(); it != p->allocs.end(); ++it)
+      if (*it == p->eps) {
+        p->allocs.erase(it);
+        break;
+      }
+    cudaFree(p->eps);
+    p->eps = nullptr;
+  }
+  std::vector<int64_t> sizes(g.M, 0);
+  if (!readmask) {
+    k_iota<<<blocks_for(img), 256, 0, s>>>(p->ridx, p->rlist, img);
+    JUBIK_TRY_CUDA(cudaGetLastError());
+    for (int m = 0; m < g.M; ++m) sizes[m] = (int64_t)g.E * g.pixels();
+  } else {
+    const int64_t nb = (img + kScanBlock - 1) / kScanBlock;
+    int32_t* counts = nullptr;
+    int64_t* offsets = nullptr;
+    JUBIK_TRY_CUDA(cudaMallocAsync((void**)&counts, sizeof(int32_t) * nb, s));
+    JUBIK_TRY_CUDA(cudaMallocAsync((void**)&offsets, sizeof(int64_t) * (nb + 1), s));
+    k_mask_counts<<<(unsigned)nb, 256, 0, s>>>(readmask, img, counts);
+    k_scan_counts<<<1, 1, 0, s>>>(counts, nb, offsets);
+    k_mask_compact<<<(unsigned)nb, 256, 0, s>>>(readmask, img, offsets, p->ridx, p->rlist);
+    JUBIK_TRY_CUDA(cudaGetLastError());
+    // per-module sizes (host count of the uploaded mask; one-off set-up work)
+    const int64_t per_module = (int64_t)g.E * g.pixels();
+    JUBIK_TRY_CUDA(cudaStreamSynchronize(s));
+    std::vector<uint8_t> hmask(img);
+    JUBIK_TRY_CUDA(cudaMemcpy(hmask.data(), readmask, img, cudaMemcpyDeviceToHost));
+    for (int m = 0; m < g.M; ++m) {
+      int64_t c = 0;
+      const uint8_t* mm = hmask.data() + m * per_module;
+      for (int64_t i = 0; i < per_module; ++i) c += mm[i] ? 1 : 0;
+      sizes[m] = c;
+    }
+    cudaFreeAsync(counts, s);
+    cudaFreeAsync(offsets, s);
+  }
+  JUBIK_TRY_CUDA(cudaStreamSynchronize(s));
+  p->readout_sizes = sizes;
+  p->readout_total = 0;
+  for (int64_t v : sizes) p->readout_total += v;
+  p->exposure_set = true;
+  p->data_set = false;
+  p->lam_valid = false;
+  return JUBIK_OK;
+}
+
+int jubik_plan_readout_sizes(const jubik_plan* p, int64_t* per_module, int64_t* total) {
+  JUBIK_TRY(check_plan(p));
+  if (per_module)
+    for (int m = 0; m < p->g.M; ++m) per_module[m] = p->readout_sizes[m];
+  if (total) *total = p->readout_total;
+  return JUBIK_OK;
+}
+
+int jubik_plan_readout_index(const jubik_plan* p, const int64_t** device_index) {
+  JUBIK_TRY(check_plan(p));
+  if (device_index) *device_index = p->rlist;
+  return JUBIK_OK;
+}
+
+int jubik_plan_set_data(jubik_plan* p, const int32_t* counts, void* stream) {
+  JUBIK_TRY(check_plan(p));
+  if (!counts) {
+    set_error("counts is NULL");
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  if (!p->data) JUBIK_TRY(p->alloc((void**)&p->data, image_elems(p) * sizeof(int32_t)));
+  JUBIK_TRY_CUDA(cudaMemcpyAsync(p->data, counts, p->readout_total * sizeof(int32_t),
+                                 cudaMemcpyDeviceToDevice, S(stream)));
+  p->data_set = true;
+  return JUBIK_OK;
+}
+
+int jubik_psf_forward(jubik_plan* p, const void* x, void* out, void* stream) {
+  JUBIK_TRY(check_plan(p));
+  JUBIK_TRY(need(p->psf_set, "PSF"));
+  return do_forward(p, x, out, 1.0, S(stream));
+}
+
+int jubik_psf_adjoint(jubik_plan* p, const void* cot, void* out_x, void* stream) {
+  JUBIK_TRY(check_plan(p));
+  JUBIK_TRY(need(p->psf_set, "PSF"));
+  return do_adjoint(p, cot, out_x, 1.0, S(stream));
+}
+
+int jubik_response_forward(jubik_plan* p, const void* x, void* out_readout, void* stream) {
+  JUBIK_TRY(check_plan(p));
+  JUBIK_TRY(need(p->psf_set, "PSF"));
+  cudaStream_t s = S(stream);
+  JUBIK_TRY(do_forward(p, x, p->conv, p->desc.pixel_area, s));
+  return p->dtype == JUBIK_F32
+             ? readout_gather<float>(p->conv, p->eps, p->rlist, p->readout_total, out_readout, s)
+             : readout_gather<double>(p->conv, p->eps, p->rlist, p->readout_total, out_readout, s);
+}
+
+int jubik_response_jvp(jubik_plan* p, const void* t, void* out_readout, void* stream) {
+  return jubik_response_forward(p, t, out_readout, stream);
+}
+
+int jubik_response_vjp(jubik_plan* p, const void* cot_readout, void* out_x, void* stream) {
+  JUBIK_TRY(check_plan(p));
+  JUBIK_TRY(need(p->psf_set, "PSF"));
+  cudaStream_t s = S(stream);
+  JUBIK_TRY_CUDA(cudaMemsetAsync(p->resid, 0, image_elems(p) * p->esz, s));
+  JUBIK_TRY(p->dtype == JUBIK_F32
+                ? readout_scatter<float>(cot_readout, p->eps, p->rlist, p->readout_total,
+                                         p->resid, s)
+                : readout_scatter<double>(cot_readout, p->eps, p->rlist, p->readout_total,
+                                          p->resid, s));
+  return do_adjoint(p, p->resid, out_x, p->desc.pixel_area, s);
+}
+
+int jubik_poisson_energy_grad(jubik_plan* p, const void* x, double* energy, void* grad_x,
+                              void* stream) {
+  JUBIK_TRY(check_plan(p));
+  JUBIK_TRY(need(p->psf_set, "PSF"));
+  JUBIK_TRY(need(p->data_set, "data"));
+  cudaStream_t s = S(stream);
+  JUBIK_TRY(do_forward(p, x, p->conv, p->desc.pixel_area, s));
+  const int64_t img = image_elems(p);
+  JUBIK_TRY(p->dtype == JUBIK_F32
+                ? poisson_image<float>(p->conv, p->eps, p->ridx, p->data, img, nullptr, p->lam,
+                                       grad_x ? p->resid : nullptr, p->partials, p->counter,
+                                       energy, s)
+                : poisson_image<double>(p->conv, p->eps, p->ridx, p->data, img, nullptr, p->lam,
+                                        grad_x ? p->resid : nullptr, p->partials, p->counter,
+                                        energy, s));
+  p->lam_valid = true;
+  if (!grad_x) return JUBIK_OK;
+  return do_adjoint(p, p->resid, grad_x, p->desc.pixel_area, s);
+}
+
+int jubik_metric_apply(jubik_plan* p, const void* x, const void* v, void* out, void* stream) {
+  JUBIK_TRY(check_plan(p));
+  JUBIK_TRY(need(p->psf_set, "PSF"));
+  cudaStream_t s = S(stream);
+  const int64_t img = image_elems(p);
+  if (x) {
+    JUBIK_TRY(do_forward(p, x, p->conv, p->desc.pixel_area, s));
+    // lam = eps * conv (read-out pixels are the only ones the weights use)
+    if (p->eps) {
+      JUBIK_TRY(p->dtype == JUBIK_F32
+                    ? elementwise_op<float>(3, p->conv, p->eps, nullptr, img, p->lam, s)
+                    : elementwise_op<double>(3, p->conv, p->eps, nullptr, img, p->lam, s));
+    } else {
+      JUBIK_TRY_CUDA(
+          cudaMemcpyAsync(p->lam, p->conv, img * p->esz, cudaMemcpyDeviceToDevice, s));
+    }
+    p->lam_valid = true;
+  }
+  JUBIK_TRY(need(p->lam_valid, "lambda (call with x or after poisson_energy_grad)"));
+  JUBIK_TRY(do_forward(p, v, p->conv_v, p->desc.pixel_area, s));
+  JUBIK_TRY(p->dtype == JUBIK_F32
+                ? metric_weights<float>(p->conv_v, p->eps, p->ridx, p->lam, img, p->resid, s)
+                : metric_weights<double>(p->conv_v, p->eps, p->ridx, p->lam, img, p->resid, s));
+  return do_adjoint(p, p->resid, out, p->desc.pixel_area, s);
+}
+
+int jubik_poisson_energy(const void* lam, const int32_t* data, int64_t n, int32_t dtype,
+                         double* energy, void* grad, void* stream) {
+  if (!lam || !data || !energy || n < 0) {
+    set_error("invalid argument");
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  cudaStream_t s = S(stream);
+  const int nb = energy_partials_count();
+  double* partials = nullptr;
+  unsigned int* counter = nullptr;
+  JUBIK_TRY_CUDA(cudaMallocAsync((void**)&partials, 2 * nb * sizeof(double), s));
+  JUBIK_TRY_CUDA(cudaMallocAsync((void**)&counter, sizeof(unsigned int), s));
+  JUBIK_TRY_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned int), s));
+  int st = dtype == JUBIK_F32 ? poisson_vec<float>(lam, data, n, partials, counter, energy, grad, s)
+                              : poisson_vec<double>(lam, data, n, partials, counter, energy, grad,
+                                                    s);
+  cudaFreeAsync(partials, s);
+  cudaFreeAsync(counter, s);
+  return st;
+}
+
+int jubik_elementwise(int32_t op, const void* a, const void* b, const int32_t* data, int64_t n,
+                      int32_t dtype, void* out, void* stream) {
+  if (op < 0 || op > 3 || !a || !out || (op != 2 && !b) || (op == 2 && !data)) {
+    set_error("invalid elementwise arguments");
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  return dtype == JUBIK_F32 ? elementwise_op<float>(op, a, b, data, n, out, S(stream))
+                            : elementwise_op<double>(op, a, b, data, n, out, S(stream));
+}
+
+int jubik_readout_gather(const void* img, const void* eps, const int64_t* idx, int64_t nread,
+                         int32_t dtype, void* out, void* stream) {
+  return dtype == JUBIK_F32 ? readout_gather<float>(img, eps, idx, nread, out, S(stream))
+                            : readout_gather<double>(img, eps, idx, nread, out, S(stream));
+}
+
+int jubik_readout_scatter(const void* vec, const void* eps, const int64_t* idx, int64_t nread,
+                          int32_t dtype, void* img, void* stream) {
+  return dtype == JUBIK_F32 ? readout_scatter<float>(vec, eps, idx, nread, img, S(stream))
+                            : readout_scatter<double>(vec, eps, idx, nread, img, S(stream));
+}
+
+int jubik_slice_patches(const void* x, int64_t batch, int32_t nx, int32_t ny, int32_t n,
+                        int32_t additional_margin, int32_t dtype, void* out, void* stream) {
+  return dtype == JUBIK_F32
+             ? slice_patches_op<float>(x, batch, nx, ny, n, additional_margin, out, S(stream))
+             : slice_patches_op<double>(x, batch, nx, ny, n, additional_margin, out, S(stream));
+}
+
+int jubik_slice_patches_adjoint(const void* patches, int64_t batch, int32_t nx, int32_t ny,
+                                int32_t n, int32_t additional_margin, int32_t dtype, void* out,
+                                void* stream) {
+  return dtype == JUBIK_F32 ? slice_patches_adjoint_op<float>(patches, batch, nx, ny, n,
+                                                              additional_margin, out, S(stream))
+                            : slice_patches_adjoint_op<double>(patches, batch, nx, ny, n,
+                                                               additional_margin, out, S(stream));
+}
+
+int jubik_convolve2d(const void* kernel, int64_t bk, const void* signal, int64_t bs, int32_t h,
+                     int32_t w, double dvol, int32_t dtype, void* out, void* stream) {
+  if (!kernel || !signal || !out || bk < 1 || bs < 1 || h < 1 || w < 1 || bs % bk != 0) {
+    set_error("convolve2d: invalid shapes (kernel batch must divide the signal batch)");
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  cudaStream_t s = S(stream);
+  Fft1D fh, fw;
+  JUBIK_TRY(fft1d_init(&fh, h));
+  int st = fft1d_init(&fw, w);
+  if (st) {
+    fft1d_free(&fh);
+    return st;
+  }
+  const size_t csz = dtype == JUBIK_F32 ? 8 : 16;
+  const int64_t hw = (int64_t)h * w;
+  void* zk = nullptr;
+  void* zs = nullptr;
+  st = cuda_status(cudaMallocAsync(&zk, csz * bk * hw, s), "cudaMallocAsync");
+  if (!st) st = cuda_status(cudaMallocAsync(&zs, csz * bs * hw, s), "cudaMallocAsync");
+  if (!st)
+    st = dtype == JUBIK_F32 ? convolve2d_run<float>(kernel, bk, signal, bs, hw, dvol, fh, fw, zk, zs, out, s)
+                            : convolve2d_run<double>(kernel, bk, signal, bs, hw, dvol, fh, fw, zk, zs, out, s);
+  if (zk) cudaFreeAsync(zk, s);
+  if (zs) cudaFreeAsync(zs, s);
+  cudaStreamSynchronize(s);
+  fft1d_free(&fh);
+  fft1d_free(&fw);
+  return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,96 @@
+// Register-resident small DFTs (sizes 1, 2, 3, 4, 6, 8, 12, 16) in natural
+// order, fully unrolled at compile time.  Composite sizes use one level of
+// Cooley-Tukey, N = N1 * N2 with n = N2*n1 + n2 and k = k1 + N1*k2:
+//   X[k1 + N1 k2] = sum_n2 w_N2^(n2 k2) w_N^(n2 k1) sum_n1 x[N2 n1 + n2] w_N1^(n1 k1)
+#pragma once
+
+#include "jubik_common.cuh"
+
+namespace jubik {
+
+template <int N, bool INV, typename T> struct Dft;
+
+template <bool INV, typename T> struct Dft<1, INV, T> {
+  __device__ __forceinline__ static void run(cx<T>*) {}
+};
+
+template <bool INV, typename T> struct Dft<2, INV, T> {
+  __device__ __forceinline__ static void run(cx<T>* v) {
+    cx<T> a = v[0];
+    v[0] = cadd<T>(a, v[1]);
+    v[1] = csub<T>(a, v[1]);
+  }
+};
+
+template <bool INV, typename T> struct Dft<3, INV, T> {
+  __device__ __forceinline__ static void run(cx<T>* v) {
+    constexpr T s3 = (T)0.8660254037844386467637232;  // sin(2 pi / 3)
+    cx<T> t1 = cadd<T>(v[1], v[2]);
+    cx<T> t2 = mkc<T>(v[0].x - (T)0.5 * t1.x, v[0].y - (T)0.5 * t1.y);
+    cx<T> t3 = mkc<T>(s3 * (v[1].x - v[2].x), s3 * (v[1].y - v[2].y));
+    v[0] = cadd<T>(v[0], t1);
+    if (INV) {
+      v[1] = cadd<T>(t2, cmul_i<T>(t3));
+      v[2] = csub<T>(t2, cmul_i<T>(t3));
+    } else {
+      v[1] = csub<T>(t2, cmul_i<T>(t3));
+      v[2] = cadd<T>(t2, cmul_i<T>(t3));
+    }
+  }
+};
+
+template <bool INV, typename T> struct Dft<4, INV, T> {
+  __device__ __forceinline__ static void run(cx<T>* v) {
+    cx<T> t0 = cadd<T>(v[0], v[2]);
+    cx<T> t1 = csub<T>(v[0], v[2]);
+    cx<T> t2 = cadd<T>(v[1], v[3]);
+    cx<T> t3 = csub<T>(v[1], v[3]);
+    v[0] = cadd<T>(t0, t2);
+    v[2] = csub<T>(t0, t2);
+    if (INV) {
+      v[1] = cadd<T>(t1, cmul_i<T>(t3));
+      v[3] = csub<T>(t1, cmul_i<T>(t3));
+    } else {
+      v[1] = csub<T>(t1, cmul_i<T>(t3));
+      v[3] = cadd<T>(t1, cmul_i<T>(t3));
+    }
+  }
+};
+
+template <int N1, int N2, bool INV, typename T>
+__device__ __forceinline__ void dft_ct(cx<T>* v) {
+  constexpr int N = N1 * N2;
+  cx<T> y[N];
+  sfor<N2>([&](auto n2c) {
+    constexpr int n2 = decltype(n2c)::value;
+    cx<T> t[N1];
+    sfor<N1>([&](auto n1c) { t[decltype(n1c)::value] = v[N2 * decltype(n1c)::value + n2]; });
+    Dft<N1, INV, T>::run(t);
+    sfor<N1>([&](auto k1c) {
+      constexpr int k1 = decltype(k1c)::value;
+      y[k1 * N2 + n2] = twc<N, n2 * k1, INV, T>(t[k1]);
+    });
+  });
+  sfor<N1>([&](auto k1c) {
+    constexpr int k1 = decltype(k1c)::value;
+    cx<T> t[N2];
+    sfor<N2>([&](auto n2c) { t[decltype(n2c)::value] = y[k1 * N2 + decltype(n2c)::value]; });
+    Dft<N2, INV, T>::run(t);
+    sfor<N2>([&](auto k2c) { v[k1 + N1 * decltype(k2c)::value] = t[decltype(k2c)::value]; });
+  });
+}
+
+template <bool INV, typename T> struct Dft<6, INV, T> {
+  __device__ __forceinline__ static void run(cx<T>* v) { dft_ct<3, 2, INV, T>(v); }
+};
+template <bool INV, typename T> struct Dft<8, INV, T> {
+  __device__ __forceinline__ static void run(cx<T>* v) { dft_ct<4, 2, INV, T>(v); }
+};
+template <bool INV, typename T> struct Dft<12, INV, T> {
+  __device__ __forceinline__ static void run(cx<T>* v) { dft_ct<3, 4, INV, T>(v); }
+};
+template <bool INV, typename T> struct Dft<16, INV, T> {
+  __device__ __forceinline__ static void run(cx<T>* v) { dft_ct<4, 4, INV, T>(v); }
+};
+
+}  // namespace jubik

@@ -1,0 +1,139 @@
+// Internal declarations shared by the translation units of libjubik_gb300.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/jubik_gb300.h"
+
+namespace jubik {
+
+// ------------------------------------------------------------------ errors
+void set_error(const char* fmt, ...);
+int cuda_status(cudaError_t err, const char* what);
+
+#define JUBIK_TRY_CUDA(expr)                                   \
+  do {                                                         \
+    cudaError_t _e = (expr);                                   \
+    if (_e != cudaSuccess) return ::jubik::cuda_status(_e, #expr); \
+  } while (0)
+
+#define JUBIK_TRY(expr)              \
+  do {                               \
+    int _s = (expr);                 \
+    if (_s != JUBIK_OK) return _s;   \
+  } while (0)
+
+// ------------------------------------------------------------------ geometry
+// Patch geometry of jubik/convolve.py:43-63 / :102-143 (square patches).
+struct Geom {
+  int M = 0, E = 0, nx = 0, ny = 0, n = 0;
+  int dx = 0, margin = 0, half = 0;  // half = dx // 2 (the slice pad)
+  int K = 0, P = 0;                  // window 2*dx, FFT side 2*dx + 2*margin
+  int sr_max = 0, sc_max = 0;        // clamp of dynamic_slice starts
+  int64_t units() const { return (int64_t)M * E * n * n; }
+  int64_t pixels() const { return (int64_t)nx * ny; }
+};
+
+// ------------------------------------------------------------------ plain FFT
+constexpr int kMaxStages = 24;
+constexpr int kMaxGenericRadix = 64;
+struct FftStages {
+  int n = 0;
+  int r[kMaxStages] = {0};
+};
+
+// Mixed-radix Stockham plan for complex length-L transforms.  Twiddles
+// w_L^t = exp(-2 pi i t / L) are evaluated once in long double on the host
+// and rounded once to each precision.
+struct Fft1D {
+  int L = 0;
+  FftStages st;
+  void* tw32 = nullptr;  // float2[L]
+  void* tw64 = nullptr;  // double2[L]
+};
+int fft1d_init(Fft1D* f, int L);
+void fft1d_free(Fft1D* f);
+bool fft_length_supported(int L);
+
+// In-place batched complex FFT of nseq sequences of length f.L; sequence q
+// starts at (q / nb) * sa + (q % nb) * sb, element i at + i * se (elements).
+template <typename T>
+int fft_batched(const Fft1D& f, void* data, int64_t nseq, int nb, int64_t sa, int64_t sb,
+                int64_t se, bool inverse, double scale, cudaStream_t s);
+
+// 2-D FFT over the last two axes of a (batch, h, w) complex array.
+template <typename T>
+int fft2_batched(const Fft1D& fh, const Fft1D& fw, void* data, int64_t batch, bool inverse,
+                 cudaStream_t s);
+
+// ------------------------------------------------------------------ fused path
+bool fused_supported(int P, int dtype);
+size_t fused_smem_bytes(int P, int dtype);
+struct FusedLaunch {
+  const void* in;       // forward: sky (E,nx,ny); adjoint: cotangent (M,E,nx,ny)
+  void* out;            // forward: (M,E,nx,ny) accumulator; adjoint: (E,nx,ny)
+  const void* hmain;    // (units, P, P/2) complex, rows in 4-step order
+  const void* hnyq;     // (units, P) complex: the kx = P/2 column
+  const void* tw;       // (P) complex twiddles
+  const void* wt;       // (2*dx) bilinear weight vector
+  double scale;
+};
+int fused_forward(const Geom& g, int dtype, const FusedLaunch& a, cudaStream_t s);
+int fused_adjoint(const Geom& g, int dtype, const FusedLaunch& a, cudaStream_t s);
+int fused_prepare_attributes();
+
+// ------------------------------------------------------------------ ops
+template <typename T>
+int psf_to_cplx(const Geom& g, const void* psf, int layout, int e_broadcast, int64_t u0,
+                int64_t nu, double* sums, void* buf, cudaStream_t s);
+template <typename T>
+int spectra_store(const Geom& g, const void* buf, int64_t u0, int64_t nu, void* hfull,
+                  void* hmain, void* hnyq, cudaStream_t s);
+template <typename T>
+int plain_sky_patches(const Geom& g, const void* x, const void* wt, void* zs, cudaStream_t s);
+template <typename T>
+int plain_mul_modules(const Geom& g, const void* zs, const void* hfull, int m0, int nm, void* zu,
+                      cudaStream_t s);
+template <typename T>
+int plain_overlap_gather(const Geom& g, const void* zu, int m0, int nm, double scale, void* out,
+                         cudaStream_t s);
+template <typename T>
+int plain_cot_patches(const Geom& g, const void* cot, int m0, int nm, void* zu, cudaStream_t s);
+template <typename T>
+int plain_mulconj_accum(const Geom& g, const void* zu, const void* hfull, int m0, int nm,
+                        bool first, void* zs, cudaStream_t s);
+template <typename T>
+int plain_grad_gather(const Geom& g, const void* zs, const void* wt, double scale, void* out,
+                      cudaStream_t s);
+
+template <typename T>
+int slice_patches_op(const void* x, int64_t batch, int nx, int ny, int n, int dr, void* out,
+                     cudaStream_t s);
+template <typename T>
+int slice_patches_adjoint_op(const void* patches, int64_t batch, int nx, int ny, int n, int dr,
+                             void* out, cudaStream_t s);
+
+// response epilogues / prologues over the (M,E,nx,ny) image
+template <typename T>
+int readout_gather(const void* img, const void* eps, const int64_t* idx, int64_t nread,
+                   void* out, cudaStream_t s);
+template <typename T>
+int readout_scatter(const void* vec, const void* eps, const int64_t* idx, int64_t nread,
+                    void* img, cudaStream_t s);
+template <typename T>
+int poisson_image(const void* conv, const void* eps, const int32_t* ridx, const int32_t* data,
+                  int64_t npix, void* lam_out_readout, void* lam_cache, void* resid,
+                  double* partials, unsigned int* counter, double* energy, cudaStream_t s);
+template <typename T>
+int metric_weights(const void* conv_v, const void* eps, const int32_t* ridx, const void* lam_cache,
+                   int64_t npix, void* resid, cudaStream_t s);
+template <typename T>
+int poisson_vec(const void* lam, const int32_t* data, int64_t n, double* partials,
+                unsigned int* counter, double* energy, void* grad, cudaStream_t s);
+template <typename T>
+int elementwise_op(int op, const void* a, const void* b, const int32_t* d, int64_t n, void* out,
+                   cudaStream_t s);
+int energy_partials_count();
+
+}  // namespace jubik

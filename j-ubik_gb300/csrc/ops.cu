@@ -1,0 +1,715 @@
+// Gather/scatter, spectrum preparation, unfused-path and likelihood kernels.
+#include <cmath>
+#include <cstdio>
+
+#include "fft_codelets.cuh"
+#include "internal.h"
+
+namespace jubik {
+
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kRedBlocks = 1024;  // fixed grid of the energy reductions
+
+inline unsigned grid_for(int64_t n, int per = kBlock) {
+  int64_t b = (n + per - 1) / per;
+  if (b > 1048576) b = 1048576;  // grid-stride beyond this
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+__device__ __forceinline__ int img_row_base(int p, int dx, int smax, int half, int margin) {
+  return min(p * dx, smax) - half - margin;
+}
+
+// --------------------------------------------------------------- PSF prep
+// One block per unit hu = (m*n^2 + k)*E + e.  Reads the (2dx)^2 window (from
+// the pre-cut or the full-field kernel: fftshift + centre cut of
+// convolve.py:107-111), sums it in FP64, and writes the normalised kernel
+// into a P x P complex FP64 array at the ifftshift(pad) positions
+// ((a - dx) mod P, (b - dx) mod P) of convolve.py:118-131.
+template <typename T>
+__global__ void k_psf_to_cplx(const T* __restrict__ psf, int layout, int e_bcast, int E, int n2p,
+                              int nx, int ny, int dx, int P, int64_t u0, double* __restrict__ sums,
+                              double2* __restrict__ buf) {
+  const int64_t hu = u0 + blockIdx.x;
+  const int e = (int)(hu % E);
+  const int64_t mk = hu / E;
+  const int esrc = e_bcast ? 0 : e;
+  const int Esrc = e_bcast ? 1 : E;
+  const int K = 2 * dx;
+  __shared__ double red[kBlock];
+  auto fetch = [&](int a, int b) -> double {
+    if (layout == JUBIK_PSF_PRECUT) {
+      return (double)psf[((mk * Esrc + esrc) * K + a) * (int64_t)K + b];
+    }
+    const int kcx = (nx - 2 * dx) / 2, kcy = (ny - 2 * dx) / 2;
+    int ia = (kcx + a - nx / 2) % nx;
+    if (ia < 0) ia += nx;
+    int ib = (kcy + b - ny / 2) % ny;
+    if (ib < 0) ib += ny;
+    return (double)psf[((mk * Esrc + esrc) * nx + ia) * (int64_t)ny + ib];
+  };
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < K * K; i += blockDim.x) acc += fetch(i / K, i % K);
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  const double sum = red[0];
+  if (threadIdx.x == 0) sums[blockIdx.x] = sum;
+  double2* dst = buf + (int64_t)blockIdx.x * P * P;
+  for (int i = threadIdx.x; i < P * P; i += blockDim.x) dst[i] = make_double2(0.0, 0.0);
+  __syncthreads();
+  for (int i = threadIdx.x; i < K * K; i += blockDim.x) {
+    const int a = i / K, b = i % K;
+    int y = (a - dx) % P;
+    if (y < 0) y += P;
+    int x = (b - dx) % P;
+    if (x < 0) x += P;
+    dst[y * P + x] = make_double2(fetch(a, b) / sum, 0.0);
+  }
+}
+
+// Spectrum (FP64, natural order) -> plan storage in dtype T, scaled by 1/P^2
+// (the 1/N of ifftn folded in).  hfull: (U,P,P) for the unfused path;
+// hmain/hnyq: half-spectrum rows in the fused kernel's 4-step order.
+template <typename T>
+__global__ void k_spectra_store(const double2* __restrict__ buf, int P, int64_t u0, int64_t nu,
+                                cx<T>* __restrict__ hfull, cx<T>* __restrict__ hmain,
+                                cx<T>* __restrict__ hnyq) {
+  const int H = P / 2;
+  const int L1 = P / 16;
+  const double sc = 1.0 / ((double)P * (double)P);
+  const int64_t total = nu * P * P;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ul = i / ((int64_t)P * P);
+    const int rem = (int)(i - ul * P * P);
+    const int ky = rem / P, kx = rem % P;
+    const double2 v = buf[i];
+    const cx<T> w = mkc<T>((T)(v.x * sc), (T)(v.y * sc));
+    const int64_t hu = u0 + ul;
+    if (hfull) hfull[hu * P * P + rem] = w;
+    if (hmain && kx <= H) {
+      const int slot = 16 * (ky % L1) + ky / L1;
+      if (kx < H)
+        hmain[(hu * P + slot) * H + kx] = w;
+      else
+        hnyq[hu * P + slot] = w;
+    }
+  }
+}
+
+// --------------------------------------------------------------- plain path
+template <typename T>
+__global__ void k_plain_sky_patches(const T* __restrict__ x, const T* __restrict__ wt, int E,
+                                    int n, int nx, int ny, int dx, int margin, int half,
+                                    int sr_max, int sc_max, int P, cx<T>* __restrict__ zs) {
+  const int n2p = n * n;
+  const int64_t total = (int64_t)E * n2p * P * P;
+  const int K = 2 * dx;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ek = i / ((int64_t)P * P);
+    const int rem = (int)(i - ek * P * P);
+    const int y = rem / P, xx = rem % P;
+    const int k = (int)(ek % n2p), e = (int)(ek / n2p);
+    const int rb = img_row_base(k % n, dx, sr_max, half, margin);
+    const int cb = img_row_base(k / n, dx, sc_max, half, margin);
+    const int ya = y - margin, xa = xx - margin, row = rb + y, col = cb + xx;
+    T v = (T)0;
+    if (ya >= 0 && ya < K && xa >= 0 && xa < K && row >= 0 && row < nx && col >= 0 && col < ny)
+      v = (wt[ya] * wt[xa]) * x[((int64_t)e * nx + row) * ny + col];
+    zs[i] = mkc<T>(v, (T)0);
+  }
+}
+
+template <typename T>
+__global__ void k_plain_mul_modules(const cx<T>* __restrict__ zs, const cx<T>* __restrict__ hfull,
+                                    int m0, int nm, int E, int n2p, int P,
+                                    cx<T>* __restrict__ zu) {
+  const int64_t pp = (int64_t)P * P;
+  const int64_t total = (int64_t)nm * E * n2p * pp;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t unit = i / pp;
+    const int64_t rem = i - unit * pp;
+    const int k = (int)(unit % n2p);
+    const int64_t me = unit / n2p;
+    const int e = (int)(me % E);
+    const int m = m0 + (int)(me / E);
+    const int64_t hu = ((int64_t)m * n2p + k) * E + e;
+    zu[i] = cmul<T>(zs[((int64_t)e * n2p + k) * pp + rem], hfull[hu * pp + rem]);
+  }
+}
+
+// Deterministic overlap-add (transpose of the margin slice, convolve.py:135-144):
+// every output pixel sums the <= 9 patch outputs that cover it, in patch
+// order, with Kahan compensation.
+template <typename T>
+__global__ void k_plain_overlap_gather(const cx<T>* __restrict__ zu, int m0, int nm, int E,
+                                       int n, int nx, int ny, int dx, int margin, int half,
+                                       int sr_max, int sc_max, int P, T scale,
+                                       T* __restrict__ out) {
+  const int n2p = n * n;
+  const int64_t pp = (int64_t)P * P;
+  const int64_t total = (int64_t)nm * E * nx * ny;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i % ny);
+    const int64_t t = i / ny;
+    const int r = (int)(t % nx);
+    const int64_t me = t / nx;  // (m - m0) * E + e
+    const int tr = r + half + margin, tc = c + half + margin;
+    const int ri_hi = min(n - 1, tr / dx), ci_hi = min(n - 1, tc / dx);
+    const int ri_lo = tr - P + 1 <= 0 ? 0 : (tr - P + 1 + dx - 1) / dx;
+    const int ci_lo = tc - P + 1 <= 0 ? 0 : (tc - P + 1 + dx - 1) / dx;
+    T s = (T)0, comp = (T)0;
+    auto visit = [&](int pi, int pj) {
+      const int rb = img_row_base(pi, dx, sr_max, half, margin);
+      const int cb = img_row_base(pj, dx, sc_max, half, margin);
+      const int y = r - rb, xx = c - cb;
+      if (y < 0 || y >= P || xx < 0 || xx >= P) return;
+      const T v = zu[(me * n2p + (int64_t)pj * n + pi) * pp + (int64_t)y * P + xx].x;
+      const T yk = v - comp;
+      const T tt = s + yk;
+      comp = (tt - s) - yk;
+      s = tt;
+    };
+    for (int pj = ci_lo; pj <= ci_hi; ++pj) {
+      for (int pi = ri_lo; pi <= ri_hi; ++pi) visit(pi, pj);
+      if (ri_hi < n - 1) visit(n - 1, pj);
+    }
+    if (ci_hi < n - 1) {
+      for (int pi = ri_lo; pi <= ri_hi; ++pi) visit(pi, n - 1);
+      if (ri_hi < n - 1) visit(n - 1, n - 1);
+    }
+    const int64_t m = m0 + me / E;
+    const int e = (int)(me % E);
+    out[((m * E + e) * nx + r) * (int64_t)ny + c] = scale * s;
+  }
+}
+
+template <typename T>
+__global__ void k_plain_cot_patches(const T* __restrict__ cot, int m0, int nm, int E, int n,
+                                    int nx, int ny, int dx, int margin, int half, int sr_max,
+                                    int sc_max, int P, cx<T>* __restrict__ zu) {
+  const int n2p = n * n;
+  const int64_t pp = (int64_t)P * P;
+  const int64_t total = (int64_t)nm * E * n2p * pp;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t unit = i / pp;
+    const int rem = (int)(i - unit * pp);
+    const int y = rem / P, xx = rem % P;
+    const int k = (int)(unit % n2p);
+    const int64_t me = unit / n2p;
+    const int rb = img_row_base(k % n, dx, sr_max, half, margin);
+    const int cb = img_row_base(k / n, dx, sc_max, half, margin);
+    const int row = rb + y, col = cb + xx;
+    T v = (T)0;
+    if (row >= 0 && row < nx && col >= 0 && col < ny) {
+      const int64_t m = m0 + me / E;
+      const int e = (int)(me % E);
+      v = cot[((m * E + e) * nx + row) * (int64_t)ny + col];
+    }
+    zu[i] = mkc<T>(v, (T)0);
+  }
+}
+
+template <typename T>
+__global__ void k_plain_mulconj_accum(const cx<T>* __restrict__ zu, const cx<T>* __restrict__ hfull,
+                                      int m0, int nm, int E, int n2p, int P, int first,
+                                      cx<T>* __restrict__ zs) {
+  const int64_t pp = (int64_t)P * P;
+  const int64_t total = (int64_t)E * n2p * pp;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ek = i / pp;
+    const int64_t rem = i - ek * pp;
+    const int k = (int)(ek % n2p), e = (int)(ek / n2p);
+    cx<T> acc = first ? mkc<T>((T)0, (T)0) : zs[i];
+    for (int mm = 0; mm < nm; ++mm) {
+      const int64_t hu = ((int64_t)(m0 + mm) * n2p + k) * E + e;
+      const cx<T> z = zu[(((int64_t)mm * E + e) * n2p + k) * pp + rem];
+      acc = cadd<T>(acc, cmulc<T>(z, hfull[hu * pp + rem]));
+    }
+    zs[i] = acc;
+  }
+}
+
+template <typename T>
+__global__ void k_plain_grad_gather(const cx<T>* __restrict__ zs, const T* __restrict__ wt, int E,
+                                    int n, int nx, int ny, int dx, int margin, int half,
+                                    int sr_max, int sc_max, int P, T scale, T* __restrict__ out) {
+  const int n2p = n * n;
+  const int64_t pp = (int64_t)P * P;
+  const int K = 2 * dx;
+  const int64_t total = (int64_t)E * nx * ny;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i % ny);
+    const int64_t t = i / ny;
+    const int r = (int)(t % nx);
+    const int e = (int)(t / nx);
+    const int tr = r + half + margin, tc = c + half + margin;
+    const int ri_hi = min(n - 1, tr / dx), ci_hi = min(n - 1, tc / dx);
+    const int ri_lo = tr - P + 1 <= 0 ? 0 : (tr - P + 1 + dx - 1) / dx;
+    const int ci_lo = tc - P + 1 <= 0 ? 0 : (tc - P + 1 + dx - 1) / dx;
+    T s = (T)0, comp = (T)0;
+    auto visit = [&](int pi, int pj) {
+      const int rb = img_row_base(pi, dx, sr_max, half, margin);
+      const int cb = img_row_base(pj, dx, sc_max, half, margin);
+      const int ya = r - rb - margin, xa = c - cb - margin;
+      if (ya < 0 || ya >= K || xa < 0 || xa >= K) return;
+      const T v = (wt[ya] * wt[xa]) *
+                  zs[((int64_t)e * n2p + (int64_t)pj * n + pi) * pp +
+                     (int64_t)(ya + margin) * P + (xa + margin)].x;
+      const T yk = v - comp;
+      const T tt = s + yk;
+      comp = (tt - s) - yk;
+      s = tt;
+    };
+    for (int pj = ci_lo; pj <= ci_hi; ++pj) {
+      for (int pi = ri_lo; pi <= ri_hi; ++pi) visit(pi, pj);
+      if (ri_hi < n - 1) visit(n - 1, pj);
+    }
+    if (ci_hi < n - 1) {
+      for (int pi = ri_lo; pi <= ri_hi; ++pi) visit(pi, n - 1);
+      if (ri_hi < n - 1) visit(n - 1, n - 1);
+    }
+    out[i] = scale * s;
+  }
+}
+
+// --------------------------------------------------------------- slice_patches
+struct SliceGeom {
+  int n, nx, ny, dx, dy, hx, hy, sh, sw, rmax, cmax;
+};
+
+inline int make_slice_geom(int nx, int ny, int n, int dr, SliceGeom* g) {
+  if (n < 1 || dr < 0) {
+    set_error("n_patches_per_axis must be >= 1 and the margin >= 0");
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  g->n = n;
+  g->nx = nx;
+  g->ny = ny;
+  g->dx = (nx - 2 * dr) / n;
+  g->dy = (ny - 2 * dr) / n;
+  g->hx = g->dx / 2;
+  g->hy = g->dy / 2;
+  g->sh = 2 * g->dx + 2 * dr;
+  g->sw = 2 * g->dy + 2 * dr;
+  const int ph = nx + 2 * g->hx, pw = ny + 2 * g->hy;
+  if (g->dx < 1 || g->dy < 1 || g->sh > ph || g->sw > pw) {
+    set_error("slice window (%d x %d) does not fit the padded field (%d x %d)", g->sh, g->sw, ph,
+              pw);
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  g->rmax = ph - g->sh;
+  g->cmax = pw - g->sw;
+  return JUBIK_OK;
+}
+
+template <typename T>
+__global__ void k_slice_patches(const T* __restrict__ x, int64_t batch, SliceGeom g,
+                                T* __restrict__ out) {
+  const int n2p = g.n * g.n;
+  const int64_t total = (int64_t)n2p * batch * g.sh * g.sw;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int xx = (int)(i % g.sw);
+    int64_t t = i / g.sw;
+    const int y = (int)(t % g.sh);
+    t /= g.sh;
+    const int64_t b = t % batch;
+    const int k = (int)(t / batch);
+    const int r0 = min((k % g.n) * g.dx, g.rmax), c0 = min((k / g.n) * g.dy, g.cmax);
+    const int row = r0 + y - g.hx, col = c0 + xx - g.hy;
+    out[i] = (row >= 0 && row < g.nx && col >= 0 && col < g.ny)
+                 ? x[(b * g.nx + row) * (int64_t)g.ny + col]
+                 : (T)0;
+  }
+}
+
+template <typename T>
+__global__ void k_slice_patches_adjoint(const T* __restrict__ pt, int64_t batch, SliceGeom g,
+                                        T* __restrict__ out) {
+  const int64_t total = batch * g.nx * g.ny;
+  const int64_t ps = (int64_t)g.sh * g.sw;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i % g.ny);
+    const int64_t t = i / g.ny;
+    const int r = (int)(t % g.nx);
+    const int64_t b = t / g.nx;
+    const int tr = r + g.hx, tc = c + g.hy;
+    const int ri_hi = min(g.n - 1, tr / g.dx), ci_hi = min(g.n - 1, tc / g.dy);
+    const int ri_lo = tr - g.sh + 1 <= 0 ? 0 : (tr - g.sh + 1 + g.dx - 1) / g.dx;
+    const int ci_lo = tc - g.sw + 1 <= 0 ? 0 : (tc - g.sw + 1 + g.dy - 1) / g.dy;
+    T s = (T)0;
+    auto visit = [&](int pi, int pj) {
+      const int r0 = min(pi * g.dx, g.rmax), c0 = min(pj * g.dy, g.cmax);
+      const int y = tr - r0, xx = tc - c0;
+      if (y < 0 || y >= g.sh || xx < 0 || xx >= g.sw) return;
+      const int64_t k = (int64_t)pj * g.n + pi;
+      s += pt[(k * batch + b) * ps + (int64_t)y * g.sw + xx];
+    };
+    for (int pj = ci_lo; pj <= ci_hi; ++pj) {
+      for (int pi = ri_lo; pi <= ri_hi; ++pi) visit(pi, pj);
+      if (ri_hi < g.n - 1) visit(g.n - 1, pj);
+    }
+    if (ci_hi < g.n - 1) {
+      for (int pi = ri_lo; pi <= ri_hi; ++pi) visit(pi, g.n - 1);
+      if (ri_hi < g.n - 1) visit(g.n - 1, g.n - 1);
+    }
+    out[i] = s;
+  }
+}
+
+// --------------------------------------------------------------- readout
+template <typename T>
+__global__ void k_readout_gather(const T* __restrict__ img, const T* __restrict__ eps,
+                                 const int64_t* __restrict__ idx, int64_t nread,
+                                 T* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nread;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = idx[i];
+    out[i] = eps ? eps[p] * img[p] : img[p];
+  }
+}
+
+template <typename T>
+__global__ void k_readout_scatter(const T* __restrict__ vec, const T* __restrict__ eps,
+                                  const int64_t* __restrict__ idx, int64_t nread,
+                                  T* __restrict__ img) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nread;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = idx[i];
+    img[p] = eps ? eps[p] * vec[i] : vec[i];
+  }
+}
+
+// --------------------------------------------------------------- Poisson
+// Compensated (Kahan) accumulation in the working precision per thread, FP64
+// across threads and blocks; the last block sums the block partials in a
+// fixed order, so the total is deterministic.
+template <typename T>
+struct Kahan {
+  T s = (T)0, c = (T)0;
+  __device__ __forceinline__ void add(T v) {
+    const T y = v - c;
+    const T t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+__device__ __forceinline__ void block_reduce2(double a, double b, double* partials,
+                                              unsigned int* counter, double* energy) {
+  __shared__ double sa[kBlock], sb[kBlock];
+  __shared__ bool last;
+  sa[threadIdx.x] = a;
+  sb[threadIdx.x] = b;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      sa[threadIdx.x] += sa[threadIdx.x + w];
+      sb[threadIdx.x] += sb[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = sa[0];
+    partials[2 * blockIdx.x + 1] = sb[0];
+    __threadfence();
+    const unsigned int done = atomicAdd(counter, 1u);
+    last = (done == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    double s1 = 0.0, s2 = 0.0;
+    for (unsigned int i = 0; i < gridDim.x; ++i) {
+      s1 += ((volatile double*)partials)[2 * i];
+      s2 += ((volatile double*)partials)[2 * i + 1];
+    }
+    // H = sum(lam) - vdot(d, log(lam))
+    if (energy) energy[0] = s1 - s2;
+    *counter = 0u;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock)
+    k_poisson_image(const T* __restrict__ conv, const T* __restrict__ eps,
+                    const int32_t* __restrict__ ridx, const int32_t* __restrict__ data,
+                    int64_t npix, T* __restrict__ lam_out, T* __restrict__ lam_cache,
+                    T* __restrict__ resid, double* partials, unsigned int* counter,
+                    double* energy) {
+  Kahan<T> s_lam, s_dlog;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npix;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t r = ridx[p];
+    if (r < 0) {
+      if (resid) resid[p] = (T)0;
+      continue;
+    }
+    const T ep = eps ? eps[p] : (T)1;
+    const T lam = ep * conv[p];
+    const T d = (T)data[r];
+    s_lam.add(lam);
+    s_dlog.add(d * log(lam));
+    if (lam_out) lam_out[r] = lam;
+    if (lam_cache) lam_cache[p] = lam;
+    if (resid) resid[p] = ep * ((T)1 - d / lam);
+  }
+  block_reduce2(s_lam.value(), s_dlog.value(), partials, counter, energy);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock)
+    k_poisson_vec(const T* __restrict__ lam, const int32_t* __restrict__ data, int64_t n,
+                  double* partials, unsigned int* counter, double* energy, T* __restrict__ grad) {
+  Kahan<T> s_lam, s_dlog;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const T l = lam[i];
+    const T d = (T)data[i];
+    s_lam.add(l);
+    s_dlog.add(d * log(l));
+    if (grad) grad[i] = (T)1 - d / l;
+  }
+  block_reduce2(s_lam.value(), s_dlog.value(), partials, counter, energy);
+}
+
+template <typename T>
+__global__ void k_metric_weights(const T* __restrict__ conv_v, const T* __restrict__ eps,
+                                 const int32_t* __restrict__ ridx, const T* __restrict__ lam,
+                                 int64_t npix, T* __restrict__ resid) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npix;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    if (ridx[p] < 0) {
+      resid[p] = (T)0;
+      continue;
+    }
+    const T ep = eps ? eps[p] : (T)1;
+    resid[p] = ep * ((ep * conv_v[p]) / lam[p]);
+  }
+}
+
+template <typename T>
+__global__ void k_elementwise(int op, const T* __restrict__ a, const T* __restrict__ b,
+                              const int32_t* __restrict__ d, int64_t n, T* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    switch (op) {
+      case 0: out[i] = b[i] / a[i]; break;
+      case 1: out[i] = b[i] / sqrt(a[i]); break;
+      case 2: out[i] = ((T)d[i] - a[i]) / sqrt(a[i]); break;
+      default: out[i] = a[i] * b[i]; break;
+    }
+  }
+}
+
+}  // namespace
+
+int energy_partials_count() { return kRedBlocks; }
+
+// --------------------------------------------------------------- host wrappers
+template <typename T>
+int psf_to_cplx(const Geom& g, const void* psf, int layout, int e_broadcast, int64_t u0,
+                int64_t nu, double* sums, void* buf, cudaStream_t s) {
+  if (nu <= 0) return JUBIK_OK;
+  k_psf_to_cplx<T><<<(unsigned)nu, kBlock, 0, s>>>((const T*)psf, layout, e_broadcast, g.E,
+                                                   g.n * g.n, g.nx, g.ny, g.dx, g.P, u0, sums,
+                                                   (double2*)buf);
+  return cuda_status(cudaGetLastError(), "k_psf_to_cplx");
+}
+
+template <typename T>
+int spectra_store(const Geom& g, const void* buf, int64_t u0, int64_t nu, void* hfull,
+                  void* hmain, void* hnyq, cudaStream_t s) {
+  const int64_t total = nu * g.P * g.P;
+  k_spectra_store<T><<<grid_for(total), kBlock, 0, s>>>((const double2*)buf, g.P, u0, nu,
+                                                        (cx<T>*)hfull, (cx<T>*)hmain,
+                                                        (cx<T>*)hnyq);
+  return cuda_status(cudaGetLastError(), "k_spectra_store");
+}
+
+template <typename T>
+int plain_sky_patches(const Geom& g, const void* x, const void* wt, void* zs, cudaStream_t s) {
+  const int64_t total = (int64_t)g.E * g.n * g.n * g.P * g.P;
+  k_plain_sky_patches<T><<<grid_for(total), kBlock, 0, s>>>(
+      (const T*)x, (const T*)wt, g.E, g.n, g.nx, g.ny, g.dx, g.margin, g.half, g.sr_max, g.sc_max,
+      g.P, (cx<T>*)zs);
+  return cuda_status(cudaGetLastError(), "k_plain_sky_patches");
+}
+
+template <typename T>
+int plain_mul_modules(const Geom& g, const void* zs, const void* hfull, int m0, int nm, void* zu,
+                      cudaStream_t s) {
+  const int64_t total = (int64_t)nm * g.E * g.n * g.n * g.P * g.P;
+  k_plain_mul_modules<T><<<grid_for(total), kBlock, 0, s>>>(
+      (const cx<T>*)zs, (const cx<T>*)hfull, m0, nm, g.E, g.n * g.n, g.P, (cx<T>*)zu);
+  return cuda_status(cudaGetLastError(), "k_plain_mul_modules");
+}
+
+template <typename T>
+int plain_overlap_gather(const Geom& g, const void* zu, int m0, int nm, double scale, void* out,
+                         cudaStream_t s) {
+  const int64_t total = (int64_t)nm * g.E * g.nx * g.ny;
+  k_plain_overlap_gather<T><<<grid_for(total), kBlock, 0, s>>>(
+      (const cx<T>*)zu, m0, nm, g.E, g.n, g.nx, g.ny, g.dx, g.margin, g.half, g.sr_max, g.sc_max,
+      g.P, (T)scale, (T*)out);
+  return cuda_status(cudaGetLastError(), "k_plain_overlap_gather");
+}
+
+template <typename T>
+int plain_cot_patches(const Geom& g, const void* cot, int m0, int nm, void* zu, cudaStream_t s) {
+  const int64_t total = (int64_t)nm * g.E * g.n * g.n * g.P * g.P;
+  k_plain_cot_patches<T><<<grid_for(total), kBlock, 0, s>>>(
+      (const T*)cot, m0, nm, g.E, g.n, g.nx, g.ny, g.dx, g.margin, g.half, g.sr_max, g.sc_max,
+      g.P, (cx<T>*)zu);
+  return cuda_status(cudaGetLastError(), "k_plain_cot_patches");
+}
+
+template <typename T>
+int plain_mulconj_accum(const Geom& g, const void* zu, const void* hfull, int m0, int nm,
+                        bool first, void* zs, cudaStream_t s) {
+  const int64_t total = (int64_t)g.E * g.n * g.n * g.P * g.P;
+  k_plain_mulconj_accum<T><<<grid_for(total), kBlock, 0, s>>>(
+      (const cx<T>*)zu, (const cx<T>*)hfull, m0, nm, g.E, g.n * g.n, g.P, first ? 1 : 0,
+      (cx<T>*)zs);
+  return cuda_status(cudaGetLastError(), "k_plain_mulconj_accum");
+}
+
+template <typename T>
+int plain_grad_gather(const Geom& g, const void* zs, const void* wt, double scale, void* out,
+                      cudaStream_t s) {
+  const int64_t total = (int64_t)g.E * g.nx * g.ny;
+  k_plain_grad_gather<T><<<grid_for(total), kBlock, 0, s>>>(
+      (const cx<T>*)zs, (const T*)wt, g.E, g.n, g.nx, g.ny, g.dx, g.margin, g.half, g.sr_max,
+      g.sc_max, g.P, (T)scale, (T*)out);
+  return cuda_status(cudaGetLastError(), "k_plain_grad_gather");
+}
+
+template <typename T>
+int slice_patches_op(const void* x, int64_t batch, int nx, int ny, int n, int dr, void* out,
+                     cudaStream_t s) {
+  SliceGeom g;
+  JUBIK_TRY(make_slice_geom(nx, ny, n, dr, &g));
+  const int64_t total = (int64_t)n * n * batch * g.sh * g.sw;
+  if (total == 0) return JUBIK_OK;
+  k_slice_patches<T><<<grid_for(total), kBlock, 0, s>>>((const T*)x, batch, g, (T*)out);
+  return cuda_status(cudaGetLastError(), "k_slice_patches");
+}
+
+template <typename T>
+int slice_patches_adjoint_op(const void* patches, int64_t batch, int nx, int ny, int n, int dr,
+                             void* out, cudaStream_t s) {
+  SliceGeom g;
+  JUBIK_TRY(make_slice_geom(nx, ny, n, dr, &g));
+  const int64_t total = batch * nx * ny;
+  if (total == 0) return JUBIK_OK;
+  k_slice_patches_adjoint<T><<<grid_for(total), kBlock, 0, s>>>((const T*)patches, batch, g,
+                                                                (T*)out);
+  return cuda_status(cudaGetLastError(), "k_slice_patches_adjoint");
+}
+
+template <typename T>
+int readout_gather(const void* img, const void* eps, const int64_t* idx, int64_t nread,
+                   void* out, cudaStream_t s) {
+  if (nread <= 0) return JUBIK_OK;
+  k_readout_gather<T><<<grid_for(nread), kBlock, 0, s>>>((const T*)img, (const T*)eps, idx,
+                                                         nread, (T*)out);
+  return cuda_status(cudaGetLastError(), "k_readout_gather");
+}
+
+template <typename T>
+int readout_scatter(const void* vec, const void* eps, const int64_t* idx, int64_t nread,
+                    void* img, cudaStream_t s) {
+  if (nread <= 0) return JUBIK_OK;
+  k_readout_scatter<T><<<grid_for(nread), kBlock, 0, s>>>((const T*)vec, (const T*)eps, idx,
+                                                          nread, (T*)img);
+  return cuda_status(cudaGetLastError(), "k_readout_scatter");
+}
+
+template <typename T>
+int poisson_image(const void* conv, const void* eps, const int32_t* ridx, const int32_t* data,
+                  int64_t npix, void* lam_out_readout, void* lam_cache, void* resid,
+                  double* partials, unsigned int* counter, double* energy, cudaStream_t s) {
+  k_poisson_image<T><<<kRedBlocks, kBlock, 0, s>>>((const T*)conv, (const T*)eps, ridx, data,
+                                                   npix, (T*)lam_out_readout, (T*)lam_cache,
+                                                   (T*)resid, partials, counter, energy);
+  return cuda_status(cudaGetLastError(), "k_poisson_image");
+}
+
+template <typename T>
+int metric_weights(const void* conv_v, const void* eps, const int32_t* ridx, const void* lam_cache,
+                   int64_t npix, void* resid, cudaStream_t s) {
+  k_metric_weights<T><<<grid_for(npix), kBlock, 0, s>>>((const T*)conv_v, (const T*)eps, ridx,
+                                                        (const T*)lam_cache, npix, (T*)resid);
+  return cuda_status(cudaGetLastError(), "k_metric_weights");
+}
+
+template <typename T>
+int poisson_vec(const void* lam, const int32_t* data, int64_t n, double* partials,
+                unsigned int* counter, double* energy, void* grad, cudaStream_t s) {
+  k_poisson_vec<T><<<kRedBlocks, kBlock, 0, s>>>((const T*)lam, data, n, partials, counter,
+                                                 energy, (T*)grad);
+  return cuda_status(cudaGetLastError(), "k_poisson_vec");
+}
+
+template <typename T>
+int elementwise_op(int op, const void* a, const void* b, const int32_t* d, int64_t n, void* out,
+                   cudaStream_t s) {
+  if (n <= 0) return JUBIK_OK;
+  k_elementwise<T><<<grid_for(n), kBlock, 0, s>>>(op, (const T*)a, (const T*)b, d, n, (T*)out);
+  return cuda_status(cudaGetLastError(), "k_elementwise");
+}
+
+#define JUBIK_INST(T)                                                                            \
+  template int psf_to_cplx<T>(const Geom&, const void*, int, int, int64_t, int64_t, double*,     \
+                              void*, cudaStream_t);                                              \
+  template int spectra_store<T>(const Geom&, const void*, int64_t, int64_t, void*, void*, void*, \
+                                cudaStream_t);                                                   \
+  template int plain_sky_patches<T>(const Geom&, const void*, const void*, void*, cudaStream_t); \
+  template int plain_mul_modules<T>(const Geom&, const void*, const void*, int, int, void*,      \
+                                    cudaStream_t);                                               \
+  template int plain_overlap_gather<T>(const Geom&, const void*, int, int, double, void*,        \
+                                       cudaStream_t);                                            \
+  template int plain_cot_patches<T>(const Geom&, const void*, int, int, void*, cudaStream_t);    \
+  template int plain_mulconj_accum<T>(const Geom&, const void*, const void*, int, int, bool,     \
+                                      void*, cudaStream_t);                                      \
+  template int plain_grad_gather<T>(const Geom&, const void*, const void*, double, void*,        \
+                                    cudaStream_t);                                               \
+  template int slice_patches_op<T>(const void*, int64_t, int, int, int, int, void*,              \
+                                   cudaStream_t);                                                \
+  template int slice_patches_adjoint_op<T>(const void*, int64_t, int, int, int, int, void*,      \
+                                           cudaStream_t);                                        \
+  template int readout_gather<T>(const void*, const void*, const int64_t*, int64_t, void*,       \
+                                 cudaStream_t);                                                  \
+  template int readout_scatter<T>(const void*, const void*, const int64_t*, int64_t, void*,      \
+                                  cudaStream_t);                                                 \
+  template int poisson_image<T>(const void*, const void*, const int32_t*, const int32_t*,        \
+                                int64_t, void*, void*, void*, double*, unsigned int*, double*,   \
+                                cudaStream_t);                                                   \
+  template int metric_weights<T>(const void*, const void*, const int32_t*, const void*, int64_t, \
+                                 void*, cudaStream_t);                                           \
+  template int poisson_vec<T>(const void*, const int32_t*, int64_t, double*, unsigned int*,      \
+                              double*, void*, cudaStream_t);                                     \
+  template int elementwise_op<T>(int, const void*, const void*, const int32_t*, int64_t, void*,  \
+                                 cudaStream_t);
+
+JUBIK_INST(float)
+JUBIK_INST(double)
+#undef JUBIK_INST
+
+}  // namespace jubik

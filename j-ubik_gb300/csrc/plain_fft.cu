@@ -1,0 +1,266 @@
+// Batched complex FFTs of arbitrary supported length (mixed radix 4/2/3 with
+// generic odd radices up to 64), Stockham auto-sort in shared memory.
+//
+// This is the "plain" transform: it stands in for the jnp.fft.fftn / ifftn
+// calls of jubik/convolve.py:165-174 (complex, full size, unnormalised
+// forward; the caller applies the 1/N of ifftn through `scale`).  It is used
+// by the unfused path, by the FP64 PSF-spectrum preparation of every plan and
+// by the stand-alone convolve.  Stage s with radix r and running length Ns:
+//   v_q = in[j + q L/r] * w^(q k),  k = j mod Ns,  w = exp(-2 pi i / (Ns r))
+//   out[(j / Ns) Ns r + k + q Ns] = DFT_r(v)_q
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "fft_codelets.cuh"
+#include "internal.h"
+
+namespace jubik {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+template <int R, typename T>
+__device__ __forceinline__ void bfly(const cx<T>* __restrict__ src, cx<T>* __restrict__ dst,
+                                     int j, int Lr, int Ns, int tstep,
+                                     const cx<T>* __restrict__ tw, bool inv) {
+  const int k = j % Ns;
+  cx<T> v[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) v[q] = src[j + q * Lr];
+#pragma unroll
+  for (int q = 1; q < R; ++q) {
+    cx<T> w = tw[q * k * tstep];
+    v[q] = inv ? cmulc<T>(v[q], w) : cmul<T>(v[q], w);
+  }
+  if (inv)
+    Dft<R, true, T>::run(v);
+  else
+    Dft<R, false, T>::run(v);
+  const int base = (j / Ns) * Ns * R + k;
+#pragma unroll
+  for (int q = 0; q < R; ++q) dst[base + q * Ns] = v[q];
+}
+
+// Generic radix r (odd prime up to kMaxGenericRadix): direct r-point DFT with
+// the length-L twiddle table (w_r^t = tw[t * L / r]).
+template <typename T>
+__device__ void bfly_generic(const cx<T>* __restrict__ src, cx<T>* __restrict__ dst, int j,
+                             int L, int r, int Ns, const cx<T>* __restrict__ tw, bool inv) {
+  const int Lr = L / r;
+  const int k = j % Ns;
+  const int tstep = L / (Ns * r);
+  cx<T> v[kMaxGenericRadix];
+  for (int q = 0; q < r; ++q) {
+    cx<T> a = src[j + q * Lr];
+    if (q > 0) {
+      cx<T> w = tw[q * k * tstep];
+      a = inv ? cmulc<T>(a, w) : cmul<T>(a, w);
+    }
+    v[q] = a;
+  }
+  const int base = (j / Ns) * Ns * r + k;
+  for (int kk = 0; kk < r; ++kk) {
+    cx<T> acc = v[0];
+    for (int q = 1; q < r; ++q) {
+      cx<T> w = tw[((q * kk) % r) * Lr];
+      acc = cadd<T>(acc, inv ? cmulc<T>(v[q], w) : cmul<T>(v[q], w));
+    }
+    dst[base + kk * Ns] = acc;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    k_fft_batched(cx<T>* __restrict__ data, int64_t nseq, int L, int nb, int64_t sa, int64_t sb,
+                  int64_t se, const cx<T>* __restrict__ tw, FftStages st, int inv, T scale,
+                  int spc) {
+  extern __shared__ unsigned char smem_raw[];
+  cx<T>* b0 = reinterpret_cast<cx<T>*>(smem_raw);
+  cx<T>* b1 = b0 + (size_t)spc * L;
+  const int64_t s0 = (int64_t)blockIdx.x * spc;
+  const int ns = (int)min((int64_t)spc, nseq - s0);
+  const bool seq_fast = (se != 1);
+  for (int idx = threadIdx.x; idx < ns * L; idx += blockDim.x) {
+    int s, i;
+    if (seq_fast) {
+      s = idx % ns;
+      i = idx / ns;
+    } else {
+      i = idx % L;
+      s = idx / L;
+    }
+    const int64_t q = s0 + s;
+    b0[s * L + i] = data[(q / nb) * sa + (q % nb) * sb + (int64_t)i * se];
+  }
+  __syncthreads();
+  cx<T>* in = b0;
+  cx<T>* out = b1;
+  int Ns = 1;
+  for (int stg = 0; stg < st.n; ++stg) {
+    const int r = st.r[stg];
+    const int Lr = L / r;
+    const int tstep = L / (Ns * r);
+    for (int b = threadIdx.x; b < ns * Lr; b += blockDim.x) {
+      const int s = b / Lr;
+      const int j = b - s * Lr;
+      const cx<T>* src = in + s * L;
+      cx<T>* dst = out + s * L;
+      switch (r) {
+        case 2: bfly<2, T>(src, dst, j, Lr, Ns, tstep, tw, inv); break;
+        case 3: bfly<3, T>(src, dst, j, Lr, Ns, tstep, tw, inv); break;
+        case 4: bfly<4, T>(src, dst, j, Lr, Ns, tstep, tw, inv); break;
+        default: bfly_generic<T>(src, dst, j, L, r, Ns, tw, inv); break;
+      }
+    }
+    __syncthreads();
+    cx<T>* t = in;
+    in = out;
+    out = t;
+    Ns *= r;
+  }
+  for (int idx = threadIdx.x; idx < ns * L; idx += blockDim.x) {
+    int s, i;
+    if (seq_fast) {
+      s = idx % ns;
+      i = idx / ns;
+    } else {
+      i = idx % L;
+      s = idx / L;
+    }
+    const int64_t q = s0 + s;
+    cx<T> v = in[s * L + i];
+    data[(q / nb) * sa + (q % nb) * sb + (int64_t)i * se] = mkc<T>(v.x * scale, v.y * scale);
+  }
+}
+
+bool factorize(int L, FftStages* st) {
+  st->n = 0;
+  if (L < 1) return false;
+  int rem = L;
+  auto push = [&](int r) {
+    if (st->n >= kMaxStages) return false;
+    st->r[st->n++] = r;
+    return true;
+  };
+  while (rem % 4 == 0) {
+    if (!push(4)) return false;
+    rem /= 4;
+  }
+  while (rem % 2 == 0) {
+    if (!push(2)) return false;
+    rem /= 2;
+  }
+  while (rem % 3 == 0) {
+    if (!push(3)) return false;
+    rem /= 3;
+  }
+  for (int p = 5; rem > 1 && p <= kMaxGenericRadix; p += 2) {
+    while (rem % p == 0) {
+      if (!push(p)) return false;
+      rem /= p;
+    }
+  }
+  return rem == 1;
+}
+
+constexpr int kMaxL = 4096;
+
+int max_smem_optin() {
+  static int v = -1;
+  if (v < 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+      v = 48 * 1024;
+  }
+  return v;
+}
+
+}  // namespace
+
+bool fft_length_supported(int L) {
+  FftStages st;
+  return L >= 1 && L <= kMaxL && factorize(L, &st);
+}
+
+int fft1d_init(Fft1D* f, int L) {
+  if (!fft_length_supported(L)) {
+    set_error("FFT length %d unsupported (needs prime factors <= %d and L <= %d)", L,
+              kMaxGenericRadix, kMaxL);
+    return JUBIK_ERR_UNSUPPORTED;
+  }
+  f->L = L;
+  factorize(L, &f->st);
+  std::vector<float2> t32(L);
+  std::vector<double2> t64(L);
+  const long double twopi = 6.283185307179586476925286766559005768L;
+  for (int t = 0; t < L; ++t) {
+    const long double a = twopi * (long double)t / (long double)L;
+    const long double c = cosl(a), s = -sinl(a);
+    t64[t] = make_double2((double)c, (double)s);
+    t32[t] = make_float2((float)c, (float)s);
+  }
+  JUBIK_TRY_CUDA(cudaMalloc(&f->tw32, sizeof(float2) * L));
+  JUBIK_TRY_CUDA(cudaMalloc(&f->tw64, sizeof(double2) * L));
+  JUBIK_TRY_CUDA(cudaMemcpy(f->tw32, t32.data(), sizeof(float2) * L, cudaMemcpyHostToDevice));
+  JUBIK_TRY_CUDA(cudaMemcpy(f->tw64, t64.data(), sizeof(double2) * L, cudaMemcpyHostToDevice));
+  return JUBIK_OK;
+}
+
+void fft1d_free(Fft1D* f) {
+  if (f->tw32) cudaFree(f->tw32);
+  if (f->tw64) cudaFree(f->tw64);
+  f->tw32 = f->tw64 = nullptr;
+  f->L = 0;
+}
+
+template <typename T>
+int fft_batched(const Fft1D& f, void* data, int64_t nseq, int nb, int64_t sa, int64_t sb,
+                int64_t se, bool inverse, double scale, cudaStream_t s) {
+  if (nseq <= 0) return JUBIK_OK;
+  const int L = f.L;
+  const size_t per = 2 * sizeof(cx<T>) * (size_t)L;
+  const int smax = max_smem_optin();
+  int spc = (int)std::max<size_t>(1, std::min<size_t>(64, (size_t)(48 * 1024) / per));
+  if (per > (size_t)smax) {
+    set_error("FFT length %d needs %zu bytes of shared memory", L, per);
+    return JUBIK_ERR_UNSUPPORTED;
+  }
+  const size_t smem = per * spc;
+  if (smem > 48 * 1024) {
+    JUBIK_TRY_CUDA(cudaFuncSetAttribute(k_fft_batched<T>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  }
+  const int64_t blocks = (nseq + spc - 1) / spc;
+  if (blocks > 0x7fffffffLL) {
+    set_error("too many FFT sequences");
+    return JUBIK_ERR_UNSUPPORTED;
+  }
+  const cx<T>* tw = (const cx<T>*)(sizeof(T) == 4 ? f.tw32 : f.tw64);
+  k_fft_batched<T><<<(unsigned)blocks, kThreads, smem, s>>>((cx<T>*)data, nseq, L, nb, sa, sb, se,
+                                                           tw, f.st, inverse ? 1 : 0, (T)scale,
+                                                           spc);
+  return cuda_status(cudaGetLastError(), "k_fft_batched launch");
+}
+
+template <typename T>
+int fft2_batched(const Fft1D& fh, const Fft1D& fw, void* data, int64_t batch, bool inverse,
+                 cudaStream_t s) {
+  const int64_t h = fh.L, w = fw.L;
+  // rows: sequences (b, y), contiguous
+  JUBIK_TRY(fft_batched<T>(fw, data, batch * h, (int)h, h * w, w, 1, inverse, 1.0, s));
+  // columns: sequences (b, x), stride w
+  JUBIK_TRY(fft_batched<T>(fh, data, batch * w, (int)w, h * w, 1, w, inverse, 1.0, s));
+  return JUBIK_OK;
+}
+
+template int fft_batched<float>(const Fft1D&, void*, int64_t, int, int64_t, int64_t, int64_t,
+                                bool, double, cudaStream_t);
+template int fft_batched<double>(const Fft1D&, void*, int64_t, int, int64_t, int64_t, int64_t,
+                                 bool, double, cudaStream_t);
+template int fft2_batched<float>(const Fft1D&, const Fft1D&, void*, int64_t, bool, cudaStream_t);
+template int fft2_batched<double>(const Fft1D&, const Fft1D&, void*, int64_t, bool, cudaStream_t);
+
+}  // namespace jubik

@@ -1,0 +1,265 @@
+"""Host-side plan object over the C ABI (``jubik_plan_*``).
+
+A :class:`ResponsePlan` holds, on one GPU, everything the response needs
+between calls: the normalised PSF spectra (computed once, where the
+reference recomputes the kernel preparation of ``jubik/convolve.py:104-131``
+on every call), the exposure, the readout index map and the Poisson counts.
+All arrays are PyTorch CUDA tensors; the library only sees raw pointers.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _lib
+
+_DTYPES = {torch.float32: _lib.F32, torch.float64: _lib.F64}
+_PATHS = {"auto": _lib.PATH_AUTO, "fused": _lib.PATH_FUSED, "plain": _lib.PATH_PLAIN}
+
+
+def dtype_code(dtype: torch.dtype) -> int:
+    try:
+        return _DTYPES[dtype]
+    except KeyError:
+        raise TypeError(f"unsupported dtype {dtype}; use float32 or float64") from None
+
+
+def stream_handle(device: torch.device) -> C.c_void_p:
+    return C.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def require_cuda() -> torch.device:
+    if not torch.cuda.is_available():
+        raise _lib.JubikError("the GB300 response needs a CUDA device; none is visible")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def as_device(x, dtype: Optional[torch.dtype], device: torch.device) -> torch.Tensor:
+    """Contiguous CUDA tensor view/copy of ``x`` (numpy array or tensor)."""
+    if isinstance(x, torch.Tensor):
+        t = x
+    else:
+        t = torch.as_tensor(np.asarray(x))
+    if dtype is not None and t.dtype != dtype:
+        t = t.to(dtype)
+    if t.device != device:
+        t = t.to(device)
+    return t.contiguous()
+
+
+def ptr(t: Optional[torch.Tensor]) -> C.c_void_p:
+    return C.c_void_p(0 if t is None else t.data_ptr())
+
+
+class ResponsePlan:
+    """Plan for ``R(x) = mask(exposure(psf(x * pixel_area)))`` on one GPU.
+
+    Parameters mirror the reference: ``n_modules`` is the vmapped module axis
+    of ``erosita_response.py:209-212``, ``shape`` the field ``Domain.shape[-2:]``,
+    ``n_patches`` / ``margin`` those of ``linpatch_convolve``
+    (``jubik/convolve.py:66``).  ``path`` picks the fused single-kernel path
+    ("auto"/"fused") or the unfused one ("plain").
+    """
+
+    def __init__(self, n_modules: int, n_energies: int, shape: Sequence[int], n_patches: int,
+                 margin: int, dtype: torch.dtype = torch.float32, path: str = "auto",
+                 pixel_area: float = 1.0, device: Optional[torch.device] = None):
+        self.device = device if device is not None else require_cuda()
+        self.dtype = dtype
+        self.n_modules, self.n_energies = int(n_modules), int(n_energies)
+        self.shape = (int(shape[0]), int(shape[1]))
+        self.n_patches, self.margin = int(n_patches), int(margin)
+        self.pixel_area = float(pixel_area)
+        self.dx = self.shape[0] // self.n_patches
+        self.K = 2 * self.dx
+        self.P = self.K + 2 * self.margin
+        desc = _lib.PlanDesc(self.n_modules, self.n_energies, self.shape[0], self.shape[1],
+                             self.n_patches, self.margin, dtype_code(dtype), _PATHS[path],
+                             self.pixel_area)
+        h = C.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.load().jubik_plan_create(C.byref(desc), C.byref(h)),
+                       "jubik_plan_create")
+        self._h = h
+        p = C.c_int32()
+        _lib.call("jubik_plan_path", self._h, C.byref(p))
+        self.path = {1: "fused", 2: "plain"}[p.value]
+        self._refresh_readout()
+        self._keep = []  # tensors the plan reads asynchronously
+
+    # -------------------------------------------------------------- state
+    def close(self):
+        if getattr(self, "_h", None):
+            torch.cuda.synchronize(self.device)
+            _lib.load().jubik_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def workspace_bytes(self) -> int:
+        b = C.c_int64()
+        _lib.call("jubik_plan_workspace_bytes", self._h, C.byref(b))
+        return b.value
+
+    def _s(self):
+        return stream_handle(self.device)
+
+    def _refresh_readout(self):
+        sizes = (C.c_int64 * self.n_modules)()
+        tot = C.c_int64()
+        _lib.call("jubik_plan_readout_sizes", self._h, sizes, C.byref(tot))
+        self.readout_sizes = [int(v) for v in sizes]
+        self.readout_total = int(tot.value)
+
+    def set_psf(self, psf, layout: str = "auto") -> "ResponsePlan":
+        """PSF kernels: (M, n^2, E, K, K) pre-cut windows or (M, n^2, E, nx, ny)
+        full-field kernels; an array without the E axis is broadcast over
+        energies (``convolve.py:167-171``)."""
+        t = as_device(psf, self.dtype, self.device)
+        n2 = self.n_patches ** 2
+        if t.dim() == 4:
+            t = t.unsqueeze(2)
+            bcast = 1
+        elif t.dim() == 5:
+            bcast = 0
+        else:
+            raise ValueError("kernel must have shape (M, n^2, [E,] k, k)")
+        if t.shape[0] != self.n_modules or t.shape[1] != n2:
+            raise ValueError(f"kernel leading shape {tuple(t.shape[:2])} does not match "
+                             f"(modules, n^2) = ({self.n_modules}, {n2})")
+        if not bcast and t.shape[2] != self.n_energies:
+            raise ValueError("kernel energy axis does not match the plan")
+        win = tuple(t.shape[-2:])
+        if layout == "auto":
+            layout = "precut" if win == (self.K, self.K) else "full"
+        if layout == "precut" and win != (self.K, self.K):
+            raise ValueError(f"pre-cut kernels must be ({self.K}, {self.K}), got {win}")
+        if layout == "full" and win != self.shape:
+            raise ValueError(f"full-field kernels must be {self.shape}, got {win}")
+        code = _lib.PSF_PRECUT if layout == "precut" else _lib.PSF_FULL
+        _lib.call("jubik_plan_set_psf", self._h, ptr(t), code, bcast, self._s())
+        torch.cuda.current_stream(self.device).synchronize()
+        return self
+
+    def set_exposure(self, exposure=None, readmask=None) -> "ResponsePlan":
+        """exposure (M,E,nx,ny) (None = ones); readmask (M,E,nx,ny) bool, True
+        where the pixel is read out (None = all)."""
+        full = (self.n_modules, self.n_energies) + self.shape
+        e = None
+        if exposure is not None:
+            e = as_device(exposure, self.dtype, self.device)
+            e = e.expand(full).contiguous() if tuple(e.shape) != full else e
+        m = None
+        if readmask is not None:
+            m = as_device(readmask, None, self.device)
+            m = m.expand(full) if tuple(m.shape) != full else m
+            m = m.to(torch.uint8).contiguous()
+        _lib.call("jubik_plan_set_exposure", self._h, ptr(e), ptr(m), self._s())
+        self._refresh_readout()
+        return self
+
+    def readout_index(self) -> torch.Tensor:
+        """Flat (M,E,nx,ny) indices of the read-out pixels (device int64 view)."""
+        p = C.c_void_p()
+        _lib.call("jubik_plan_readout_index", self._h, C.byref(p))
+        if self.readout_total == 0:
+            return torch.empty(0, dtype=torch.int64, device=self.device)
+        return _wrap_device(p.value, self.readout_total, "<i8", self.device).clone()
+
+    def set_data(self, counts) -> "ResponsePlan":
+        """Poisson counts in readout order (total,) -> int32 on the device."""
+        d = as_device(counts, torch.int32, self.device).reshape(-1)
+        if d.numel() != self.readout_total:
+            raise ValueError(f"data has {d.numel()} entries, the readout has {self.readout_total}")
+        if torch.any(d < 0):
+            raise ValueError("`data` may not be negative")
+        _lib.call("jubik_plan_set_data", self._h, ptr(d), self._s())
+        torch.cuda.current_stream(self.device).synchronize()
+        return self
+
+    # -------------------------------------------------------------- operators
+    def _sky(self, x) -> torch.Tensor:
+        t = as_device(x, self.dtype, self.device)
+        want = (self.n_energies,) + self.shape
+        if tuple(t.shape) != want:
+            t = t.reshape(want)
+        return t
+
+    def psf_forward(self, x, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        x = self._sky(x)
+        if out is None:
+            out = torch.empty((self.n_modules, self.n_energies) + self.shape, dtype=self.dtype,
+                              device=self.device)
+        _lib.call("jubik_psf_forward", self._h, ptr(x), ptr(out), self._s())
+        return out
+
+    def psf_adjoint(self, cot, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        c = as_device(cot, self.dtype, self.device).reshape(
+            (self.n_modules, self.n_energies) + self.shape)
+        if out is None:
+            out = torch.empty((self.n_energies,) + self.shape, dtype=self.dtype,
+                              device=self.device)
+        _lib.call("jubik_psf_adjoint", self._h, ptr(c), ptr(out), self._s())
+        return out
+
+    def response(self, x, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        x = self._sky(x)
+        if out is None:
+            out = torch.empty(self.readout_total, dtype=self.dtype, device=self.device)
+        _lib.call("jubik_response_forward", self._h, ptr(x), ptr(out), self._s())
+        return out
+
+    def response_vjp(self, cot, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        c = as_device(cot, self.dtype, self.device).reshape(-1)
+        if c.numel() != self.readout_total:
+            raise ValueError("cotangent size does not match the readout")
+        if out is None:
+            out = torch.empty((self.n_energies,) + self.shape, dtype=self.dtype,
+                              device=self.device)
+        _lib.call("jubik_response_vjp", self._h, ptr(c), ptr(out), self._s())
+        return out
+
+    def energy_and_grad(self, x, need_grad: bool = True, energy: Optional[torch.Tensor] = None,
+                        grad: Optional[torch.Tensor] = None):
+        """Poisson energy (float64 0-d device tensor) and dE/dx, one fused pass."""
+        x = self._sky(x)
+        if energy is None:
+            energy = torch.empty((), dtype=torch.float64, device=self.device)
+        if need_grad and grad is None:
+            grad = torch.empty((self.n_energies,) + self.shape, dtype=self.dtype,
+                               device=self.device)
+        _lib.call("jubik_poisson_energy_grad", self._h, ptr(x), ptr(energy),
+                  ptr(grad if need_grad else None), self._s())
+        return energy, (grad if need_grad else None)
+
+    def metric(self, x, v, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """R^T diag(1/lam) R v with lam = R(x); x=None reuses the last lam."""
+        xx = None if x is None else self._sky(x)
+        vv = self._sky(v)
+        if out is None:
+            out = torch.empty((self.n_energies,) + self.shape, dtype=self.dtype,
+                              device=self.device)
+        _lib.call("jubik_metric_apply", self._h, ptr(xx), ptr(vv), ptr(out), self._s())
+        return out
+
+    def split_readout(self, flat: torch.Tensor):
+        """Split a flat readout vector into the per-module pieces."""
+        return list(torch.split(flat, self.readout_sizes))
+
+
+def _wrap_device(address: int, n: int, typestr: str, device: torch.device) -> torch.Tensor:
+    """Read-only tensor view of n elements at a raw device address."""
+
+    class _View:
+        __cuda_array_interface__ = {"shape": (n,), "typestr": typestr,
+                                    "data": (address, True), "version": 3}
+
+    return torch.as_tensor(_View(), device=device)

@@ -1,0 +1,60 @@
+"""The C-ABI library loads and exports every symbol the public header
+declares (no compute calls: no GPU needed)."""
+import ctypes
+import os
+
+import pytest
+
+import jubik_gb300 as ju
+from jubik_gb300 import _lib
+
+
+def _built():
+    return os.path.exists(_lib.LIB_PATH)
+
+
+@pytest.mark.skipif(not _built(), reason="library not built")
+def test_library_exports_every_header_symbol():
+    lib = _lib.load()
+    names = _lib.header_symbols()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert missing == []
+    # and the ctypes signature table covers exactly the header
+    assert sorted(_lib._SIGS) == names
+
+
+@pytest.mark.skipif(not _built(), reason="library not built")
+def test_info_calls_need_no_gpu():
+    lib = _lib.load()
+    assert lib.jubik_abi_version() == 1
+    assert lib.jubik_fused_supported(192, _lib.F32) == 1
+    assert lib.jubik_fused_supported(192, _lib.F64) == 0
+    assert lib.jubik_fused_supported(80, _lib.F32) == 0
+    assert lib.jubik_fft_length_supported(96) == 1
+    assert lib.jubik_fft_length_supported(131) == 0  # prime > 64
+
+
+@pytest.mark.skipif(not _built(), reason="library not built")
+def test_invalid_plan_descriptions_fail_without_touching_the_gpu():
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    bad = [
+        _lib.PlanDesc(1, 1, 64, 64, 4, 0, 0, 0, 1.0),     # margin 0: reference crops [0:-0]
+        _lib.PlanDesc(1, 1, 64, 64, 0, 4, 0, 0, 1.0),     # no patches
+        _lib.PlanDesc(1, 1, 64, 32, 4, 4, 0, 0, 1.0),     # non-square stride
+        _lib.PlanDesc(1, 1, 64, 64, 4, 4, 7, 0, 1.0),     # bad dtype
+    ]
+    for d in bad:
+        st = lib.jubik_plan_create(ctypes.byref(d), ctypes.byref(h))
+        assert st == _lib.ERR_INVALID_ARGUMENT, _lib.last_error()
+        assert h.value is None
+    with pytest.raises(ValueError):
+        _lib.check(_lib.ERR_INVALID_ARGUMENT, "x")
+    with pytest.raises(_lib.JubikUnsupported):
+        _lib.check(_lib.ERR_UNSUPPORTED, "x")
+
+
+def test_header_parser_finds_declarations():
+    names = _lib.header_symbols()
+    assert "jubik_poisson_energy_grad" in names and "jubik_plan_create" in names

@@ -1,0 +1,68 @@
+"""Host-side logic of the drop-ins that runs before any GPU work (no GPU)."""
+import numpy as np
+import pytest
+
+import jubik_gb300 as ju
+
+
+def test_coord_center_matches_reference_known_answer():
+    np.testing.assert_array_equal(ju.coord_center(4, 2), np.array([5, 13, 7, 15]))
+
+
+def test_bilinear_weights_drop_in():
+    w = ju._bilinear_weights((4, 4))
+    assert w.shape == (4, 4) and np.all(w >= 0)
+    np.testing.assert_allclose(w, w[::-1, :])
+    with pytest.raises(ValueError):
+        ju._bilinear_weights((3, 3))
+
+
+def test_exposure_negative_cut_raises_before_gpu():
+    with pytest.raises(ValueError):
+        ju.build_exposure_function(np.ones((2, 4, 4)), -1)
+
+
+def test_exposure_cut_is_applied_in_place():
+    exp = np.array([[1.0, 5.0], [10.0, 0.5]])
+    try:
+        ju.build_exposure_function(exp, 2.0)
+    except Exception:
+        pass  # no GPU here: the in-place threshold happens first
+    np.testing.assert_array_equal(exp, [[0.0, 5.0], [10.0, 0.0]])
+
+
+def test_readout_validation_before_gpu():
+    flags = np.ones((2, 3, 4, 4))
+    with pytest.raises(ValueError):
+        ju.build_readout_function(flags.copy(), -1, ("a", "b"))
+    with pytest.raises(ValueError):
+        ju.build_readout_function(flags.copy(), None, ("a",))
+    f = ju.build_readout_function(np.ones((1, 4, 4)), None, ("a",))
+    with pytest.raises(ValueError, match="flags should have shape"):
+        f(np.ones((1, 2, 4, 4)))
+    g = ju.build_readout_function(flags.copy(), None, ("a", "b"))
+    with pytest.raises(ValueError, match="input should have shape"):
+        g(np.ones((3, 4, 4)))
+
+
+def test_readout_threshold_in_place():
+    flags = np.array([[[[1.0, 30.0], [50.0, 5.0]]]])
+    ju.build_readout_function(flags, 20, None)
+    np.testing.assert_array_equal(flags, [[[[0.0, 30.0], [50.0, 0.0]]]])
+
+
+def test_poissonian_rejects_float_data():
+    with pytest.raises(TypeError):
+        ju.Poissonian(np.array([1.0, 2.0]))
+
+
+def test_vector_tree_interface():
+    v = ju.Vector({"a": np.ones(2), "b": np.zeros(3)})
+    assert list(v.keys()) == ["a", "b"]
+    w = v * 2.0 + v
+    np.testing.assert_array_equal(w.tree["a"], [3.0, 3.0])
+
+
+def test_linpatch_domain_type_checked():
+    with pytest.raises(ValueError, match="domain has to be"):
+        ju.linpatch_convolve(np.ones((8, 8)), (8, 8), np.ones((4, 8, 8)), 2, 1)
