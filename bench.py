@@ -1,0 +1,367 @@
+"""Benchmark: Mpix/s of the FP32 fused response forward + VJP with the Poisson
+likelihood (energy + gradient) on the 1024^2 x 7 modules x 3 energies
+workload (16x16 patches of stride 64, margin 32, FFT side 192).
+
+One step = lam = R(x); H = sum(lam - d log lam); grad = R^T(1 - d/lam), i.e.
+one ``jubik_poisson_energy_grad`` call: 22.02 Mpix of data-space pixels.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  ``--impl reference`` times the float64 CPU
+restatement of the reference path on the host cores (the reference itself is
+JAX, which is not installed) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = {"workload": "response_fwd_vjp_poisson", "field": [1024, 1024], "modules": 7,
+            "energies": 3, "patches_per_axis": 16, "patch_stride": 64, "margin": 32,
+            "fft_side": 192, "psf": "Moffat beta 2.5, FWHM 2-8 px, per-module rotation",
+            "l2": "inputs larger than L2 (801 MB of PSF spectra per pass)"}
+METRIC = "Mpix/s response fwd+VJP (1024²×7 modules×3 E); FP32 vs FP64, rel err ≤1e-6"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--path", choices=["auto", "fused", "plain"], default="auto")
+    ap.add_argument("--nx", type=int, default=1024)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the FP64 comparison and the CPU baseline")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="one warm-up and two steps (for a launch list under a profiler)")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the GPU works."""
+
+    FIELDS = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: str):
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", index, f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "50"],
+                stdout=self.file, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        self.file.seek(0)
+        rows = [r.split(",") for r in self.file.read().strip().splitlines() if r.count(",") >= 8]
+        os.unlink(self.file.name)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU legs
+def cpu_sample(inst, data, reps=1):
+    """The float64 CPU restatement on module 0, energy 0 of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import jubik_oracle as O
+
+    nx = inst.shape[0]
+    dom = O.Domain((1, nx, nx), (1.0, 1.0, 1.0))
+    R = O.Response(dom, inst.psf[:1, :, :1], inst.n_patches, inst.margin,
+                   inst.exposure[:1, :1], inst.readmask[:1, :1])
+    x = inst.sky[:1].astype(np.float64)
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        R.energy_and_grad(x, [data])
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    mpix = nx * nx / 1e6
+    return mpix / best, best, mpix
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from jubik_gb300 import synthetic
+
+    inst = synthetic.config2(nx=args.nx, n_modules=1, n_energies=1)
+    rng = np.random.default_rng(1)
+    data = rng.poisson(inst.exposure[0, 0][inst.readmask[0, 0]] * 2.0).astype(np.int64)
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_sample(inst, data)
+    times = []
+    steps = max(1, min(args.steps, 5))
+    for _ in range(steps):
+        v, dt, mpix = cpu_sample(inst, data)
+        times.append(dt)
+    t = statistics.median(times)
+    value = mpix / t
+    cores = os.cpu_count()
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mpix/s",
+            "n_gpus": world, "steps": steps, "warmup": min(args.warmup, 1),
+            "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": WORKLOAD,
+            "cpu_baseline": {"value": value, "unit": "Mpix/s", "cores": cores, "kind": "port",
+                             "sample": "float64 numpy/scipy.fft restatement, module 0 x energy 0 "
+                                       f"of the workload ({args.nx}^2 px, "
+                                       f"{inst.n_patches ** 2} patch units) per step"},
+            "e2e": {"value": value, "unit": "Mpix/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU leg
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+
+    import jubik_gb300 as ju
+    from jubik_gb300 import synthetic
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        pg = dist
+
+    inst = synthetic.config2(nx=args.nx, dtype=np.float32)
+    M, E, nx = inst.n_modules, inst.n_energies, inst.shape[0]
+    mpix = M * E * nx * nx / 1e6
+    plan = ju.ResponsePlan(M, E, inst.shape, inst.n_patches, inst.margin, dtype=torch.float32,
+                           path=args.path, pixel_area=1.0, device=dev)
+    plan.set_psf(inst.psf)
+    plan.set_exposure(inst.exposure, inst.readmask)
+    x = torch.as_tensor(inst.sky, device=dev)
+    lam = plan.response(x).double().cpu().numpy()
+    data = synthetic.poisson_data(lam, seed=1)
+    plan.set_data(data)
+    energy = torch.empty((), dtype=torch.float64, device=dev)
+    grad = torch.empty_like(x)
+
+    def step():
+        plan.energy_and_grad(x, need_grad=True, energy=energy, grad=grad)
+
+    if args.profile_only:
+        step()
+        step()
+        step()
+        torch.cuda.synchronize()
+        if rank == 0:
+            print(json.dumps({"profile_only": True, "path": plan.path}))
+        return
+
+    index = os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[local if world > 1
+                                                                          else 0]
+    sampler = ClockSampler(index.strip() or "0")
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+    stream = torch.cuda.current_stream(dev)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+    clocks = sampler.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if pg:
+        t = torch.tensor([ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * mpix / (ms / 1e3)
+
+    # per-kernel durations (events on the launch stream, inside the library)
+    plan.set_profiling(True)
+    nprof = min(args.steps, 20)
+    for _ in range(nprof):
+        step()
+    prof = plan.profile()
+    plan.set_profiling(False)
+    fwd_ms = prof["forward"][0] / max(prof["forward"][1], 1)
+    adj_ms = prof["adjoint"][0] / max(prof["adjoint"][1], 1)
+    lik_ms = prof["likelihood"][0] / max(prof["likelihood"][1], 1)
+    mem_ms = prof["memset"][0] / max(prof["memset"][1], 1)
+
+    # end-to-end through the public API with pinned host buffers
+    xh = torch.as_tensor(inst.sky).pin_memory()
+    gh = torch.empty_like(xh).pin_memory()
+    eh = torch.empty((), dtype=torch.float64).pin_memory()
+    xd = torch.empty_like(x)
+
+    def e2e_step():
+        xd.copy_(xh, non_blocking=True)
+        plan.energy_and_grad(xd, need_grad=True, energy=energy, grad=grad)
+        gh.copy_(grad, non_blocking=True)
+        eh.copy_(energy, non_blocking=True)
+
+    for _ in range(3):
+        e2e_step()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    ke = max(1, min(args.steps, 50))
+    for _ in range(ke):
+        e2e_step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = ev0.elapsed_time(ev1) / ke
+    h2d = xh.numel() * xh.element_size()
+    d2h = gh.numel() * gh.element_size() + 8
+
+    # roofline of the dominant kernel
+    U = M * E * inst.n_patches ** 2
+    P = inst.P
+    spec = U * (P * P // 2 + P) * 8
+    fwd_bytes = spec + E * nx * nx * 4 + M * E * nx * nx * 4
+    adj_bytes = spec + M * E * nx * nx * 4 + E * nx * nx * 4
+    flops_unit = 2 * 5.0 * P * P * np.log2(P) + 6.0 * P * (P // 2)
+    flops = U * flops_unit
+    dom_name, dom_ms, dom_bytes = (("k_fused<float,192,forward>", fwd_ms, fwd_bytes)
+                                   if fwd_ms >= adj_ms else
+                                   ("k_fused<float,192,adjoint>", adj_ms, adj_bytes))
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    sm_mhz = clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    achieved = dom_bytes / (dom_ms / 1e3) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "fused_config2_traffic.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            tr = json.load(f)
+        traffic = tr.get("forward" if "forward" in dom_name else "adjoint")
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mpix/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded GRF sky, Moffat PSFs, Poisson counts)",
+        "config": dict(WORKLOAD, path=plan.path, parallelism="replicas" if world > 1 else "1gpu"),
+        "e2e": {"value": world * mpix / (e2e_ms / 1e3), "unit": "Mpix/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+        "gpu_launches": 3 * args.steps,
+        "clocks": clocks,
+        "kernels_ms": {"forward": fwd_ms, "adjoint": adj_ms, "likelihood": lik_ms,
+                       "memset": mem_ms},
+        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                     "traffic": traffic, "algorithmic_bytes": dom_bytes,
+                     "peak_source": peak_src,
+                     "fp32": {"achieved": flops / (dom_ms / 1e3) / 1e12, "peak": fp32_peak,
+                              "unit": "TFLOP/s",
+                              "frac": flops / (dom_ms / 1e3) / 1e12 / fp32_peak,
+                              "flops": flops,
+                              "peak_source": "152 SMs x 128 FP32 lanes x 2 x median SM clock"}},
+    }
+
+    if rank == 0 and not args.no_extras:
+        # accuracy vs the GPU FP64 unfused path and its speed
+        plan64 = ju.ResponsePlan(M, E, inst.shape, inst.n_patches, inst.margin,
+                                 dtype=torch.float64, path="plain", pixel_area=1.0, device=dev)
+        plan64.set_psf(inst.psf.astype(np.float64))
+        plan64.set_exposure(inst.exposure.astype(np.float64), inst.readmask)
+        plan64.set_data(data)
+        x64 = x.double()
+        rng = np.random.default_rng(5)
+        cot = torch.as_tensor(rng.normal(size=plan.readout_total), device=dev)
+
+        def rel(a, b):
+            return float(torch.linalg.norm(a.double() - b) / torch.linalg.norm(b))
+
+        err = {"forward": rel(plan.response(x), plan64.response(x64)),
+               "vjp": rel(plan.response_vjp(cot.float()), plan64.response_vjp(cot))}
+        e32, g32 = plan.energy_and_grad(x)
+        e64, g64 = plan64.energy_and_grad(x64)
+        err["energy"] = abs(float(e32) - float(e64)) / abs(float(e64))
+        err["grad"] = rel(g32, g64)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(2):
+            plan64.energy_and_grad(x64)
+        torch.cuda.synchronize()
+        fp64_ms = (time.perf_counter() - t0) / 2 * 1e3
+        plan64.close()
+        line["rel_err_vs_fp64_gpu"] = err
+        line["fp64_plain_ms_per_step"] = fp64_ms
+        line["speedup_vs_fp64_plain"] = fp64_ms / ms
+        # CPU baseline: the float64 restatement on a bounded sample
+        d0 = data[: plan.readout_sizes[0]]
+        per_e = d0.size // E
+        v, dt, smp = cpu_sample(inst, d0[:per_e], reps=1)
+        line["cpu_baseline"] = {"value": v, "unit": "Mpix/s", "cores": os.cpu_count(),
+                                "kind": "port",
+                                "sample": f"float64 numpy/scipy.fft restatement, module 0 x "
+                                          f"energy 0 ({nx}^2 px, {inst.n_patches ** 2} units), "
+                                          f"{dt:.2f} s"}
+    plan.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -138,6 +138,15 @@ JUBIK_API int jubik_poisson_energy_grad(jubik_plan* plan, const void* x, double*
 JUBIK_API int jubik_metric_apply(jubik_plan* plan, const void* x, const void* v, void* out,
                        void* stream);
 
+/* Profiling: when on, every kernel phase of a plan call is bracketed by CUDA
+ * events on the call's stream and its duration accumulated (the call then
+ * synchronises on the phase's end event).  Phases: 0 forward PSF kernel,
+ * 1 adjoint PSF kernel, 2 likelihood / readout kernels, 3 memsets. */
+#define JUBIK_PHASES 4
+JUBIK_API int jubik_plan_set_profiling(jubik_plan* plan, int32_t on);
+/* ms and launch counts per phase accumulated since profiling was switched on. */
+JUBIK_API int jubik_plan_profile(const jubik_plan* plan, double* ms, int64_t* launches);
+
 /* Stand-alone Poisson likelihood on readout vectors (jft.Poissonian(data)):
  * energy (device double[1]) = sum(lam - d log lam); grad (may be NULL) = 1 - d/lam. */
 JUBIK_API int jubik_poisson_energy(const void* lam, const int32_t* data, int64_t n, int32_t dtype,

@@ -56,6 +56,8 @@ _SIGS = {
     "jubik_plan_destroy": ([_vp], C.c_int),
     "jubik_plan_workspace_bytes": ([_vp, C.POINTER(_i64)], C.c_int),
     "jubik_plan_path": ([_vp, C.POINTER(_i32)], C.c_int),
+    "jubik_plan_set_profiling": ([_vp, _i32], C.c_int),
+    "jubik_plan_profile": ([_vp, C.POINTER(C.c_double), C.POINTER(_i64)], C.c_int),
     "jubik_plan_set_psf": ([_vp, _vp, _i32, _i32, _vp], C.c_int),
     "jubik_plan_set_exposure": ([_vp, _vp, _vp, _vp], C.c_int),
     "jubik_plan_readout_sizes": ([_vp, C.POINTER(_i64), C.POINTER(_i64)], C.c_int),

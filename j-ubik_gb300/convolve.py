@@ -125,7 +125,9 @@ def linpatch_plan(x_shape, kernel_shape, n_patches_per_axis, margin, dtype, n_mo
     return ent
 
 
-def _prepare_kernel(ent, kernel: torch.Tensor, E: int):
+def _prepare_kernel(ent, kernel: torch.Tensor, E: int, field):
+    """Kernels shaped like the field are full-field kernels (the reference's
+    input, cut by convolve.py:107-111); any other window is taken as pre-cut."""
     plan: ResponsePlan = ent["plan"]
     key = _kernel_key(kernel)
     if ent["psf_key"] == key:
@@ -135,7 +137,7 @@ def _prepare_kernel(ent, kernel: torch.Tensor, E: int):
         k = kernel.unsqueeze(0)
     else:
         k = kernel.reshape(1, n2, E, kernel.shape[-2], kernel.shape[-1])
-    plan.set_psf(k)
+    plan.set_psf(k, "full" if tuple(kernel.shape[-2:]) == tuple(field) else "precut")
     ent["psf_key"] = key
 
 
@@ -179,7 +181,7 @@ def linpatch_convolve(x, domain, kernel, n_patches_per_axis, margin):
         print("signal_shape:", (kt.shape[0],) + shape)
         print("Dimension Inconsistency. Broadcasting PSFs")
     ent = linpatch_plan(shape, tuple(kt.shape), n_patches_per_axis, margin, dtype)
-    _prepare_kernel(ent, kt, E)
+    _prepare_kernel(ent, kt, E, shape[-2:])
     plan = ent["plan"]
     xin = xt.reshape((E,) + shape[-2:])
     out = _LinpatchFn.apply(xin, plan)
@@ -193,8 +195,8 @@ def convolve(x, y, domain, axes):
     dtype = _float_dtype(x, y)
     xt = as_device(x, dtype, dev)
     yt = as_device(y, dtype, dev)
+    dlist = [domain.distances[i] for i in axes]  # as convolve.py:161 (negative axes allowed)
     axes = tuple(a % yt.dim() for a in axes)
-    dlist = [domain.distances[i] for i in axes]
     dvol = float(reduce(lambda a, b: a * b, dlist))
     if len(axes) not in (1, 2):
         raise NotImplementedError("convolve covers one or two axes")

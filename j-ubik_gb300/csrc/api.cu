@@ -212,6 +212,11 @@ struct jubik_plan {
   std::vector<int64_t> readout_sizes;
   int64_t readout_total = 0;
   std::vector<void*> allocs;
+  // profiling
+  bool prof = false;
+  cudaEvent_t ev_a[JUBIK_PHASES] = {}, ev_b[JUBIK_PHASES] = {};
+  double prof_ms[JUBIK_PHASES] = {0};
+  int64_t prof_n[JUBIK_PHASES] = {0};
 
   int alloc(void** p, size_t n) {
     if (n == 0) n = 16;
@@ -222,6 +227,10 @@ struct jubik_plan {
     return JUBIK_OK;
   }
   ~jubik_plan() {
+    for (int i = 0; i < JUBIK_PHASES; ++i) {
+      if (ev_a[i]) cudaEventDestroy(ev_a[i]);
+      if (ev_b[i]) cudaEventDestroy(ev_b[i]);
+    }
     for (void* p : allocs) cudaFree(p);
     fft1d_free(&fft);
   }
@@ -230,6 +239,27 @@ struct jubik_plan {
 namespace {
 
 inline cudaStream_t S(void* s) { return (cudaStream_t)s; }
+
+// Brackets one kernel phase with events when the plan profiles.
+struct Phase {
+  jubik_plan* p;
+  int k;
+  cudaStream_t s;
+  Phase(jubik_plan* p_, int k_, cudaStream_t s_) : p(p_), k(k_), s(s_) {
+    if (p->prof) cudaEventRecord(p->ev_a[k], s);
+  }
+  ~Phase() {
+    if (!p->prof) return;
+    cudaEventRecord(p->ev_b[k], s);
+    if (cudaEventSynchronize(p->ev_b[k]) == cudaSuccess) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, p->ev_a[k], p->ev_b[k]);
+      p->prof_ms[k] += ms;
+      p->prof_n[k] += 1;
+    }
+  }
+};
+
 
 int check_plan(const jubik_plan* p) {
   if (!p) {
@@ -245,10 +275,15 @@ int64_t image_elems(const jubik_plan* p) { return (int64_t)p->g.M * p->g.E * p->
 int do_forward(jubik_plan* p, const void* x, void* out, double scale, cudaStream_t s) {
   const Geom& g = p->g;
   if (p->path == JUBIK_PATH_FUSED) {
-    JUBIK_TRY_CUDA(cudaMemsetAsync(out, 0, image_elems(p) * p->esz, s));
+    {
+      Phase ph(p, 3, s);
+      JUBIK_TRY_CUDA(cudaMemsetAsync(out, 0, image_elems(p) * p->esz, s));
+    }
+    Phase ph(p, 0, s);
     FusedLaunch a{x, out, p->hmain, p->hnyq, p->tw, p->wt, scale};
     return fused_forward(g, p->dtype, a, s);
   }
+  Phase ph(p, 0, s);
   const bool f32 = p->dtype == JUBIK_F32;
   const int64_t n2p = (int64_t)g.n * g.n;
   JUBIK_TRY(f32 ? plain_sky_patches<float>(g, x, p->wt, p->zs, s)
@@ -271,10 +306,15 @@ int do_forward(jubik_plan* p, const void* x, void* out, double scale, cudaStream
 int do_adjoint(jubik_plan* p, const void* cot, void* out_x, double scale, cudaStream_t s) {
   const Geom& g = p->g;
   if (p->path == JUBIK_PATH_FUSED) {
-    JUBIK_TRY_CUDA(cudaMemsetAsync(out_x, 0, (size_t)g.E * g.pixels() * p->esz, s));
+    {
+      Phase ph(p, 3, s);
+      JUBIK_TRY_CUDA(cudaMemsetAsync(out_x, 0, (size_t)g.E * g.pixels() * p->esz, s));
+    }
+    Phase ph(p, 1, s);
     FusedLaunch a{cot, out_x, p->hmain, p->hnyq, p->tw, p->wt, scale};
     return fused_adjoint(g, p->dtype, a, s);
   }
+  Phase ph(p, 1, s);
   const bool f32 = p->dtype == JUBIK_F32;
   const int64_t n2p = (int64_t)g.n * g.n;
   for (int m0 = 0; m0 < g.M; m0 += p->zu_modules) {
@@ -459,6 +499,31 @@ int jubik_plan_path(const jubik_plan* plan, int32_t* path) {
   return JUBIK_OK;
 }
 
+int jubik_plan_set_profiling(jubik_plan* p, int32_t on) {
+  JUBIK_TRY(check_plan(p));
+  if (on && !p->ev_a[0]) {
+    for (int i = 0; i < JUBIK_PHASES; ++i) {
+      JUBIK_TRY_CUDA(cudaEventCreate(&p->ev_a[i]));
+      JUBIK_TRY_CUDA(cudaEventCreate(&p->ev_b[i]));
+    }
+  }
+  p->prof = on != 0;
+  for (int i = 0; i < JUBIK_PHASES; ++i) {
+    p->prof_ms[i] = 0.0;
+    p->prof_n[i] = 0;
+  }
+  return JUBIK_OK;
+}
+
+int jubik_plan_profile(const jubik_plan* p, double* ms, int64_t* launches) {
+  JUBIK_TRY(check_plan(p));
+  for (int i = 0; i < JUBIK_PHASES; ++i) {
+    if (ms) ms[i] = p->prof_ms[i];
+    if (launches) launches[i] = p->prof_n[i];
+  }
+  return JUBIK_OK;
+}
+
 int jubik_plan_set_psf(jubik_plan* p, const void* psf, int32_t layout, int32_t e_broadcast,
                        void* stream) {
   JUBIK_TRY(check_plan(p));
@@ -607,6 +672,7 @@ int jubik_response_forward(jubik_plan* p, const void* x, void* out_readout, void
   JUBIK_TRY(need(p->psf_set, "PSF"));
   cudaStream_t s = S(stream);
   JUBIK_TRY(do_forward(p, x, p->conv, p->desc.pixel_area, s));
+  Phase ph(p, 2, s);
   return p->dtype == JUBIK_F32
              ? readout_gather<float>(p->conv, p->eps, p->rlist, p->readout_total, out_readout, s)
              : readout_gather<double>(p->conv, p->eps, p->rlist, p->readout_total, out_readout, s);
@@ -620,12 +686,15 @@ int jubik_response_vjp(jubik_plan* p, const void* cot_readout, void* out_x, void
   JUBIK_TRY(check_plan(p));
   JUBIK_TRY(need(p->psf_set, "PSF"));
   cudaStream_t s = S(stream);
-  JUBIK_TRY_CUDA(cudaMemsetAsync(p->resid, 0, image_elems(p) * p->esz, s));
-  JUBIK_TRY(p->dtype == JUBIK_F32
-                ? readout_scatter<float>(cot_readout, p->eps, p->rlist, p->readout_total,
-                                         p->resid, s)
-                : readout_scatter<double>(cot_readout, p->eps, p->rlist, p->readout_total,
-                                          p->resid, s));
+  {
+    Phase ph(p, 2, s);
+    JUBIK_TRY_CUDA(cudaMemsetAsync(p->resid, 0, image_elems(p) * p->esz, s));
+    JUBIK_TRY(p->dtype == JUBIK_F32
+                  ? readout_scatter<float>(cot_readout, p->eps, p->rlist, p->readout_total,
+                                           p->resid, s)
+                  : readout_scatter<double>(cot_readout, p->eps, p->rlist, p->readout_total,
+                                            p->resid, s));
+  }
   return do_adjoint(p, p->resid, out_x, p->desc.pixel_area, s);
 }
 
@@ -637,6 +706,8 @@ int jubik_poisson_energy_grad(jubik_plan* p, const void* x, double* energy, void
   cudaStream_t s = S(stream);
   JUBIK_TRY(do_forward(p, x, p->conv, p->desc.pixel_area, s));
   const int64_t img = image_elems(p);
+  {
+  Phase ph(p, 2, s);
   JUBIK_TRY(p->dtype == JUBIK_F32
                 ? poisson_image<float>(p->conv, p->eps, p->ridx, p->data, img, nullptr, p->lam,
                                        grad_x ? p->resid : nullptr, p->partials, p->counter,
@@ -644,6 +715,7 @@ int jubik_poisson_energy_grad(jubik_plan* p, const void* x, double* energy, void
                 : poisson_image<double>(p->conv, p->eps, p->ridx, p->data, img, nullptr, p->lam,
                                         grad_x ? p->resid : nullptr, p->partials, p->counter,
                                         energy, s));
+  }
   p->lam_valid = true;
   if (!grad_x) return JUBIK_OK;
   return do_adjoint(p, p->resid, grad_x, p->desc.pixel_area, s);
@@ -669,9 +741,13 @@ int jubik_metric_apply(jubik_plan* p, const void* x, const void* v, void* out, v
   }
   JUBIK_TRY(need(p->lam_valid, "lambda (call with x or after poisson_energy_grad)"));
   JUBIK_TRY(do_forward(p, v, p->conv_v, p->desc.pixel_area, s));
-  JUBIK_TRY(p->dtype == JUBIK_F32
-                ? metric_weights<float>(p->conv_v, p->eps, p->ridx, p->lam, img, p->resid, s)
-                : metric_weights<double>(p->conv_v, p->eps, p->ridx, p->lam, img, p->resid, s));
+  {
+    Phase ph(p, 2, s);
+    JUBIK_TRY(p->dtype == JUBIK_F32
+                  ? metric_weights<float>(p->conv_v, p->eps, p->ridx, p->lam, img, p->resid, s)
+                  : metric_weights<double>(p->conv_v, p->eps, p->ridx, p->lam, img, p->resid,
+                                           s));
+  }
   return do_adjoint(p, p->resid, out, p->desc.pixel_area, s);
 }
 

@@ -112,6 +112,19 @@ class ResponsePlan:
     def _s(self):
         return stream_handle(self.device)
 
+    PHASES = ("forward", "adjoint", "likelihood", "memset")
+
+    def set_profiling(self, on: bool = True) -> None:
+        """Bracket every kernel phase with CUDA events (resets the totals)."""
+        _lib.call("jubik_plan_set_profiling", self._h, int(bool(on)))
+
+    def profile(self) -> dict:
+        """{phase: (total ms, launches)} since profiling was switched on."""
+        ms = (C.c_double * 4)()
+        n = (C.c_int64 * 4)()
+        _lib.call("jubik_plan_profile", self._h, ms, n)
+        return {name: (float(ms[i]), int(n[i])) for i, name in enumerate(self.PHASES)}
+
     def _refresh_readout(self):
         sizes = (C.c_int64 * self.n_modules)()
         tot = C.c_int64()
@@ -256,10 +269,10 @@ class ResponsePlan:
 
 
 def _wrap_device(address: int, n: int, typestr: str, device: torch.device) -> torch.Tensor:
-    """Read-only tensor view of n elements at a raw device address."""
+    """Tensor view of n elements at a raw device address (callers copy it)."""
 
     class _View:
         __cuda_array_interface__ = {"shape": (n,), "typestr": typestr,
-                                    "data": (address, True), "version": 3}
+                                    "data": (address, False), "version": 3}
 
     return torch.as_tensor(_View(), device=device)

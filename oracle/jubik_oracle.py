@@ -385,3 +385,23 @@ class Response:
         lam = self(x)
         rv = self(v)
         return self.adjoint([poisson_metric(l, t) for l, t in zip(lam, rv)])
+
+
+# ---------------------------------------------------------------- C restatement
+def linpatch_direct_c(x, kernel_precut, n_patches_per_axis, margin):
+    """Direct (non-FFT) C restatement of ``linpatch_convolve`` (oracle/direct_linpatch.c),
+    built by ``make -C oracle``.  x: (E, nx, ny); kernel (n^2, E, 2dx, 2dx)."""
+    import ctypes
+
+    here = os.path.dirname(os.path.abspath(__file__))
+    lib = ctypes.CDLL(os.path.join(here, "_build", "libjubik_oracle_c.so"))
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    k = np.ascontiguousarray(kernel_precut, dtype=np.float64)
+    E, nx, ny = x.shape
+    out = np.empty_like(x)
+    dp = ctypes.POINTER(ctypes.c_double)
+    st = lib.oracle_linpatch_direct(x.ctypes.data_as(dp), E, nx, ny, int(n_patches_per_axis),
+                                    int(margin), k.ctypes.data_as(dp), out.ctypes.data_as(dp))
+    if st != 0:
+        raise ValueError("invalid geometry")
+    return out

@@ -216,3 +216,18 @@ def test_golden_fixtures_reproduce():
         assert set(ref.files) == set(got)
         for k in ref.files:
             np.testing.assert_allclose(got[k], ref[k], rtol=1e-12, atol=1e-300, err_msg=name + k)
+
+
+# ---- two independent restatements agree (numpy FFT vs direct C convolution)
+@pytest.mark.parametrize("E,N,n,m", [(2, 48, 3, 8), (1, 21, 3, 2), (1, 36, 16, 2),
+                                     (2, 40, 4, 5), (1, 64, 4, 24)])
+def test_fft_oracle_matches_direct_c_restatement(E, N, n, m):
+    import subprocess
+    subprocess.run(["make", "-s", "-C", os.path.dirname(O.__file__)], check=True)
+    rng = np.random.default_rng(E * 1000 + N)
+    dx = N // n
+    x = rng.random((E, N, N))
+    k = rng.random((n * n, E, 2 * dx, 2 * dx))
+    a = O.linpatch_convolve(x, O.Domain((E, N, N), (1.0, 1.0, 1.0)), k, n, m, precut=True)
+    b = O.linpatch_direct_c(x, k, n, m)
+    np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-14 * np.abs(a).max())
