@@ -40,7 +40,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--path", choices=["auto", "fused", "plain"], default="auto")
+    ap.add_argument("--path", choices=["auto", "fused", "fused_unit", "plain"], default="auto")
     ap.add_argument("--nx", type=int, default=1024)
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the FP64 comparison and the CPU baseline")
@@ -235,10 +235,8 @@ def main():
         step()
     prof = plan.profile()
     plan.set_profiling(False)
-    fwd_ms = prof["forward"][0] / max(prof["forward"][1], 1)
-    adj_ms = prof["adjoint"][0] / max(prof["adjoint"][1], 1)
-    lik_ms = prof["likelihood"][0] / max(prof["likelihood"][1], 1)
-    mem_ms = prof["memset"][0] / max(prof["memset"][1], 1)
+    per_launch = {k: (v[0] / v[1] if v[1] else 0.0) for k, v in prof.items()}
+    launches_per_step = sum(v[1] for k, v in prof.items() if k != "memset") / nprof
 
     # end-to-end through the public API with pinned host buffers
     xh = torch.as_tensor(inst.sky).pin_memory()
@@ -265,17 +263,29 @@ def main():
     h2d = xh.numel() * xh.element_size()
     d2h = gh.numel() * gh.element_size() + 8
 
-    # roofline of the dominant kernel
+    # roofline of the dominant kernel (algorithmic = compulsory DRAM bytes per launch)
     U = M * E * inst.n_patches ** 2
+    NP = E * inst.n_patches ** 2
     P = inst.P
-    spec = U * (P * P // 2 + P) * 8
-    fwd_bytes = spec + E * nx * nx * 4 + M * E * nx * nx * 4
-    adj_bytes = spec + M * E * nx * nx * 4 + E * nx * nx * 4
-    flops_unit = 2 * 5.0 * P * P * np.log2(P) + 6.0 * P * (P // 2)
-    flops = U * flops_unit
-    dom_name, dom_ms, dom_bytes = (("k_fused<float,192,forward>", fwd_ms, fwd_bytes)
-                                   if fwd_ms >= adj_ms else
-                                   ("k_fused<float,192,adjoint>", adj_ms, adj_bytes))
+    spec = U * (P * P // 2 + P) * 8          # PSF spectra, read once per launch
+    pspec = NP * P * (P // 2) * 8            # shared patch spectra
+    img, sky = M * E * nx * nx * 4, E * nx * nx * 4
+    fft_unit = 5.0 * P * P * np.log2(P)      # one real 2-D FFT of side P (5 N log2 N / 2)
+    mul_unit = 6.0 * P * (P // 2)
+    shared = plan.shared_spectra
+    kinfo = {  # phase -> (kernel, bytes, flops)
+        "forward": ("k_fwd_from_spec<float,192>" if shared else "k_fused<float,192,fwd>",
+                    spec + (pspec if shared else sky) + img,
+                    U * (fft_unit * (1 if shared else 2) + mul_unit)),
+        "adjoint": ("k_adj_to_spec<float,192>" if shared else "k_fused<float,192,adj>",
+                    spec + img + (pspec if shared else sky),
+                    U * (fft_unit * (1 if shared else 2) + mul_unit)),
+        "forward_patch": ("k_sky_spec<float,192>", sky + pspec, NP * fft_unit),
+        "adjoint_patch": ("k_adj_from_spec<float,192>", pspec + sky, NP * fft_unit),
+    }
+    dom = max((k for k in kinfo if per_launch.get(k, 0.0) > 0), key=lambda k: per_launch[k])
+    dom_name, dom_bytes, flops = kinfo[dom]
+    dom_ms = per_launch[dom]
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -291,8 +301,7 @@ def main():
     tfile = os.path.join(ROOT, "profiles", "fused_config2_traffic.json")
     if os.path.exists(tfile):
         with open(tfile) as f:
-            tr = json.load(f)
-        traffic = tr.get("forward" if "forward" in dom_name else "adjoint")
+            traffic = json.load(f).get(dom_name)
 
     line = {
         "metric": METRIC, "value": value, "unit": "Mpix/s", "n_gpus": world,
@@ -302,10 +311,10 @@ def main():
         "config": dict(WORKLOAD, path=plan.path, parallelism="replicas" if world > 1 else "1gpu"),
         "e2e": {"value": world * mpix / (e2e_ms / 1e3), "unit": "Mpix/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
-        "gpu_launches": 3 * args.steps,
+        "gpu_launches": int(round(launches_per_step * args.steps)),
         "clocks": clocks,
-        "kernels_ms": {"forward": fwd_ms, "adjoint": adj_ms, "likelihood": lik_ms,
-                       "memset": mem_ms},
+        "kernels_ms": {(kinfo[k][0] if k in kinfo else k): v for k, v in per_launch.items()
+                       if prof[k][1]},
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved,
                      "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
                      "traffic": traffic, "algorithmic_bytes": dom_bytes,

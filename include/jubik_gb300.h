@@ -46,7 +46,9 @@ enum jubik_dtype { JUBIK_F32 = 0, JUBIK_F64 = 1 };
 enum jubik_path {
   JUBIK_PATH_AUTO = 0,  /* fused when the FFT side and dtype allow it */
   JUBIK_PATH_FUSED = 1, /* one kernel per patch unit: FFT, PSF product, overlap-add */
-  JUBIK_PATH_PLAIN = 2  /* unfused: batched FFT kernels + gather kernels */
+  JUBIK_PATH_PLAIN = 2, /* unfused: batched FFT kernels + gather kernels */
+  JUBIK_PATH_FUSED_UNIT = 3 /* fused, one kernel per (module, energy, patch) unit with no
+                               sharing of patch spectra across modules */
 };
 
 enum jubik_psf_layout {
@@ -140,9 +142,11 @@ JUBIK_API int jubik_metric_apply(jubik_plan* plan, const void* x, const void* v,
 
 /* Profiling: when on, every kernel phase of a plan call is bracketed by CUDA
  * events on the call's stream and its duration accumulated (the call then
- * synchronises on the phase's end event).  Phases: 0 forward PSF kernel,
- * 1 adjoint PSF kernel, 2 likelihood / readout kernels, 3 memsets. */
-#define JUBIK_PHASES 4
+ * synchronises on the phase's end event).  Phases: 0 forward per-unit PSF
+ * kernel, 1 adjoint per-unit PSF kernel, 2 likelihood / readout kernels,
+ * 3 memsets, 4 forward per-patch sky-spectrum kernel, 5 adjoint per-patch
+ * inverse kernel (4 and 5 run when modules share patch spectra). */
+#define JUBIK_PHASES 6
 JUBIK_API int jubik_plan_set_profiling(jubik_plan* plan, int32_t on);
 /* ms and launch counts per phase accumulated since profiling was switched on. */
 JUBIK_API int jubik_plan_profile(const jubik_plan* plan, double* ms, int64_t* launches);

@@ -22,7 +22,7 @@ ERR_ALLOC = -4
 ERR_STATE = -5
 
 F32, F64 = 0, 1
-PATH_AUTO, PATH_FUSED, PATH_PLAIN = 0, 1, 2
+PATH_AUTO, PATH_FUSED, PATH_PLAIN, PATH_FUSED_UNIT = 0, 1, 2, 3
 PSF_PRECUT, PSF_FULL = 0, 1
 
 

@@ -192,6 +192,7 @@ struct jubik_plan {
   void* hmain = nullptr;
   void* hnyq = nullptr;
   void* hfull = nullptr;
+  void* spec = nullptr;  // per-(energy, patch) spectra shared by the modules
   // images (M,E,nx,ny)
   void* conv = nullptr;
   void* conv_v = nullptr;
@@ -201,6 +202,7 @@ struct jubik_plan {
   int32_t* ridx = nullptr;
   int64_t* rlist = nullptr;
   int32_t* data = nullptr;
+  int32_t* dimg = nullptr;  // per-pixel counts, -1 where not read out
   double* partials = nullptr;
   unsigned int* counter = nullptr;
   // unfused work buffers
@@ -279,9 +281,17 @@ int do_forward(jubik_plan* p, const void* x, void* out, double scale, cudaStream
       Phase ph(p, 3, s);
       JUBIK_TRY_CUDA(cudaMemsetAsync(out, 0, image_elems(p) * p->esz, s));
     }
+    FusedLaunch a{x, out, p->hmain, p->hnyq, p->tw, p->wt, scale, p->spec};
+    if (!p->spec) {
+      Phase ph(p, 0, s);
+      return fused_run(g, p->dtype, a, FUSED_FWD_UNITS, s);
+    }
+    {
+      Phase ph(p, 4, s);
+      JUBIK_TRY(fused_run(g, p->dtype, a, FUSED_FWD_SKY, s));
+    }
     Phase ph(p, 0, s);
-    FusedLaunch a{x, out, p->hmain, p->hnyq, p->tw, p->wt, scale};
-    return fused_forward(g, p->dtype, a, s);
+    return fused_run(g, p->dtype, a, FUSED_FWD_FROM_SPEC, s);
   }
   Phase ph(p, 0, s);
   const bool f32 = p->dtype == JUBIK_F32;
@@ -310,9 +320,21 @@ int do_adjoint(jubik_plan* p, const void* cot, void* out_x, double scale, cudaSt
       Phase ph(p, 3, s);
       JUBIK_TRY_CUDA(cudaMemsetAsync(out_x, 0, (size_t)g.E * g.pixels() * p->esz, s));
     }
-    Phase ph(p, 1, s);
-    FusedLaunch a{cot, out_x, p->hmain, p->hnyq, p->tw, p->wt, scale};
-    return fused_adjoint(g, p->dtype, a, s);
+    FusedLaunch a{cot, out_x, p->hmain, p->hnyq, p->tw, p->wt, scale, p->spec};
+    if (!p->spec) {
+      Phase ph(p, 1, s);
+      return fused_run(g, p->dtype, a, FUSED_ADJ_UNITS, s);
+    }
+    {
+      Phase ph(p, 3, s);
+      JUBIK_TRY_CUDA(cudaMemsetAsync(p->spec, 0, fused_spec_bytes(g, p->dtype), s));
+    }
+    {
+      Phase ph(p, 1, s);
+      JUBIK_TRY(fused_run(g, p->dtype, a, FUSED_ADJ_TO_SPEC, s));
+    }
+    Phase ph(p, 5, s);
+    return fused_run(g, p->dtype, a, FUSED_ADJ_FROM_SPEC, s);
   }
   Phase ph(p, 1, s);
   const bool f32 = p->dtype == JUBIK_F32;
@@ -415,7 +437,19 @@ int jubik_plan_create(const jubik_plan_desc* d, jubik_plan** out) {
     set_error("fused path does not cover P=%d in this dtype", g.P);
     return JUBIK_ERR_UNSUPPORTED;
   }
+  if (d->path < JUBIK_PATH_AUTO || d->path > JUBIK_PATH_FUSED_UNIT) {
+    delete p;
+    set_error("unknown path %d", d->path);
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  if (d->path == JUBIK_PATH_FUSED_UNIT && !fused_ok) {
+    delete p;
+    set_error("fused path does not cover P=%d in this dtype", g.P);
+    return JUBIK_ERR_UNSUPPORTED;
+  }
   p->path = (d->path == JUBIK_PATH_PLAIN || !fused_ok) ? JUBIK_PATH_PLAIN : JUBIK_PATH_FUSED;
+  // modules share the patch spectra (sky forward, summed adjoint) when there are several
+  const bool share = p->path == JUBIK_PATH_FUSED && d->path != JUBIK_PATH_FUSED_UNIT && g.M >= 2;
 
   int st = JUBIK_OK;
   auto fail = [&](int s) {
@@ -445,6 +479,7 @@ int jubik_plan_create(const jubik_plan_desc* d, jubik_plan** out) {
   if (p->path == JUBIK_PATH_FUSED) {
     if ((st = p->alloc(&p->hmain, (size_t)units * g.P * (g.P / 2) * csz))) return fail(st);
     if ((st = p->alloc(&p->hnyq, (size_t)units * g.P * csz))) return fail(st);
+    if (share && (st = p->alloc(&p->spec, fused_spec_bytes(g, p->dtype)))) return fail(st);
   } else {
     if ((st = p->alloc(&p->hfull, (size_t)units * g.P * g.P * csz))) return fail(st);
     const int64_t n2p = (int64_t)g.n * g.n;
@@ -649,8 +684,10 @@ int jubik_plan_set_data(jubik_plan* p, const int32_t* counts, void* stream) {
     return JUBIK_ERR_INVALID_ARGUMENT;
   }
   if (!p->data) JUBIK_TRY(p->alloc((void**)&p->data, image_elems(p) * sizeof(int32_t)));
+  if (!p->dimg) JUBIK_TRY(p->alloc((void**)&p->dimg, image_elems(p) * sizeof(int32_t)));
   JUBIK_TRY_CUDA(cudaMemcpyAsync(p->data, counts, p->readout_total * sizeof(int32_t),
                                  cudaMemcpyDeviceToDevice, S(stream)));
+  JUBIK_TRY(count_image(p->ridx, p->data, image_elems(p), p->dimg, S(stream)));
   p->data_set = true;
   return JUBIK_OK;
 }
@@ -709,10 +746,10 @@ int jubik_poisson_energy_grad(jubik_plan* p, const void* x, double* energy, void
   {
   Phase ph(p, 2, s);
   JUBIK_TRY(p->dtype == JUBIK_F32
-                ? poisson_image<float>(p->conv, p->eps, p->ridx, p->data, img, nullptr, p->lam,
+                ? poisson_image<float>(p->conv, p->eps, p->dimg, img, p->lam,
                                        grad_x ? p->resid : nullptr, p->partials, p->counter,
                                        energy, s)
-                : poisson_image<double>(p->conv, p->eps, p->ridx, p->data, img, nullptr, p->lam,
+                : poisson_image<double>(p->conv, p->eps, p->dimg, img, p->lam,
                                         grad_x ? p->resid : nullptr, p->partials, p->counter,
                                         energy, s));
   }

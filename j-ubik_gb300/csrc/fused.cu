@@ -59,6 +59,7 @@ struct Args {
   const void* hnyq;
   const void* tw;
   const void* wt;
+  void* spec;  // (E n^2, P, P/2) spectra shared by the modules of a patch
   double scale;
   int M, E, nx, ny, n, dx, margin, half, sr_max, sc_max;
 };
@@ -95,6 +96,15 @@ __device__ __forceinline__ void red_add_v4(float* p, float a, float b, float c, 
                : "memory");
 }
 
+__device__ __forceinline__ void red_add_v2(float* p, float a, float b) {
+  asm volatile("red.global.add.v2.f32 [%0], {%1,%2};" ::"l"(p), "f"(a), "f"(b) : "memory");
+}
+__device__ __forceinline__ void red_add_cx(float2* p, float2 v) { red_add_v2((float*)p, v.x, v.y); }
+__device__ __forceinline__ void red_add_cx(double2* p, double2 v) {
+  atomicAdd(&p->x, v.x);
+  atomicAdd(&p->y, v.y);
+}
+
 // (a + conj(b)) / 2 and (a - conj(b)) / (2i)
 template <typename T>
 __device__ __forceinline__ cx<T> sp_a(cx<T> a, cx<T> b) {
@@ -120,100 +130,111 @@ __device__ __forceinline__ int rf(int y, int c) {
   return (y >> 1) * (P + 1) + (y & 1) * (P / 2) + c;
 }
 
-template <typename T, int P, bool ADJ>
-__global__ void __launch_bounds__(Tr<T, P>::NT) k_fused(Args a) {
+// Per-CTA view of one unit: geometry, warp class and its register twiddles.
+template <typename T, int P>
+struct Unit {
   using R = Tr<T, P>;
-  constexpr int L1 = R::L1, H = R::H, NT = R::NT, TP = R::TP, CH = R::CH, HL = L1 / 2;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  cx<T>* tile = reinterpret_cast<cx<T>*>(smem_raw);
-  cx<T>* stg = tile + R::TILE;
-  const int tid = threadIdx.x;
-  const int warp = tid >> 5, lane = tid & 31;
-  const int cls = warp;  // 16-point class of this warp
-
-  // unit u = ((e * n^2 + k) * M + m): the modules of one sky window are adjacent
-  const int n2p = a.n * a.n;
-  int u = blockIdx.x;
-  const int m = u % a.M;
-  u /= a.M;
-  const int k = u % n2p;
-  const int e = u / n2p;
-  const int sr = min((k % a.n) * a.dx, a.sr_max);
-  const int sc = min((k / a.n) * a.dx, a.sc_max);
-  const int rb = sr - a.half - a.margin;  // image row of FFT row 0
-  const int cb = sc - a.half - a.margin;  // image column of FFT column 0
-  const int K = 2 * a.dx;
-  const int mg = a.margin;
-  const int64_t hu = ((int64_t)m * n2p + k) * a.E + e;
-  const cx<T>* __restrict__ hmain = (const cx<T>*)a.hmain + hu * (int64_t)(P * H);
-  const cx<T>* __restrict__ hnyq = (const cx<T>*)a.hnyq + hu * (int64_t)P;
-  const T* __restrict__ wt = (const T*)a.wt;
-  const cx<T>* __restrict__ twg = (const cx<T>*)a.tw;
-  const int64_t npix = (int64_t)a.nx * a.ny;
-
-  if (tid == 0) {
-    prefetch_l2(hmain, (unsigned)(sizeof(cx<T>) * P * H));
-    prefetch_l2(hnyq, (unsigned)(sizeof(cx<T>) * P));
-  }
-  // this warp's twiddles w_P^(cls*q), q = 0..15
+  cx<T>* tile;
+  cx<T>* stg;
+  int tid, warp, lane, cls;
+  int m, e, k, rb, cb, K, mg;
+  int64_t npix;
+  const cx<T>* hmain;
+  const cx<T>* hnyq;
+  cx<T>* spec;  // this patch's shared spectrum (P rows x P/2 columns, A order)
+  const T* wt;
+  const cx<T>* twg;
   cx<T> wq[16];
-#pragma unroll
-  for (int q = 0; q < 16; ++q) wq[q] = ldg2(twg + cls * q);
 
-  // pairs holding input rows (forward: the window rows only)
+  // blockIdx -> (m, e, k); per_module == false decodes (e, k) only
+  __device__ __forceinline__ void init(const Args& a, unsigned char* smem, bool per_module) {
+    tile = reinterpret_cast<cx<T>*>(smem);
+    stg = tile + R::TILE;
+    tid = threadIdx.x;
+    warp = tid >> 5;
+    lane = tid & 31;
+    cls = warp;
+    const int n2p = a.n * a.n;
+    int u = blockIdx.x;
+    m = 0;
+    if (per_module) {
+      m = u % a.M;
+      u /= a.M;
+    }
+    k = u % n2p;
+    e = u / n2p;
+    const int sr = min((k % a.n) * a.dx, a.sr_max);
+    const int sc = min((k / a.n) * a.dx, a.sc_max);
+    rb = sr - a.half - a.margin;
+    cb = sc - a.half - a.margin;
+    K = 2 * a.dx;
+    mg = a.margin;
+    npix = (int64_t)a.nx * a.ny;
+    const int64_t hu = ((int64_t)m * n2p + k) * a.E + e;
+    hmain = (const cx<T>*)a.hmain + hu * (int64_t)(P * R::H);
+    hnyq = (const cx<T>*)a.hnyq + hu * (int64_t)P;
+    spec = a.spec ? (cx<T>*)a.spec + ((int64_t)e * n2p + k) * (int64_t)(P * R::H) : nullptr;
+    wt = (const T*)a.wt;
+    twg = (const cx<T>*)a.tw;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) wq[q] = ldg2(twg + cls * q);
+  }
+};
+
+// ---- input rows -> staging (cp.async) -> row step A (variant B forward)
+// forward: weighted sky window rows; adjoint: cotangent window rows.
+template <typename T, int P, bool ADJ>
+__device__ __forceinline__ void stage_input(Unit<T, P>& U, const Args& a) {
+  using R = Tr<T, P>;
+  constexpr int L1 = R::L1, H = R::H, NT = R::NT, TP = R::TP, CH = R::CH;
+  cx<T>* tile = U.tile;
+  cx<T>* stg = U.stg;
+  const int mg = U.mg, K = U.K;
   const int jlo = ADJ ? 0 : mg / 2;
   const int jhi = ADJ ? H : (mg + K + 1) / 2;
-
-  // ---- 1. input: staged chunks of pairs -> row step A (variant B forward)
   if (!ADJ) {
-    // zero the pairs outside the window rows
     const int nz_lo = jlo, nz_hi = H - jhi;
-    for (int i = tid; i < (nz_lo + nz_hi) * P; i += NT) {
+    for (int i = U.tid; i < (nz_lo + nz_hi) * P; i += NT) {
       const int jj = i / P, s = i - jj * P;
       const int j = jj < nz_lo ? jj : jhi + (jj - nz_lo);
       tile[j * TP + s] = mkc<T>((T)0, (T)0);
     }
   }
-  const int xoff = ADJ ? 0 : mg;     // staging column 0 = FFT column xoff
-  const int width = ADJ ? P : K;     // staged columns
-  // per-warp column weights of the 16 slots this class reads (forward)
+  const int xoff = ADJ ? 0 : mg;
+  const int width = ADJ ? P : K;
   T wc[16];
 #pragma unroll
   for (int q = 0; q < 16; ++q) {
-    const int xa = cls + L1 * q - mg;
-    wc[q] = (!ADJ && xa >= 0 && xa < K) ? wt[xa] : (T)0;
+    const int xa = U.cls + L1 * q - mg;
+    wc[q] = (!ADJ && xa >= 0 && xa < K) ? U.wt[xa] : (T)0;
   }
+  const T* __restrict__ src =
+      (const T*)a.in + (ADJ ? ((int64_t)U.m * a.E + U.e) : (int64_t)U.e) * U.npix;
   for (int j0 = jlo; j0 < jhi; j0 += CH) {
     const int nch = min(CH, jhi - j0);
-    {
-      // raw window rows (zero outside the field / window) -> staging, asynchronously
-      const T* __restrict__ src =
-          (const T*)a.in + (ADJ ? ((int64_t)m * a.E + e) : (int64_t)e) * npix;
-      for (int i = tid; i < nch * width; i += NT) {
-        const int jj = i / width, xs = i - jj * width;
-        const int col = cb + xoff + xs;
-        const int y0 = 2 * (j0 + jj);
-        const int row = rb + y0;
-        const bool cok = col >= 0 && col < a.ny;
-        const bool ok0 = cok && row >= 0 && row < a.nx && (ADJ || (y0 - mg >= 0 && y0 - mg < K));
-        const bool ok1 = cok && row + 1 >= 0 && row + 1 < a.nx &&
-                         (ADJ || (y0 + 1 - mg >= 0 && y0 + 1 - mg < K));
-        T* d = reinterpret_cast<T*>(stg + jj * TP + xs);
-        cp_async<T>(d, ok0 ? src + (int64_t)row * a.ny + col : src, ok0);
-        cp_async<T>(d + 1, ok1 ? src + (int64_t)(row + 1) * a.ny + col : src, ok1);
-      }
-      cp_async_wait_all();
-    }
-    __syncthreads();
-    // step A: items (pair, n1 = cls): x = cls + L1 q -> DFT16 -> twiddle -> slots 16 cls + k2
-    for (int jj = lane; jj < nch; jj += 32) {
+    for (int i = U.tid; i < nch * width; i += NT) {
+      const int jj = i / width, xs = i - jj * width;
+      const int col = U.cb + xoff + xs;
       const int y0 = 2 * (j0 + jj);
-      const T wr0 = (!ADJ && y0 - mg >= 0 && y0 - mg < K) ? wt[y0 - mg] : (T)0;
-      const T wr1 = (!ADJ && y0 + 1 - mg >= 0 && y0 + 1 - mg < K) ? wt[y0 + 1 - mg] : (T)0;
+      const int row = U.rb + y0;
+      const bool cok = col >= 0 && col < a.ny;
+      const bool ok0 = cok && row >= 0 && row < a.nx && (ADJ || (y0 - mg >= 0 && y0 - mg < K));
+      const bool ok1 = cok && row + 1 >= 0 && row + 1 < a.nx &&
+                       (ADJ || (y0 + 1 - mg >= 0 && y0 + 1 - mg < K));
+      T* d = reinterpret_cast<T*>(stg + jj * TP + xs);
+      cp_async<T>(d, ok0 ? src + (int64_t)row * a.ny + col : src, ok0);
+      cp_async<T>(d + 1, ok1 ? src + (int64_t)(row + 1) * a.ny + col : src, ok1);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    for (int jj = U.lane; jj < nch; jj += 32) {
+      const int y0 = 2 * (j0 + jj);
+      const T wr0 = (!ADJ && y0 - mg >= 0 && y0 - mg < K) ? U.wt[y0 - mg] : (T)0;
+      const T wr1 = (!ADJ && y0 + 1 - mg >= 0 && y0 + 1 - mg < K) ? U.wt[y0 + 1 - mg] : (T)0;
       cx<T> v[16];
 #pragma unroll
       for (int q = 0; q < 16; ++q) {
-        const int xs = cls + L1 * q - xoff;
+        const int xs = U.cls + L1 * q - xoff;
         if (xs >= 0 && xs < width) {
           const cx<T> t = stg[jj * TP + xs];
           // (w_row * w_col) * x, the order of weights * slices in convolve.py:89-90
@@ -223,17 +244,22 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fused(Args a) {
         }
       }
       Dft<16, false, T>::run(v);
-      cx<T>* dst = tile + (j0 + jj) * TP + 16 * cls;
+      cx<T>* dst = tile + (j0 + jj) * TP + 16 * U.cls;
 #pragma unroll
-      for (int q = 0; q < 16; ++q) dst[q] = q ? cmul<T>(v[q], wq[q]) : v[q];
+      for (int q = 0; q < 16; ++q) dst[q] = q ? cmul<T>(v[q], U.wq[q]) : v[q];
     }
     __syncthreads();
   }
+}
 
-  // ---- 2. row step B (DFT-L1 per class) fused with the real-to-complex split
-  for (int it = tid; it < H * 8; it += NT) {
+// ---- row step B (DFT-L1 per class) fused with the real-to-complex split
+template <typename T, int P>
+__device__ __forceinline__ void stage_split(Unit<T, P>& U) {
+  using R = Tr<T, P>;
+  constexpr int L1 = R::L1, H = R::H, NT = R::NT, TP = R::TP, HL = L1 / 2;
+  for (int it = U.tid; it < H * 8; it += NT) {
     const int j = it % H, kap = it / H;
-    cx<T>* row = tile + j * TP;
+    cx<T>* row = U.tile + j * TP;
     cx<T> va[L1], vb[L1];
     const int ca = kap == 0 ? 0 : kap, cbk = kap == 0 ? 8 : 16 - kap;
 #pragma unroll
@@ -268,187 +294,241 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fused(Args a) {
       }
     }
   }
-  __syncthreads();
+}
 
-  // ---- 3. column phase 1 (variant A forward): items (c, n2), DFT-L1 over n1
-  {
-    const int ylo = 2 * jlo, yhi = 2 * jhi;
-    for (int it = tid; it < H * 16; it += NT) {
-      const int c = it % H, n2 = it / H;
-      cx<T> v[L1];
+// ---- column phase 1 (variant A forward): items (c, n2), DFT-L1 over n1;
+// rows outside [ylo, yhi) are known zeros
+template <typename T, int P>
+__device__ __forceinline__ void stage_col1(Unit<T, P>& U, int ylo, int yhi) {
+  using R = Tr<T, P>;
+  constexpr int L1 = R::L1, H = R::H, NT = R::NT;
+  for (int it = U.tid; it < H * 16; it += NT) {
+    const int c = it % H, n2 = it / H;
+    cx<T> v[L1];
 #pragma unroll
-      for (int i = 0; i < L1; ++i) {
-        const int y = n2 + 16 * i;
-        v[i] = (y >= ylo && y < yhi) ? tile[rf<P>(y, c)] : mkc<T>((T)0, (T)0);
-      }
-      Dft<L1, false, T>::run(v);
-#pragma unroll
-      for (int i = 0; i < L1; ++i) tile[rf<P>(n2 + 16 * i, c)] = v[i];
+    for (int i = 0; i < L1; ++i) {
+      const int y = n2 + 16 * i;
+      v[i] = (y >= ylo && y < yhi) ? U.tile[rf<P>(y, c)] : mkc<T>((T)0, (T)0);
     }
+    Dft<L1, false, T>::run(v);
+#pragma unroll
+    for (int i = 0; i < L1; ++i) U.tile[rf<P>(n2 + 16 * i, c)] = v[i];
   }
-  __syncthreads();
+}
 
-  // ---- 4. phase 2 (class k1 = cls) + PSF product + inverse variant-B step A
-  for (int c = lane; c < H; c += 32) {
-    cx<T> hv[16];
-    if (c != 0) {
-#pragma unroll
-      for (int q = 0; q < 16; ++q) hv[q] = ldg2(hmain + (16 * cls + q) * H + c);
-    }
+// ---- column phase 2 (class k1 = warp): the spectrum-side step
+enum Mid { MID_FULL, MID_TO_SPEC, MID_FROM_SPEC, MID_TO_ACC, MID_FROM_ACC };
+
+template <typename T, int P, int MODE, bool ADJ>
+__device__ __forceinline__ void stage_mid(Unit<T, P>& U) {
+  constexpr int H = Tr<T, P>::H;
+  const int cls = U.cls;
+  for (int c = U.lane; c < H; c += 32) {
     cx<T> v[16];
+    cx<T> hv[16];
+    const bool prod = (MODE == MID_FULL || MODE == MID_FROM_SPEC || MODE == MID_TO_ACC) && c != 0;
+    if (prod) {
 #pragma unroll
-    for (int q = 0; q < 16; ++q) {
-      const cx<T> t = tile[rf<P>(16 * cls + q, c)];
-      v[q] = q ? cmul<T>(t, wq[q]) : t;
+      for (int q = 0; q < 16; ++q) hv[q] = ldg2(U.hmain + (16 * cls + q) * H + c);
     }
-    Dft<16, false, T>::run(v);
-    if (c != 0) {
+    if (MODE == MID_FROM_SPEC || MODE == MID_FROM_ACC) {
+#pragma unroll
+      for (int q = 0; q < 16; ++q) v[q] = U.spec[(16 * cls + q) * H + c];
+    } else {
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        const cx<T> t = U.tile[rf<P>(16 * cls + q, c)];
+        v[q] = q ? cmul<T>(t, U.wq[q]) : t;
+      }
+      Dft<16, false, T>::run(v);
+    }
+    if (MODE == MID_TO_SPEC) {
+#pragma unroll
+      for (int q = 0; q < 16; ++q) U.spec[(16 * cls + q) * H + c] = v[q];
+      continue;
+    }
+    if (prod) {
 #pragma unroll
       for (int q = 0; q < 16; ++q) v[q] = ADJ ? cmulc<T>(v[q], hv[q]) : cmul<T>(v[q], hv[q]);
+    }
+    if (MODE == MID_TO_ACC) {
+      if (c != 0) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) red_add_cx(U.spec + (16 * cls + q) * H + c, v[q]);
+      } else {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) U.tile[rf<P>(16 * cls + q, c)] = v[q];
+      }
+      continue;
+    }
+    // inverse variant-B step A (column 0 waits for its product unless accumulated)
+    if (c != 0 || MODE == MID_FROM_ACC) {
       Dft<16, true, T>::run(v);
 #pragma unroll
-      for (int q = 1; q < 16; ++q) v[q] = cmulc<T>(v[q], wq[q]);
+      for (int q = 1; q < 16; ++q) v[q] = cmulc<T>(v[q], U.wq[q]);
     }
 #pragma unroll
-    for (int q = 0; q < 16; ++q) tile[rf<P>(16 * cls + q, c)] = v[q];
+    for (int q = 0; q < 16; ++q) U.tile[rf<P>(16 * cls + q, c)] = v[q];
   }
-  __syncthreads();
+}
 
-  // ---- 5. column 0 (warp 0) || inverse variant-B step B for columns >= 1
-  if (warp == 0) {
-    // unpack W = A + iN into the kx = 0 and kx = P/2 spectra, multiply, repack
-    for (int ky = lane; ky <= H; ky += 32) {
-      const int s1 = 16 * (ky % L1) + ky / L1;
-      const cx<T> h0 = ldg2(hmain + s1 * H), hn = ldg2(hnyq + s1);
-      const cx<T> w1 = tile[rf<P>(s1, 0)];
-      if (ky == 0 || ky == H) {
-        const cx<T> A = ADJ ? cmulc<T>(mkc<T>(w1.x, (T)0), h0) : cmul<T>(mkc<T>(w1.x, (T)0), h0);
-        const cx<T> N = ADJ ? cmulc<T>(mkc<T>(w1.y, (T)0), hn) : cmul<T>(mkc<T>(w1.y, (T)0), hn);
+// ---- column 0: unpack W = A + iN into the kx = 0 and kx = P/2 spectra,
+// multiply by the PSF spectrum (conj for the adjoint), repack.  TO_ACC adds
+// the product to the shared accumulator; otherwise it continues with the
+// inverse column transform of column 0.  One warp.
+template <typename T, int P, bool ADJ, bool TO_ACC>
+__device__ __forceinline__ void stage_col0(Unit<T, P>& U) {
+  using R = Tr<T, P>;
+  constexpr int L1 = R::L1, H = R::H;
+  const int lane = U.lane;
+  cx<T>* tile = U.tile;
+  for (int ky = lane; ky <= H; ky += 32) {
+    const int s1 = 16 * (ky % L1) + ky / L1;
+    const cx<T> h0 = ldg2(U.hmain + s1 * H), hn = ldg2(U.hnyq + s1);
+    const cx<T> w1 = tile[rf<P>(s1, 0)];
+    if (ky == 0 || ky == H) {
+      const cx<T> A = ADJ ? cmulc<T>(mkc<T>(w1.x, (T)0), h0) : cmul<T>(mkc<T>(w1.x, (T)0), h0);
+      const cx<T> N = ADJ ? cmulc<T>(mkc<T>(w1.y, (T)0), hn) : cmul<T>(mkc<T>(w1.y, (T)0), hn);
+      if (TO_ACC)
+        red_add_cx(U.spec + s1 * H, cb_p<T>(A, N));
+      else
         tile[rf<P>(s1, 0)] = cb_p<T>(A, N);
+    } else {
+      const int km = P - ky;
+      const int s2 = 16 * (km % L1) + km / L1;
+      const cx<T> w2 = tile[rf<P>(s2, 0)];
+      cx<T> A = sp_a<T>(w1, w2), N = sp_b<T>(w1, w2);
+      A = ADJ ? cmulc<T>(A, h0) : cmul<T>(A, h0);
+      N = ADJ ? cmulc<T>(N, hn) : cmul<T>(N, hn);
+      if (TO_ACC) {
+        red_add_cx(U.spec + s1 * H, cb_p<T>(A, N));
+        red_add_cx(U.spec + s2 * H, cb_m<T>(A, N));
       } else {
-        const int km = P - ky;
-        const int s2 = 16 * (km % L1) + km / L1;
-        const cx<T> w2 = tile[rf<P>(s2, 0)];
-        cx<T> A = sp_a<T>(w1, w2), N = sp_b<T>(w1, w2);
-        A = ADJ ? cmulc<T>(A, h0) : cmul<T>(A, h0);
-        N = ADJ ? cmulc<T>(N, hn) : cmul<T>(N, hn);
         tile[rf<P>(s1, 0)] = cb_p<T>(A, N);
         tile[rf<P>(s2, 0)] = cb_m<T>(A, N);
       }
     }
-    __syncwarp();
-    // inverse step A for column 0 (lane = class k1)
-    if (lane < L1) {
-      cx<T> v[16];
-#pragma unroll
-      for (int q = 0; q < 16; ++q) v[q] = tile[rf<P>(16 * lane + q, 0)];
-      Dft<16, true, T>::run(v);
-#pragma unroll
-      for (int q = 1; q < 16; ++q) v[q] = cmulc<T>(v[q], ldg2(twg + lane * q));
-#pragma unroll
-      for (int q = 0; q < 16; ++q) tile[rf<P>(16 * lane + q, 0)] = v[q];
-    }
-    __syncwarp();
-    // inverse step B for column 0
-    if (lane < 16) {
-      cx<T> v[L1];
-#pragma unroll
-      for (int i = 0; i < L1; ++i) v[i] = tile[rf<P>(16 * i + lane, 0)];
-      Dft<L1, true, T>::run(v);
-#pragma unroll
-      for (int i = 0; i < L1; ++i) tile[rf<P>(16 * i + lane, 0)] = v[i];
-    }
   }
-  if (NT > 32 || warp == 0) {
-    // columns 1..H-1 by warps 1.. (all warps when there is only one)
-    const int t0 = NT > 32 ? tid - 32 : tid;
-    const int nt = NT > 32 ? NT - 32 : NT;
-    if (t0 >= 0) {
-      for (int it = t0; it < (H - 1) * 16; it += nt) {
-        const int c = 1 + it % (H - 1), q = it / (H - 1);
-        cx<T> v[L1];
+  if (TO_ACC) return;
+  __syncwarp();
+  if (lane < L1) {  // inverse step A, class = lane
+    cx<T> v[16];
 #pragma unroll
-        for (int i = 0; i < L1; ++i) v[i] = tile[rf<P>(16 * i + q, c)];
-        Dft<L1, true, T>::run(v);
+    for (int q = 0; q < 16; ++q) v[q] = tile[rf<P>(16 * lane + q, 0)];
+    Dft<16, true, T>::run(v);
 #pragma unroll
-        for (int i = 0; i < L1; ++i) tile[rf<P>(16 * i + q, c)] = v[i];
-      }
-    }
+    for (int q = 1; q < 16; ++q) v[q] = cmulc<T>(v[q], ldg2(U.twg + lane * q));
+#pragma unroll
+    for (int q = 0; q < 16; ++q) tile[rf<P>(16 * lane + q, 0)] = v[q];
   }
-  __syncthreads();
+  __syncwarp();
+  if (lane < 16) {  // inverse step B
+    cx<T> v[L1];
+#pragma unroll
+    for (int i = 0; i < L1; ++i) v[i] = tile[rf<P>(16 * i + lane, 0)];
+    Dft<L1, true, T>::run(v);
+#pragma unroll
+    for (int i = 0; i < L1; ++i) tile[rf<P>(16 * i + lane, 0)] = v[i];
+  }
+}
 
-  // ---- 6. combine (Hermitian pair rows) fused with inverse variant-A phase 1
-  {
-    const int jc_lo = ADJ ? mg / 2 : 0;
-    const int jc_hi = ADJ ? (mg + K + 1) / 2 : H;
-    const int ncp = jc_hi - jc_lo;
-    for (int it = tid; it < ncp * 8; it += NT) {
-      const int j = jc_lo + it % ncp, kap = it / ncp;
-      cx<T>* row = tile + j * TP;
-      cx<T> va[L1], vb[L1];
-      if (kap == 0) {
-        const cx<T> a0 = row[0], b0 = row[H];
-        va[0] = mkc<T>(a0.x, b0.x);
-        va[HL] = mkc<T>(a0.y, b0.y);
+// ---- inverse variant-B step B for columns [c0, H) by threads t0 of nt
+template <typename T, int P>
+__device__ __forceinline__ void stage_invB(Unit<T, P>& U, int c0, int t0, int nt) {
+  using R = Tr<T, P>;
+  constexpr int L1 = R::L1, H = R::H;
+  const int nc = H - c0;
+  for (int it = t0; it < nc * 16; it += nt) {
+    const int c = c0 + it % nc, q = it / nc;
+    cx<T> v[L1];
 #pragma unroll
-        for (int k1 = 1; k1 < HL; ++k1) {
-          const cx<T> A = row[16 * k1], B = row[16 * (k1 + HL)];
-          va[k1] = cb_p<T>(A, B);
-          va[L1 - k1] = cb_m<T>(A, B);
-        }
+    for (int i = 0; i < L1; ++i) v[i] = U.tile[rf<P>(16 * i + q, c)];
+    Dft<L1, true, T>::run(v);
 #pragma unroll
-        for (int k1 = 0; k1 < HL; ++k1) {
-          const cx<T> A = row[8 + 16 * k1], B = row[8 + 16 * (k1 + HL)];
-          vb[k1] = cb_p<T>(A, B);
-          vb[L1 - 1 - k1] = cb_m<T>(A, B);
-        }
-      } else {
+    for (int i = 0; i < L1; ++i) U.tile[rf<P>(16 * i + q, c)] = v[i];
+  }
+}
+
+// ---- combine (Hermitian pair rows) fused with inverse variant-A phase 1
+template <typename T, int P>
+__device__ __forceinline__ void stage_combine(Unit<T, P>& U, int jc_lo, int jc_hi) {
+  using R = Tr<T, P>;
+  constexpr int L1 = R::L1, H = R::H, NT = R::NT, TP = R::TP, HL = L1 / 2;
+  const int ncp = jc_hi - jc_lo;
+  for (int it = U.tid; it < ncp * 8; it += NT) {
+    const int j = jc_lo + it % ncp, kap = it / ncp;
+    cx<T>* row = U.tile + j * TP;
+    cx<T> va[L1], vb[L1];
+    if (kap == 0) {
+      const cx<T> a0 = row[0], b0 = row[H];
+      va[0] = mkc<T>(a0.x, b0.x);
+      va[HL] = mkc<T>(a0.y, b0.y);
 #pragma unroll
-        for (int k1 = 0; k1 < HL; ++k1) {
-          const cx<T> A = row[kap + 16 * k1], B = row[kap + 16 * (k1 + HL)];
-          va[k1] = cb_p<T>(A, B);
-          vb[L1 - 1 - k1] = cb_m<T>(A, B);
-          const cx<T> A2 = row[16 - kap + 16 * k1], B2 = row[16 - kap + 16 * (k1 + HL)];
-          vb[k1] = cb_p<T>(A2, B2);
-          va[L1 - 1 - k1] = cb_m<T>(A2, B2);
-        }
+      for (int k1 = 1; k1 < HL; ++k1) {
+        const cx<T> A = row[16 * k1], B = row[16 * (k1 + HL)];
+        va[k1] = cb_p<T>(A, B);
+        va[L1 - k1] = cb_m<T>(A, B);
       }
-      Dft<L1, true, T>::run(va);
-      Dft<L1, true, T>::run(vb);
-      const int ca = kap == 0 ? 0 : kap, cbk = kap == 0 ? 8 : 16 - kap;
 #pragma unroll
-      for (int i = 0; i < L1; ++i) {
-        row[ca + 16 * i] = va[i];
-        row[cbk + 16 * i] = vb[i];
+      for (int k1 = 0; k1 < HL; ++k1) {
+        const cx<T> A = row[8 + 16 * k1], B = row[8 + 16 * (k1 + HL)];
+        vb[k1] = cb_p<T>(A, B);
+        vb[L1 - 1 - k1] = cb_m<T>(A, B);
+      }
+    } else {
+#pragma unroll
+      for (int k1 = 0; k1 < HL; ++k1) {
+        const cx<T> A = row[kap + 16 * k1], B = row[kap + 16 * (k1 + HL)];
+        va[k1] = cb_p<T>(A, B);
+        vb[L1 - 1 - k1] = cb_m<T>(A, B);
+        const cx<T> A2 = row[16 - kap + 16 * k1], B2 = row[16 - kap + 16 * (k1 + HL)];
+        vb[k1] = cb_p<T>(A2, B2);
+        va[L1 - 1 - k1] = cb_m<T>(A2, B2);
       }
     }
+    Dft<L1, true, T>::run(va);
+    Dft<L1, true, T>::run(vb);
+    const int ca = kap == 0 ? 0 : kap, cbk = kap == 0 ? 8 : 16 - kap;
+#pragma unroll
+    for (int i = 0; i < L1; ++i) {
+      row[ca + 16 * i] = va[i];
+      row[cbk + 16 * i] = vb[i];
+    }
   }
-  __syncthreads();
+}
 
-  // ---- 7. inverse variant-A phase 2 -> natural-order staging -> global
+// ---- inverse variant-A phase 2 -> natural-order staging -> global
+// forward: overlap-add of the whole P x P patch into out[m][e];
+// adjoint: crop to the window, bilinear weights, scatter into out[e].
+template <typename T, int P, bool ADJ>
+__device__ __forceinline__ void stage_output(Unit<T, P>& U, const Args& a) {
+  using R = Tr<T, P>;
+  constexpr int L1 = R::L1, H = R::H, NT = R::NT, TP = R::TP, CH = R::CH;
+  cx<T>* stg = U.stg;
+  const int mg = U.mg, K = U.K, cb = U.cb, rb = U.rb;
   const T scale = (T)a.scale;
-  // 16-byte reductions need column groups aligned in memory and inside the field
   const bool vec4 = ((cb + (ADJ ? mg : 0)) % 4 == 0) && (a.ny % 4 == 0) &&
                     (((uintptr_t)a.out) % 16 == 0) && (ADJ ? K % 4 == 0 : true);
   const int jo_lo = ADJ ? mg / 2 : 0;
   const int jo_hi = ADJ ? (mg + K + 1) / 2 : H;
+  const T* wt = U.wt;
   for (int j0 = jo_lo; j0 < jo_hi; j0 += CH) {
     const int nch = min(CH, jo_hi - j0);
-    for (int jj = lane; jj < nch; jj += 32) {
-      const cx<T>* srcr = tile + (j0 + jj) * TP + 16 * cls;
+    for (int jj = U.lane; jj < nch; jj += 32) {
+      const cx<T>* srcr = U.tile + (j0 + jj) * TP + 16 * U.cls;
       cx<T> v[16];
 #pragma unroll
-      for (int q = 0; q < 16; ++q) v[q] = q ? cmulc<T>(srcr[q], wq[q]) : srcr[q];
+      for (int q = 0; q < 16; ++q) v[q] = q ? cmulc<T>(srcr[q], U.wq[q]) : srcr[q];
       Dft<16, true, T>::run(v);
 #pragma unroll
-      for (int q = 0; q < 16; ++q) stg[jj * TP + cls + L1 * q] = v[q];
+      for (int q = 0; q < 16; ++q) stg[jj * TP + U.cls + L1 * q] = v[q];
     }
     __syncthreads();
     if (!ADJ) {
-      T* __restrict__ dst = (T*)a.out + ((int64_t)m * a.E + e) * npix;
+      T* __restrict__ dst = (T*)a.out + ((int64_t)U.m * a.E + U.e) * U.npix;
       if (sizeof(T) == 4 && vec4) {
         // groups of 4 columns never straddle the field edge (cb, ny multiples of 4)
-        for (int i = tid; i < nch * (P / 4); i += NT) {
+        for (int i = U.tid; i < nch * (P / 4); i += NT) {
           const int jj = i / (P / 4), x = 4 * (i - jj * (P / 4));
           const int col = cb + x;
           if (col < 0 || col >= a.ny) continue;
@@ -463,7 +543,7 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fused(Args a) {
                        scale * z1.y, scale * z2.y, scale * z3.y);
         }
       } else {
-        for (int i = tid; i < nch * P; i += NT) {
+        for (int i = U.tid; i < nch * P; i += NT) {
           const int jj = i / P, x = i - jj * P;
           const int col = cb + x;
           if (col < 0 || col >= a.ny) continue;
@@ -475,9 +555,9 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fused(Args a) {
         }
       }
     } else {
-      T* __restrict__ dst = (T*)a.out + (int64_t)e * npix;
+      T* __restrict__ dst = (T*)a.out + (int64_t)U.e * U.npix;
       if (sizeof(T) == 4 && vec4) {
-        for (int i = tid; i < nch * (K / 4); i += NT) {
+        for (int i = U.tid; i < nch * (K / 4); i += NT) {
           const int jj = i / (K / 4), xa = 4 * (i - jj * (K / 4));
           const int x = xa + mg, col = cb + x;
           if (col < 0 || col >= a.ny) continue;
@@ -502,7 +582,7 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fused(Args a) {
           }
         }
       } else {
-        for (int i = tid; i < nch * K; i += NT) {
+        for (int i = U.tid; i < nch * K; i += NT) {
           const int jj = i / K, xa = i - jj * K;
           const int x = xa + mg, col = cb + x;
           if (col < 0 || col >= a.ny) continue;
@@ -521,8 +601,125 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fused(Args a) {
   }
 }
 
+// column 0 (warp 0) in parallel with the inverse step B of columns 1.. (other warps)
 template <typename T, int P, bool ADJ>
-int launch_one(const Geom& g, const FusedLaunch& f, cudaStream_t s) {
+__device__ __forceinline__ void stage_col0_and_invB(Unit<T, P>& U) {
+  constexpr int NT = Tr<T, P>::NT;
+  if (U.warp == 0) stage_col0<T, P, ADJ, false>(U);
+  if (NT > 32) {
+    if (U.warp > 0) stage_invB<T, P>(U, 1, U.tid - 32, NT - 32);
+  } else {
+    __syncwarp();
+    stage_invB<T, P>(U, 1, U.tid, NT);
+  }
+}
+
+__device__ __forceinline__ void prefetch_unit(const void* h, unsigned hb, const void* hn,
+                                              unsigned nb) {
+  if (threadIdx.x == 0) {
+    prefetch_l2(h, hb);
+    prefetch_l2(hn, nb);
+  }
+}
+
+// ================================================================= kernels
+// One CTA per unit: the whole forward or adjoint of one patch.
+template <typename T, int P, bool ADJ>
+__global__ void __launch_bounds__(Tr<T, P>::NT) k_fused(Args a) {
+  using R = Tr<T, P>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Unit<T, P> U;
+  U.init(a, smem_raw, true);
+  prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
+  stage_input<T, P, ADJ>(U, a);
+  stage_split<T, P>(U);
+  __syncthreads();
+  stage_col1<T, P>(U, ADJ ? 0 : 2 * (U.mg / 2), ADJ ? P : 2 * ((U.mg + U.K + 1) / 2));
+  __syncthreads();
+  stage_mid<T, P, MID_FULL, ADJ>(U);
+  __syncthreads();
+  stage_col0_and_invB<T, P, ADJ>(U);
+  __syncthreads();
+  stage_combine<T, P>(U, ADJ ? U.mg / 2 : 0, ADJ ? (U.mg + U.K + 1) / 2 : R::H);
+  __syncthreads();
+  stage_output<T, P, ADJ>(U, a);
+}
+
+// Forward, module-shared: the sky spectrum of each (energy, patch) once ...
+template <typename T, int P>
+__global__ void __launch_bounds__(Tr<T, P>::NT) k_sky_spec(Args a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Unit<T, P> U;
+  U.init(a, smem_raw, false);
+  stage_input<T, P, false>(U, a);
+  stage_split<T, P>(U);
+  __syncthreads();
+  stage_col1<T, P>(U, 2 * (U.mg / 2), 2 * ((U.mg + U.K + 1) / 2));
+  __syncthreads();
+  stage_mid<T, P, MID_TO_SPEC, false>(U);
+}
+
+// ... then, per unit, spectrum * PSF spectrum -> inverse -> overlap-add.
+template <typename T, int P>
+__global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_from_spec(Args a) {
+  using R = Tr<T, P>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Unit<T, P> U;
+  U.init(a, smem_raw, true);
+  prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
+  stage_mid<T, P, MID_FROM_SPEC, false>(U);
+  __syncthreads();
+  stage_col0_and_invB<T, P, false>(U);
+  __syncthreads();
+  stage_combine<T, P>(U, 0, R::H);
+  __syncthreads();
+  stage_output<T, P, false>(U, a);
+}
+
+// Adjoint, module-shared: per unit, cotangent spectrum * conj(PSF spectrum)
+// added into the patch's accumulator ...
+template <typename T, int P>
+__global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_to_spec(Args a) {
+  using R = Tr<T, P>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Unit<T, P> U;
+  U.init(a, smem_raw, true);
+  prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
+  stage_input<T, P, true>(U, a);
+  stage_split<T, P>(U);
+  __syncthreads();
+  stage_col1<T, P>(U, 0, P);
+  __syncthreads();
+  stage_mid<T, P, MID_TO_ACC, true>(U);
+  __syncthreads();
+  if (U.warp == 0) stage_col0<T, P, true, true>(U);
+}
+
+// ... then, per (energy, patch), one inverse transform -> window -> gradient.
+template <typename T, int P>
+__global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_from_spec(Args a) {
+  using R = Tr<T, P>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Unit<T, P> U;
+  U.init(a, smem_raw, false);
+  stage_mid<T, P, MID_FROM_ACC, true>(U);
+  __syncthreads();
+  stage_invB<T, P>(U, 0, U.tid, R::NT);
+  __syncthreads();
+  stage_combine<T, P>(U, U.mg / 2, (U.mg + U.K + 1) / 2);
+  __syncthreads();
+  stage_output<T, P, true>(U, a);
+}
+
+template <typename KernelT>
+int set_smem(KernelT kern, size_t smem) {
+  return cuda_status(
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+      "cudaFuncSetAttribute");
+}
+
+template <typename T, int P>
+int launch_one(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
   Args a;
   a.in = f.in;
   a.out = f.out;
@@ -530,6 +727,7 @@ int launch_one(const Geom& g, const FusedLaunch& f, cudaStream_t s) {
   a.hnyq = f.hnyq;
   a.tw = f.tw;
   a.wt = f.wt;
+  a.spec = f.spec;
   a.scale = f.scale;
   a.M = g.M;
   a.E = g.E;
@@ -541,32 +739,64 @@ int launch_one(const Geom& g, const FusedLaunch& f, cudaStream_t s) {
   a.half = g.half;
   a.sr_max = g.sr_max;
   a.sc_max = g.sc_max;
-  const size_t smem = Tr<T, P>::SMEM;
+  using R = Tr<T, P>;
+  const size_t smem = R::SMEM;
   static bool attr_set = false;
   if (!attr_set) {
-    JUBIK_TRY_CUDA(cudaFuncSetAttribute(k_fused<T, P, ADJ>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    JUBIK_TRY(set_smem(k_fused<T, P, false>, smem));
+    JUBIK_TRY(set_smem(k_fused<T, P, true>, smem));
+    JUBIK_TRY(set_smem(k_sky_spec<T, P>, smem));
+    JUBIK_TRY(set_smem(k_fwd_from_spec<T, P>, smem));
+    JUBIK_TRY(set_smem(k_adj_to_spec<T, P>, smem));
+    JUBIK_TRY(set_smem(k_adj_from_spec<T, P>, smem));
     attr_set = true;
   }
   const int64_t units = g.units();
+  const int64_t patches = (int64_t)g.E * g.n * g.n;
   if (units <= 0) return JUBIK_OK;
   if (units > 0x7fffffffLL) {
     set_error("too many patch units for one launch");
     return JUBIK_ERR_UNSUPPORTED;
   }
-  k_fused<T, P, ADJ><<<(unsigned)units, Tr<T, P>::NT, smem, s>>>(a);
-  return cuda_status(cudaGetLastError(), "k_fused launch");
+  if ((which != FUSED_FWD_UNITS && which != FUSED_ADJ_UNITS) && !f.spec) {
+    set_error("module-shared kernels need the spectrum workspace");
+    return JUBIK_ERR_STATE;
+  }
+  switch (which) {
+    case FUSED_FWD_UNITS:
+      k_fused<T, P, false><<<(unsigned)units, R::NT, smem, s>>>(a);
+      break;
+    case FUSED_ADJ_UNITS:
+      k_fused<T, P, true><<<(unsigned)units, R::NT, smem, s>>>(a);
+      break;
+    case FUSED_FWD_SKY:
+      k_sky_spec<T, P><<<(unsigned)patches, R::NT, smem, s>>>(a);
+      break;
+    case FUSED_FWD_FROM_SPEC:
+      k_fwd_from_spec<T, P><<<(unsigned)units, R::NT, smem, s>>>(a);
+      break;
+    case FUSED_ADJ_TO_SPEC:
+      k_adj_to_spec<T, P><<<(unsigned)units, R::NT, smem, s>>>(a);
+      break;
+    case FUSED_ADJ_FROM_SPEC:
+      k_adj_from_spec<T, P><<<(unsigned)patches, R::NT, smem, s>>>(a);
+      break;
+    default:
+      set_error("unknown fused stage %d", which);
+      return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  return cuda_status(cudaGetLastError(), "fused kernel launch");
 }
 
-template <typename T, bool ADJ>
-int dispatch(const Geom& g, const FusedLaunch& f, cudaStream_t s) {
+template <typename T>
+int dispatch(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
   switch (g.P) {
-    case 32: return launch_one<T, 32, ADJ>(g, f, s);
-    case 64: return launch_one<T, 64, ADJ>(g, f, s);
-    case 96: return launch_one<T, 96, ADJ>(g, f, s);
-    case 128: return launch_one<T, 128, ADJ>(g, f, s);
+    case 32: return launch_one<T, 32>(g, f, which, s);
+    case 64: return launch_one<T, 64>(g, f, which, s);
+    case 96: return launch_one<T, 96>(g, f, which, s);
+    case 128: return launch_one<T, 128>(g, f, which, s);
     case 192:
-      if constexpr (sizeof(T) == 4) return launch_one<T, 192, ADJ>(g, f, s);
+      if constexpr (sizeof(T) == 4) return launch_one<T, 192>(g, f, which, s);
       break;
     default: break;
   }
@@ -584,18 +814,19 @@ bool fused_supported(int P, int dtype) {
   }
 }
 
+size_t fused_spec_bytes(const Geom& g, int dtype) {
+  const size_t c = dtype == JUBIK_F32 ? 8 : 16;
+  return c * (size_t)g.E * g.n * g.n * g.P * (g.P / 2);
+}
+
 size_t fused_smem_bytes(int P, int dtype) {
   const size_t c = dtype == JUBIK_F32 ? 8 : 16;
   const size_t H = P / 2, TP = P + 1, CH = H < 32 ? H : 32;
   return c * (H * TP + CH * TP);
 }
 
-int fused_forward(const Geom& g, int dtype, const FusedLaunch& a, cudaStream_t s) {
-  return dtype == JUBIK_F32 ? dispatch<float, false>(g, a, s) : dispatch<double, false>(g, a, s);
-}
-
-int fused_adjoint(const Geom& g, int dtype, const FusedLaunch& a, cudaStream_t s) {
-  return dtype == JUBIK_F32 ? dispatch<float, true>(g, a, s) : dispatch<double, true>(g, a, s);
+int fused_run(const Geom& g, int dtype, const FusedLaunch& a, int which, cudaStream_t s) {
+  return dtype == JUBIK_F32 ? dispatch<float>(g, a, which, s) : dispatch<double>(g, a, which, s);
 }
 
 }  // namespace jubik

@@ -78,10 +78,18 @@ struct FusedLaunch {
   const void* tw;       // (P) complex twiddles
   const void* wt;       // (2*dx) bilinear weight vector
   double scale;
+  void* spec = nullptr; // (E n^2, P, P/2) shared spectra: module-shared kernels when set
 };
-int fused_forward(const Geom& g, int dtype, const FusedLaunch& a, cudaStream_t s);
-int fused_adjoint(const Geom& g, int dtype, const FusedLaunch& a, cudaStream_t s);
-int fused_prepare_attributes();
+size_t fused_spec_bytes(const Geom& g, int dtype);
+enum FusedStage {
+  FUSED_FWD_UNITS = 0,     // one kernel per unit, forward
+  FUSED_ADJ_UNITS = 1,     // one kernel per unit, adjoint
+  FUSED_FWD_SKY = 2,       // per (energy, patch): sky spectrum -> spec
+  FUSED_FWD_FROM_SPEC = 3, // per unit: spec * H -> inverse -> overlap-add
+  FUSED_ADJ_TO_SPEC = 4,   // per unit: cotangent spectrum * conj(H) -> spec (sum)
+  FUSED_ADJ_FROM_SPEC = 5  // per (energy, patch): spec -> inverse -> gradient
+};
+int fused_run(const Geom& g, int dtype, const FusedLaunch& a, int which, cudaStream_t s);
 
 // ------------------------------------------------------------------ ops
 template <typename T>
@@ -122,9 +130,11 @@ template <typename T>
 int readout_scatter(const void* vec, const void* eps, const int64_t* idx, int64_t nread,
                     void* img, cudaStream_t s);
 template <typename T>
-int poisson_image(const void* conv, const void* eps, const int32_t* ridx, const int32_t* data,
-                  int64_t npix, void* lam_out_readout, void* lam_cache, void* resid,
-                  double* partials, unsigned int* counter, double* energy, cudaStream_t s);
+int poisson_image(const void* conv, const void* eps, const int32_t* dimg, int64_t npix,
+                  void* lam_cache, void* resid, double* partials, unsigned int* counter,
+                  double* energy, cudaStream_t s);
+int count_image(const int32_t* ridx, const int32_t* data, int64_t npix, int32_t* dimg,
+                cudaStream_t s);
 template <typename T>
 int metric_weights(const void* conv_v, const void* eps, const int32_t* ridx, const void* lam_cache,
                    int64_t npix, void* resid, cudaStream_t s);

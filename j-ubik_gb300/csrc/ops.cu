@@ -433,44 +433,93 @@ __device__ __forceinline__ void block_reduce2(double a, double b, double* partia
     last = (done == gridDim.x - 1);
   }
   __syncthreads();
-  if (last && threadIdx.x == 0) {
-    __threadfence();
-    double s1 = 0.0, s2 = 0.0;
-    for (unsigned int i = 0; i < gridDim.x; ++i) {
-      s1 += ((volatile double*)partials)[2 * i];
-      s2 += ((volatile double*)partials)[2 * i + 1];
+  if (!last) return;
+  // the last block sums the block partials in a fixed order (deterministic)
+  __threadfence();
+  double p1 = 0.0, p2 = 0.0;
+  for (unsigned int i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
+    p1 += __ldcg(partials + 2 * i);
+    p2 += __ldcg(partials + 2 * i + 1);
+  }
+  sa[threadIdx.x] = p1;
+  sb[threadIdx.x] = p2;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      sa[threadIdx.x] += sa[threadIdx.x + w];
+      sb[threadIdx.x] += sb[threadIdx.x + w];
     }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
     // H = sum(lam) - vdot(d, log(lam))
-    if (energy) energy[0] = s1 - s2;
+    if (energy) energy[0] = sa[0] - sb[0];
     *counter = 0u;
   }
+}
+
+// One pass over the (M,E,nx,ny) images: lam = eps * conv where a pixel is read
+// out (count image >= 0), the energy terms, the residual eps * (1 - d/lam)
+// (0 elsewhere) and, optionally, lam itself for later metric products.
+template <typename T>
+__device__ __forceinline__ void poisson_px(T conv, T ep, int32_t d, T& lam_o, T& res_o,
+                                           Kahan<T>& s_lam, Kahan<T>& s_dlog) {
+  if (d < 0) {
+    res_o = (T)0;
+    lam_o = (T)0;
+    return;
+  }
+  const T lam = ep * conv;
+  const T dd = (T)d;
+  s_lam.add(lam);
+  s_dlog.add(dd * log(lam));
+  lam_o = lam;
+  res_o = ep * ((T)1 - dd / lam);
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kBlock)
     k_poisson_image(const T* __restrict__ conv, const T* __restrict__ eps,
-                    const int32_t* __restrict__ ridx, const int32_t* __restrict__ data,
-                    int64_t npix, T* __restrict__ lam_out, T* __restrict__ lam_cache,
+                    const int32_t* __restrict__ dimg, int64_t npix, T* __restrict__ lam_cache,
                     T* __restrict__ resid, double* partials, unsigned int* counter,
                     double* energy) {
   Kahan<T> s_lam, s_dlog;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t p0 = 0;
+  if constexpr (sizeof(T) == 4) {
+    // 4 pixels per thread with 16-byte accesses (all image bases are 16-byte aligned)
+    const int64_t n4 = npix / 4;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n4; g += stride) {
+      const float4 c = reinterpret_cast<const float4*>(conv)[g];
+      const float4 ep = eps ? reinterpret_cast<const float4*>(eps)[g] : make_float4(1, 1, 1, 1);
+      const int4 d = reinterpret_cast<const int4*>(dimg)[g];
+      float4 l, r;
+      poisson_px<T>(c.x, ep.x, d.x, l.x, r.x, s_lam, s_dlog);
+      poisson_px<T>(c.y, ep.y, d.y, l.y, r.y, s_lam, s_dlog);
+      poisson_px<T>(c.z, ep.z, d.z, l.z, r.z, s_lam, s_dlog);
+      poisson_px<T>(c.w, ep.w, d.w, l.w, r.w, s_lam, s_dlog);
+      if (resid) reinterpret_cast<float4*>(resid)[g] = r;
+      if (lam_cache) reinterpret_cast<float4*>(lam_cache)[g] = l;
+    }
+    p0 = n4 * 4;
+  }
+  for (int64_t p = p0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npix; p += stride) {
+    T l, r;
+    poisson_px<T>(conv[p], eps ? eps[p] : (T)1, dimg[p], l, r, s_lam, s_dlog);
+    if (resid) resid[p] = r;
+    if (lam_cache) lam_cache[p] = l;
+  }
+  block_reduce2(s_lam.value(), s_dlog.value(), partials, counter, energy);
+}
+
+// Count image: d[ridx[p]] where the pixel is read out, -1 elsewhere.
+__global__ void k_count_image(const int32_t* __restrict__ ridx, const int32_t* __restrict__ data,
+                              int64_t npix, int32_t* __restrict__ dimg) {
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npix;
        p += (int64_t)gridDim.x * blockDim.x) {
     const int32_t r = ridx[p];
-    if (r < 0) {
-      if (resid) resid[p] = (T)0;
-      continue;
-    }
-    const T ep = eps ? eps[p] : (T)1;
-    const T lam = ep * conv[p];
-    const T d = (T)data[r];
-    s_lam.add(lam);
-    s_dlog.add(d * log(lam));
-    if (lam_out) lam_out[r] = lam;
-    if (lam_cache) lam_cache[p] = lam;
-    if (resid) resid[p] = ep * ((T)1 - d / lam);
+    dimg[p] = r < 0 ? -1 : data[r];
   }
-  block_reduce2(s_lam.value(), s_dlog.value(), partials, counter, energy);
 }
 
 template <typename T>
@@ -642,13 +691,19 @@ int readout_scatter(const void* vec, const void* eps, const int64_t* idx, int64_
 }
 
 template <typename T>
-int poisson_image(const void* conv, const void* eps, const int32_t* ridx, const int32_t* data,
-                  int64_t npix, void* lam_out_readout, void* lam_cache, void* resid,
-                  double* partials, unsigned int* counter, double* energy, cudaStream_t s) {
-  k_poisson_image<T><<<kRedBlocks, kBlock, 0, s>>>((const T*)conv, (const T*)eps, ridx, data,
-                                                   npix, (T*)lam_out_readout, (T*)lam_cache,
-                                                   (T*)resid, partials, counter, energy);
+int poisson_image(const void* conv, const void* eps, const int32_t* dimg, int64_t npix,
+                  void* lam_cache, void* resid, double* partials, unsigned int* counter,
+                  double* energy, cudaStream_t s) {
+  k_poisson_image<T><<<kRedBlocks, kBlock, 0, s>>>((const T*)conv, (const T*)eps, dimg, npix,
+                                                   (T*)lam_cache, (T*)resid, partials, counter,
+                                                   energy);
   return cuda_status(cudaGetLastError(), "k_poisson_image");
+}
+
+int count_image(const int32_t* ridx, const int32_t* data, int64_t npix, int32_t* dimg,
+                cudaStream_t s) {
+  k_count_image<<<grid_for(npix), kBlock, 0, s>>>(ridx, data, npix, dimg);
+  return cuda_status(cudaGetLastError(), "k_count_image");
 }
 
 template <typename T>
@@ -698,9 +753,8 @@ int elementwise_op(int op, const void* a, const void* b, const int32_t* d, int64
                                  cudaStream_t);                                                  \
   template int readout_scatter<T>(const void*, const void*, const int64_t*, int64_t, void*,      \
                                   cudaStream_t);                                                 \
-  template int poisson_image<T>(const void*, const void*, const int32_t*, const int32_t*,        \
-                                int64_t, void*, void*, void*, double*, unsigned int*, double*,   \
-                                cudaStream_t);                                                   \
+  template int poisson_image<T>(const void*, const void*, const int32_t*, int64_t, void*, void*, \
+                                double*, unsigned int*, double*, cudaStream_t);                  \
   template int metric_weights<T>(const void*, const void*, const int32_t*, const void*, int64_t, \
                                  void*, cudaStream_t);                                           \
   template int poisson_vec<T>(const void*, const int32_t*, int64_t, double*, unsigned int*,      \

@@ -17,7 +17,8 @@ import torch
 from . import _lib
 
 _DTYPES = {torch.float32: _lib.F32, torch.float64: _lib.F64}
-_PATHS = {"auto": _lib.PATH_AUTO, "fused": _lib.PATH_FUSED, "plain": _lib.PATH_PLAIN}
+_PATHS = {"auto": _lib.PATH_AUTO, "fused": _lib.PATH_FUSED, "plain": _lib.PATH_PLAIN,
+          "fused_unit": _lib.PATH_FUSED_UNIT}
 
 
 def dtype_code(dtype: torch.dtype) -> int:
@@ -60,8 +61,10 @@ class ResponsePlan:
     Parameters mirror the reference: ``n_modules`` is the vmapped module axis
     of ``erosita_response.py:209-212``, ``shape`` the field ``Domain.shape[-2:]``,
     ``n_patches`` / ``margin`` those of ``linpatch_convolve``
-    (``jubik/convolve.py:66``).  ``path`` picks the fused single-kernel path
-    ("auto"/"fused") or the unfused one ("plain").
+    (``jubik/convolve.py:66``).  ``path`` picks the fused path ("auto"/"fused":
+    patch spectra shared across modules when there are several), the fused path
+    with one kernel per unit and no sharing ("fused_unit"), or the unfused one
+    ("plain").
     """
 
     def __init__(self, n_modules: int, n_energies: int, shape: Sequence[int], n_patches: int,
@@ -87,6 +90,7 @@ class ResponsePlan:
         p = C.c_int32()
         _lib.call("jubik_plan_path", self._h, C.byref(p))
         self.path = {1: "fused", 2: "plain"}[p.value]
+        self.shared_spectra = self.path == "fused" and path != "fused_unit" and self.n_modules >= 2
         self._refresh_readout()
         self._keep = []  # tensors the plan reads asynchronously
 
@@ -112,7 +116,7 @@ class ResponsePlan:
     def _s(self):
         return stream_handle(self.device)
 
-    PHASES = ("forward", "adjoint", "likelihood", "memset")
+    PHASES = ("forward", "adjoint", "likelihood", "memset", "forward_patch", "adjoint_patch")
 
     def set_profiling(self, on: bool = True) -> None:
         """Bracket every kernel phase with CUDA events (resets the totals)."""
@@ -120,8 +124,8 @@ class ResponsePlan:
 
     def profile(self) -> dict:
         """{phase: (total ms, launches)} since profiling was switched on."""
-        ms = (C.c_double * 4)()
-        n = (C.c_int64 * 4)()
+        ms = (C.c_double * len(self.PHASES))()
+        n = (C.c_int64 * len(self.PHASES))()
         _lib.call("jubik_plan_profile", self._h, ms, n)
         return {name: (float(ms[i]), int(n[i])) for i, name in enumerate(self.PHASES)}
 

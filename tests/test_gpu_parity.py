@@ -57,11 +57,11 @@ def oracle_cases():
 
 @pytest.mark.parametrize("case", CASES, ids=lambda c: f"P{2 * c[1] + 2 * c[2]}_M{c[3]}E{c[4]}")
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32], ids=["f64", "f32"])
-@pytest.mark.parametrize("path", ["fused", "plain"])
+@pytest.mark.parametrize("path", ["fused", "fused_unit", "plain"])
 def test_response_parity(cuda, oracle_cases, case, dtype, path):
     nx, dx, m, M, E = case
     P = 2 * dx + 2 * m
-    if path == "fused" and not ju._lib.load().jubik_fused_supported(P, 0 if dtype ==
+    if path.startswith("fused") and not ju._lib.load().jubik_fused_supported(P, 0 if dtype ==
                                                                     torch.float32 else 1):
         with pytest.raises(ju.JubikUnsupported):
             ju.ResponsePlan(M, E, (nx, nx), nx // dx, m, dtype=dtype, path=path)
