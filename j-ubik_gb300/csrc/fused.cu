@@ -321,13 +321,15 @@ enum Mid { MID_FULL, MID_TO_SPEC, MID_FROM_SPEC, MID_TO_ACC, MID_FROM_ACC };
 
 template <typename T, int P, int MODE, bool ADJ>
 __device__ __forceinline__ void stage_mid(Unit<T, P>& U) {
-  constexpr int H = Tr<T, P>::H;
+  constexpr int L1 = Tr<T, P>::L1, H = Tr<T, P>::H;
   const int cls = U.cls;
   for (int c = U.lane; c < H; c += 32) {
     cx<T> v[16];
     cx<T> hv[16];
-    const bool prod = (MODE == MID_FULL || MODE == MID_FROM_SPEC || MODE == MID_TO_ACC) && c != 0;
-    if (prod) {
+    const bool prod = MODE == MID_FULL || MODE == MID_FROM_SPEC || MODE == MID_TO_ACC;
+    // column 0 carries the packed kx = 0 / kx = P/2 columns: alpha / beta products
+    const bool col0 = c == 0 && (MODE == MID_FROM_SPEC || MODE == MID_TO_ACC);
+    if (prod && (c != 0 || col0)) {
 #pragma unroll
       for (int q = 0; q < 16; ++q) hv[q] = ldg2(U.hmain + (16 * cls + q) * H + c);
     }
@@ -347,22 +349,39 @@ __device__ __forceinline__ void stage_mid(Unit<T, P>& U) {
       for (int q = 0; q < 16; ++q) U.spec[(16 * cls + q) * H + c] = v[q];
       continue;
     }
-    if (prod) {
+    if (col0 && MODE == MID_FROM_SPEC) {
+      // W'(ky) = alpha W(ky) + beta conj(W(-ky)), W(-ky) read from the shared spectrum
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        const int ky = cls + L1 * q, km = (P - ky) % P;
+        const int sm = 16 * (km % L1) + km / L1;
+        const cx<T> wm = U.spec[sm * H];
+        const cx<T> be = ldg2(U.hnyq + 16 * cls + q);
+        v[q] = cadd<T>(cmul<T>(v[q], hv[q]), cmul<T>(cconj<T>(wm), be));
+      }
+    } else if (col0 && MODE == MID_TO_ACC) {
+      // scatter form of the conjugate product: W(ky) adds conj(alpha(ky)) W(ky) to
+      // ky and conj(beta(-ky)) conj(W(ky)) to -ky
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        const int ky = cls + L1 * q, km = (P - ky) % P;
+        const int sm = 16 * (km % L1) + km / L1;
+        const cx<T> bm = ldg2(U.hnyq + sm);
+        red_add_cx(U.spec + (16 * cls + q) * H, cmulc<T>(v[q], hv[q]));
+        red_add_cx(U.spec + sm * H, cconj<T>(cmul<T>(v[q], bm)));
+      }
+      continue;
+    } else if (prod && c != 0) {
 #pragma unroll
       for (int q = 0; q < 16; ++q) v[q] = ADJ ? cmulc<T>(v[q], hv[q]) : cmul<T>(v[q], hv[q]);
     }
     if (MODE == MID_TO_ACC) {
-      if (c != 0) {
 #pragma unroll
-        for (int q = 0; q < 16; ++q) red_add_cx(U.spec + (16 * cls + q) * H + c, v[q]);
-      } else {
-#pragma unroll
-        for (int q = 0; q < 16; ++q) U.tile[rf<P>(16 * cls + q, c)] = v[q];
-      }
+      for (int q = 0; q < 16; ++q) red_add_cx(U.spec + (16 * cls + q) * H + c, v[q]);
       continue;
     }
-    // inverse variant-B step A (column 0 waits for its product unless accumulated)
-    if (c != 0 || MODE == MID_FROM_ACC) {
+    // inverse variant-B step A; in MID_FULL column 0 waits for its product (stage_col0)
+    if (c != 0 || MODE != MID_FULL) {
       Dft<16, true, T>::run(v);
 #pragma unroll
       for (int q = 1; q < 16; ++q) v[q] = cmulc<T>(v[q], U.wq[q]);
@@ -372,44 +391,28 @@ __device__ __forceinline__ void stage_mid(Unit<T, P>& U) {
   }
 }
 
-// ---- column 0: unpack W = A + iN into the kx = 0 and kx = P/2 spectra,
-// multiply by the PSF spectrum (conj for the adjoint), repack.  TO_ACC adds
-// the product to the shared accumulator; otherwise it continues with the
-// inverse column transform of column 0.  One warp.
-template <typename T, int P, bool ADJ, bool TO_ACC>
+// ---- column 0 of the per-unit kernel: W'(ky) = alpha W(ky) + beta conj(W(-ky))
+// (conjugated coefficients for the adjoint), pairs (ky, -ky) per thread, then
+// the inverse column transform of column 0.  One warp.
+template <typename T, int P, bool ADJ>
 __device__ __forceinline__ void stage_col0(Unit<T, P>& U) {
   using R = Tr<T, P>;
   constexpr int L1 = R::L1, H = R::H;
   const int lane = U.lane;
   cx<T>* tile = U.tile;
+  auto mulc = [&](cx<T> a, cx<T> b) { return ADJ ? cmulc<T>(a, b) : cmul<T>(a, b); };
   for (int ky = lane; ky <= H; ky += 32) {
     const int s1 = 16 * (ky % L1) + ky / L1;
-    const cx<T> h0 = ldg2(U.hmain + s1 * H), hn = ldg2(U.hnyq + s1);
-    const cx<T> w1 = tile[rf<P>(s1, 0)];
-    if (ky == 0 || ky == H) {
-      const cx<T> A = ADJ ? cmulc<T>(mkc<T>(w1.x, (T)0), h0) : cmul<T>(mkc<T>(w1.x, (T)0), h0);
-      const cx<T> N = ADJ ? cmulc<T>(mkc<T>(w1.y, (T)0), hn) : cmul<T>(mkc<T>(w1.y, (T)0), hn);
-      if (TO_ACC)
-        red_add_cx(U.spec + s1 * H, cb_p<T>(A, N));
-      else
-        tile[rf<P>(s1, 0)] = cb_p<T>(A, N);
-    } else {
-      const int km = P - ky;
-      const int s2 = 16 * (km % L1) + km / L1;
-      const cx<T> w2 = tile[rf<P>(s2, 0)];
-      cx<T> A = sp_a<T>(w1, w2), N = sp_b<T>(w1, w2);
-      A = ADJ ? cmulc<T>(A, h0) : cmul<T>(A, h0);
-      N = ADJ ? cmulc<T>(N, hn) : cmul<T>(N, hn);
-      if (TO_ACC) {
-        red_add_cx(U.spec + s1 * H, cb_p<T>(A, N));
-        red_add_cx(U.spec + s2 * H, cb_m<T>(A, N));
-      } else {
-        tile[rf<P>(s1, 0)] = cb_p<T>(A, N);
-        tile[rf<P>(s2, 0)] = cb_m<T>(A, N);
-      }
+    const int km = (P - ky) % P;
+    const int s2 = 16 * (km % L1) + km / L1;
+    const cx<T> w1 = tile[rf<P>(s1, 0)], w2 = tile[rf<P>(s2, 0)];
+    const cx<T> a1 = ldg2(U.hmain + s1 * H), b1 = ldg2(U.hnyq + s1);
+    tile[rf<P>(s1, 0)] = cadd<T>(mulc(w1, a1), mulc(cconj<T>(w2), b1));
+    if (s2 != s1) {
+      const cx<T> a2 = ldg2(U.hmain + s2 * H), b2 = ldg2(U.hnyq + s2);
+      tile[rf<P>(s2, 0)] = cadd<T>(mulc(w2, a2), mulc(cconj<T>(w1), b2));
     }
   }
-  if (TO_ACC) return;
   __syncwarp();
   if (lane < L1) {  // inverse step A, class = lane
     cx<T> v[16];
@@ -605,7 +608,7 @@ __device__ __forceinline__ void stage_output(Unit<T, P>& U, const Args& a) {
 template <typename T, int P, bool ADJ>
 __device__ __forceinline__ void stage_col0_and_invB(Unit<T, P>& U) {
   constexpr int NT = Tr<T, P>::NT;
-  if (U.warp == 0) stage_col0<T, P, ADJ, false>(U);
+  if (U.warp == 0) stage_col0<T, P, ADJ>(U);
   if (NT > 32) {
     if (U.warp > 0) stage_invB<T, P>(U, 1, U.tid - 32, NT - 32);
   } else {
@@ -667,9 +670,10 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_from_spec(Args a) {
   Unit<T, P> U;
   U.init(a, smem_raw, true);
   prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
+  if (threadIdx.x == 32) prefetch_l2(U.spec, sizeof(cx<T>) * P * R::H);
   stage_mid<T, P, MID_FROM_SPEC, false>(U);
   __syncthreads();
-  stage_col0_and_invB<T, P, false>(U);
+  stage_invB<T, P>(U, 0, U.tid, R::NT);
   __syncthreads();
   stage_combine<T, P>(U, 0, R::H);
   __syncthreads();
@@ -691,8 +695,6 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_to_spec(Args a) {
   stage_col1<T, P>(U, 0, P);
   __syncthreads();
   stage_mid<T, P, MID_TO_ACC, true>(U);
-  __syncthreads();
-  if (U.warp == 0) stage_col0<T, P, true, true>(U);
 }
 
 // ... then, per (energy, patch), one inverse transform -> window -> gradient.

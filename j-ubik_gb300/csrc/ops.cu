@@ -76,7 +76,11 @@ __global__ void k_psf_to_cplx(const T* __restrict__ psf, int layout, int e_bcast
 
 // Spectrum (FP64, natural order) -> plan storage in dtype T, scaled by 1/P^2
 // (the 1/N of ifftn folded in).  hfull: (U,P,P) for the unfused path;
-// hmain/hnyq: half-spectrum rows in the fused kernel's 4-step order.
+// hmain/hnyq: half-spectrum rows in the fused kernel's 4-step order.  The
+// fused kernels carry the kx = 0 and kx = P/2 columns of a real signal packed
+// as W = A + iN; their product with the PSF is W' = alpha W + beta conj(W(-ky))
+// with alpha = (H0 + HN)/2 and beta = (H0 - HN)/2, which hmain column 0 and
+// hnyq store instead of H0 and HN.
 template <typename T>
 __global__ void k_spectra_store(const double2* __restrict__ buf, int P, int64_t u0, int64_t nu,
                                 cx<T>* __restrict__ hfull, cx<T>* __restrict__ hmain,
@@ -96,10 +100,18 @@ __global__ void k_spectra_store(const double2* __restrict__ buf, int P, int64_t 
     if (hfull) hfull[hu * P * P + rem] = w;
     if (hmain && kx <= H) {
       const int slot = 16 * (ky % L1) + ky / L1;
-      if (kx < H)
+      if (kx == 0 || kx == H) {
+        const double2 h0 = kx == 0 ? v : buf[i - H];
+        const double2 hn = kx == H ? v : buf[i + H];
+        const double2 al = make_double2(0.5 * (h0.x + hn.x) * sc, 0.5 * (h0.y + hn.y) * sc);
+        const double2 be = make_double2(0.5 * (h0.x - hn.x) * sc, 0.5 * (h0.y - hn.y) * sc);
+        if (kx == 0)
+          hmain[(hu * P + slot) * H] = mkc<T>((T)al.x, (T)al.y);
+        else
+          hnyq[hu * P + slot] = mkc<T>((T)be.x, (T)be.y);
+      } else if (kx < H) {
         hmain[(hu * P + slot) * H + kx] = w;
-      else
-        hnyq[hu * P + slot] = w;
+      }
     }
   }
 }
