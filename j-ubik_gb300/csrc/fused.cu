@@ -129,6 +129,11 @@ template <int P>
 __device__ __forceinline__ int rf(int y, int c) {
   return (y >> 1) * (P + 1) + (y & 1) * (P / 2) + c;
 }
+// Offset of row y0 + d from row y0 when y0 is even (d a compile-time constant).
+template <int P>
+__device__ __forceinline__ constexpr int rfd(int d) {
+  return (d >> 1) * (P + 1) + (d & 1) * (P / 2);
+}
 
 // Per-CTA view of one unit: geometry, warp class and its register twiddles.
 template <typename T, int P>
@@ -181,25 +186,38 @@ struct Unit {
   }
 };
 
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 // ---- input rows -> staging (cp.async) -> row step A (variant B forward)
 // forward: weighted sky window rows; adjoint: cotangent window rows.
+// Chunks of CH pairs are double-buffered when a part of the tile that the
+// current chunk does not write is free: the next chunk's loads then overlap
+// the current chunk's transform.  Buffers are pair rows of pitch TP: chunk c
+// uses the staging area (c even) or a tile region (c odd).
 template <typename T, int P, bool ADJ>
 __device__ __forceinline__ void stage_input(Unit<T, P>& U, const Args& a) {
   using R = Tr<T, P>;
   constexpr int L1 = R::L1, H = R::H, NT = R::NT, TP = R::TP, CH = R::CH;
   cx<T>* tile = U.tile;
-  cx<T>* stg = U.stg;
   const int mg = U.mg, K = U.K;
   const int jlo = ADJ ? 0 : mg / 2;
   const int jhi = ADJ ? H : (mg + K + 1) / 2;
-  if (!ADJ) {
-    const int nz_lo = jlo, nz_hi = H - jhi;
-    for (int i = U.tid; i < (nz_lo + nz_hi) * P; i += NT) {
-      const int jj = i / P, s = i - jj * P;
-      const int j = jj < nz_lo ? jj : jhi + (jj - nz_lo);
-      tile[j * TP + s] = mkc<T>((T)0, (T)0);
-    }
-  }
+  const int nchunks = (jhi - jlo + CH - 1) / CH;
+  const int nzero = H - (jhi - jlo);
+  // second buffer: adjoint with 3 chunks -> the last chunk's tile pairs;
+  // forward with 2 chunks -> the zero pairs outside the window rows
+  const bool db = ADJ ? (nchunks == 3) : (nchunks == 2 && nzero >= CH);
+  auto alt_pair = [&](int jj) -> int {  // tile pair holding row-pair jj of the odd chunk
+    if (ADJ) return 2 * CH + jj;
+    return jj < jlo ? jj : jhi + (jj - jlo);
+  };
+  auto bufp = [&](int c, int jj) -> cx<T>* {
+    return (db && (c & 1)) ? tile + alt_pair(jj) * TP : U.stg + jj * TP;
+  };
   const int xoff = ADJ ? 0 : mg;
   const int width = ADJ ? P : K;
   T wc[16];
@@ -210,33 +228,71 @@ __device__ __forceinline__ void stage_input(Unit<T, P>& U, const Args& a) {
   }
   const T* __restrict__ src =
       (const T*)a.in + (ADJ ? ((int64_t)U.m * a.E + U.e) : (int64_t)U.e) * U.npix;
-  for (int j0 = jlo; j0 < jhi; j0 += CH) {
+  auto issue = [&](int c) {
+    const int j0 = jlo + c * CH;
     const int nch = min(CH, jhi - j0);
-    for (int i = U.tid; i < nch * width; i += NT) {
-      const int jj = i / width, xs = i - jj * width;
+    if (NT % width == 0) {
+      // each thread owns one staged column and every (NT / width)-th pair row
+      const int xs = U.tid % width, jstep = NT / width;
       const int col = U.cb + xoff + xs;
-      const int y0 = 2 * (j0 + jj);
-      const int row = U.rb + y0;
       const bool cok = col >= 0 && col < a.ny;
-      const bool ok0 = cok && row >= 0 && row < a.nx && (ADJ || (y0 - mg >= 0 && y0 - mg < K));
-      const bool ok1 = cok && row + 1 >= 0 && row + 1 < a.nx &&
-                       (ADJ || (y0 + 1 - mg >= 0 && y0 + 1 - mg < K));
-      T* d = reinterpret_cast<T*>(stg + jj * TP + xs);
-      cp_async<T>(d, ok0 ? src + (int64_t)row * a.ny + col : src, ok0);
-      cp_async<T>(d + 1, ok1 ? src + (int64_t)(row + 1) * a.ny + col : src, ok1);
+      const T* gcol = src + (cok ? col : 0);
+      for (int jj = U.tid / width; jj < nch; jj += jstep) {
+        const int y0 = 2 * (j0 + jj);
+        const int row = U.rb + y0;
+        const bool ok0 = cok && row >= 0 && row < a.nx && (ADJ || (y0 - mg >= 0 && y0 - mg < K));
+        const bool ok1 = cok && row + 1 >= 0 && row + 1 < a.nx &&
+                         (ADJ || (y0 + 1 - mg >= 0 && y0 + 1 - mg < K));
+        T* d = reinterpret_cast<T*>(bufp(c, jj) + xs);
+        cp_async<T>(d, ok0 ? gcol + (int64_t)row * a.ny : src, ok0);
+        cp_async<T>(d + 1, ok1 ? gcol + (int64_t)(row + 1) * a.ny : src, ok1);
+      }
+    } else {
+      for (int i = U.tid; i < nch * width; i += NT) {
+        const int jj = i / width, xs = i - jj * width;
+        const int col = U.cb + xoff + xs;
+        const int y0 = 2 * (j0 + jj);
+        const int row = U.rb + y0;
+        const bool cok = col >= 0 && col < a.ny;
+        const bool ok0 =
+            cok && row >= 0 && row < a.nx && (ADJ || (y0 - mg >= 0 && y0 - mg < K));
+        const bool ok1 = cok && row + 1 >= 0 && row + 1 < a.nx &&
+                         (ADJ || (y0 + 1 - mg >= 0 && y0 + 1 - mg < K));
+        T* d = reinterpret_cast<T*>(bufp(c, jj) + xs);
+        cp_async<T>(d, ok0 ? src + (int64_t)row * a.ny + col : src, ok0);
+        cp_async<T>(d + 1, ok1 ? src + (int64_t)(row + 1) * a.ny + col : src, ok1);
+      }
     }
-    cp_async_wait_all();
+    cp_async_commit();
+  };
+  if (!ADJ && !db) {  // zero pairs outside the window rows (before step A writes)
+    for (int i = U.tid; i < nzero * P; i += NT) {
+      const int jj = i / P, sl = i - jj * P;
+      const int j = jj < jlo ? jj : jhi + (jj - jlo);
+      tile[j * TP + sl] = mkc<T>((T)0, (T)0);
+    }
+  }
+  issue(0);
+  if (db && nchunks > 1) issue(1);
+  for (int c = 0; c < nchunks; ++c) {
+    const int j0 = jlo + c * CH;
+    const int nch = min(CH, jhi - j0);
+    if (db && c + 1 < nchunks)
+      cp_async_wait<1>();
+    else
+      cp_async_wait<0>();
     __syncthreads();
     for (int jj = U.lane; jj < nch; jj += 32) {
       const int y0 = 2 * (j0 + jj);
       const T wr0 = (!ADJ && y0 - mg >= 0 && y0 - mg < K) ? U.wt[y0 - mg] : (T)0;
       const T wr1 = (!ADJ && y0 + 1 - mg >= 0 && y0 + 1 - mg < K) ? U.wt[y0 + 1 - mg] : (T)0;
+      const cx<T>* bsrc = bufp(c, jj);
       cx<T> v[16];
 #pragma unroll
       for (int q = 0; q < 16; ++q) {
         const int xs = U.cls + L1 * q - xoff;
         if (xs >= 0 && xs < width) {
-          const cx<T> t = stg[jj * TP + xs];
+          const cx<T> t = bsrc[xs];
           // (w_row * w_col) * x, the order of weights * slices in convolve.py:89-90
           v[q] = ADJ ? t : mkc<T>((wr0 * wc[q]) * t.x, (wr1 * wc[q]) * t.y);
         } else {
@@ -247,6 +303,19 @@ __device__ __forceinline__ void stage_input(Unit<T, P>& U, const Args& a) {
       cx<T>* dst = tile + (j0 + jj) * TP + 16 * U.cls;
 #pragma unroll
       for (int q = 0; q < 16; ++q) dst[q] = q ? cmul<T>(v[q], U.wq[q]) : v[q];
+    }
+    __syncthreads();
+    if (db) {
+      if (c + 2 < nchunks) issue(c + 2);  // into the buffer chunk c just released
+    } else if (c + 1 < nchunks) {
+      issue(c + 1);
+    }
+  }
+  if (!ADJ && db) {  // the zero pairs held chunk 1's rows; clear them now
+    for (int i = U.tid; i < nzero * P; i += NT) {
+      const int jj = i / P, sl = i - jj * P;
+      const int j = jj < jlo ? jj : jhi + (jj - jlo);
+      tile[j * TP + sl] = mkc<T>((T)0, (T)0);
     }
     __syncthreads();
   }
@@ -305,14 +374,15 @@ __device__ __forceinline__ void stage_col1(Unit<T, P>& U, int ylo, int yhi) {
   for (int it = U.tid; it < H * 16; it += NT) {
     const int c = it % H, n2 = it / H;
     cx<T> v[L1];
+    cx<T>* base = U.tile + rf<P>(n2, c);  // row n2 + 16 i is 8 i pairs further
 #pragma unroll
     for (int i = 0; i < L1; ++i) {
       const int y = n2 + 16 * i;
-      v[i] = (y >= ylo && y < yhi) ? U.tile[rf<P>(y, c)] : mkc<T>((T)0, (T)0);
+      v[i] = (y >= ylo && y < yhi) ? base[8 * i * (P + 1)] : mkc<T>((T)0, (T)0);
     }
     Dft<L1, false, T>::run(v);
 #pragma unroll
-    for (int i = 0; i < L1; ++i) U.tile[rf<P>(n2 + 16 * i, c)] = v[i];
+    for (int i = 0; i < L1; ++i) base[8 * i * (P + 1)] = v[i];
   }
 }
 
@@ -333,13 +403,14 @@ __device__ __forceinline__ void stage_mid(Unit<T, P>& U) {
 #pragma unroll
       for (int q = 0; q < 16; ++q) hv[q] = ldg2(U.hmain + (16 * cls + q) * H + c);
     }
+    cx<T>* tb = U.tile + rf<P>(16 * cls, c);  // rows 16 cls + q at rfd(q)
     if (MODE == MID_FROM_SPEC || MODE == MID_FROM_ACC) {
 #pragma unroll
       for (int q = 0; q < 16; ++q) v[q] = U.spec[(16 * cls + q) * H + c];
     } else {
 #pragma unroll
       for (int q = 0; q < 16; ++q) {
-        const cx<T> t = U.tile[rf<P>(16 * cls + q, c)];
+        const cx<T> t = tb[rfd<P>(q)];
         v[q] = q ? cmul<T>(t, U.wq[q]) : t;
       }
       Dft<16, false, T>::run(v);
@@ -387,7 +458,7 @@ __device__ __forceinline__ void stage_mid(Unit<T, P>& U) {
       for (int q = 1; q < 16; ++q) v[q] = cmulc<T>(v[q], U.wq[q]);
     }
 #pragma unroll
-    for (int q = 0; q < 16; ++q) U.tile[rf<P>(16 * cls + q, c)] = v[q];
+    for (int q = 0; q < 16; ++q) tb[rfd<P>(q)] = v[q];
   }
 }
 
@@ -435,20 +506,20 @@ __device__ __forceinline__ void stage_col0(Unit<T, P>& U) {
   }
 }
 
-// ---- inverse variant-B step B for columns [c0, H) by threads t0 of nt
-template <typename T, int P>
-__device__ __forceinline__ void stage_invB(Unit<T, P>& U, int c0, int t0, int nt) {
+// ---- inverse variant-B step B for columns [C0, H) by threads t0 of nt
+template <typename T, int P, int C0>
+__device__ __forceinline__ void stage_invB(Unit<T, P>& U, int t0, int nt) {
   using R = Tr<T, P>;
-  constexpr int L1 = R::L1, H = R::H;
-  const int nc = H - c0;
-  for (int it = t0; it < nc * 16; it += nt) {
-    const int c = c0 + it % nc, q = it / nc;
+  constexpr int L1 = R::L1, H = R::H, NC = H - C0;
+  for (int it = t0; it < NC * 16; it += nt) {
+    const int c = C0 + it % NC, q = it / NC;
+    cx<T>* base = U.tile + rf<P>(q, c);  // rows 16 i + q
     cx<T> v[L1];
 #pragma unroll
-    for (int i = 0; i < L1; ++i) v[i] = U.tile[rf<P>(16 * i + q, c)];
+    for (int i = 0; i < L1; ++i) v[i] = base[8 * i * (P + 1)];
     Dft<L1, true, T>::run(v);
 #pragma unroll
-    for (int i = 0; i < L1; ++i) U.tile[rf<P>(16 * i + q, c)] = v[i];
+    for (int i = 0; i < L1; ++i) base[8 * i * (P + 1)] = v[i];
   }
 }
 
@@ -507,7 +578,6 @@ template <typename T, int P, bool ADJ>
 __device__ __forceinline__ void stage_output(Unit<T, P>& U, const Args& a) {
   using R = Tr<T, P>;
   constexpr int L1 = R::L1, H = R::H, NT = R::NT, TP = R::TP, CH = R::CH;
-  cx<T>* stg = U.stg;
   const int mg = U.mg, K = U.K, cb = U.cb, rb = U.rb;
   const T scale = (T)a.scale;
   const bool vec4 = ((cb + (ADJ ? mg : 0)) % 4 == 0) && (a.ny % 4 == 0) &&
@@ -515,8 +585,11 @@ __device__ __forceinline__ void stage_output(Unit<T, P>& U, const Args& a) {
   const int jo_lo = ADJ ? mg / 2 : 0;
   const int jo_hi = ADJ ? (mg + K + 1) / 2 : H;
   const T* wt = U.wt;
-  for (int j0 = jo_lo; j0 < jo_hi; j0 += CH) {
+  // chunk c writes its natural-order rows into the staging area (c even) or
+  // into the tile pairs of chunk c-1, which its inverse transform already read
+  for (int j0 = jo_lo, c = 0; j0 < jo_hi; j0 += CH, ++c) {
     const int nch = min(CH, jo_hi - j0);
+    cx<T>* stg = (c & 1) ? U.tile + (j0 - CH) * TP : U.stg;
     for (int jj = U.lane; jj < nch; jj += 32) {
       const cx<T>* srcr = U.tile + (j0 + jj) * TP + 16 * U.cls;
       cx<T> v[16];
@@ -600,7 +673,6 @@ __device__ __forceinline__ void stage_output(Unit<T, P>& U, const Args& a) {
         }
       }
     }
-    __syncthreads();
   }
 }
 
@@ -610,10 +682,10 @@ __device__ __forceinline__ void stage_col0_and_invB(Unit<T, P>& U) {
   constexpr int NT = Tr<T, P>::NT;
   if (U.warp == 0) stage_col0<T, P, ADJ>(U);
   if (NT > 32) {
-    if (U.warp > 0) stage_invB<T, P>(U, 1, U.tid - 32, NT - 32);
+    if (U.warp > 0) stage_invB<T, P, 1>(U, U.tid - 32, NT - 32);
   } else {
     __syncwarp();
-    stage_invB<T, P>(U, 1, U.tid, NT);
+    stage_invB<T, P, 1>(U, U.tid, NT);
   }
 }
 
@@ -673,7 +745,7 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_from_spec(Args a) {
   if (threadIdx.x == 32) prefetch_l2(U.spec, sizeof(cx<T>) * P * R::H);
   stage_mid<T, P, MID_FROM_SPEC, false>(U);
   __syncthreads();
-  stage_invB<T, P>(U, 0, U.tid, R::NT);
+  stage_invB<T, P, 0>(U, U.tid, R::NT);
   __syncthreads();
   stage_combine<T, P>(U, 0, R::H);
   __syncthreads();
@@ -706,7 +778,7 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_from_spec(Args a) {
   U.init(a, smem_raw, false);
   stage_mid<T, P, MID_FROM_ACC, true>(U);
   __syncthreads();
-  stage_invB<T, P>(U, 0, U.tid, R::NT);
+  stage_invB<T, P, 0>(U, U.tid, R::NT);
   __syncthreads();
   stage_combine<T, P>(U, U.mg / 2, (U.mg + U.K + 1) / 2);
   __syncthreads();
