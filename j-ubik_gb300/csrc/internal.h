@@ -4,7 +4,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
-#include "../../include/jubik_gb300.h"
+#include "jubik_gb300.h"
 
 namespace jubik {
 
