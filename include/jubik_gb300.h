@@ -187,6 +187,20 @@ JUBIK_API int jubik_slice_patches_adjoint(const void* patches, int64_t batch, in
 JUBIK_API int jubik_convolve2d(const void* kernel, int64_t bk, const void* signal, int64_t bs, int32_t h,
                      int32_t w, double dvol, int32_t dtype, void* out, void* stream);
 
+/* jubik_convolve2d without any device allocation (no counterpart in the reference).
+ * For callers that cannot allocate device memory -- code under a framework that owns
+ * all device memory through its own pool (e.g. an XLA FFI handler), or a loop where
+ * cudaMalloc/cudaFree would synchronise the device.  All scratch (twiddles and the
+ * complex spectra of kernel and signal) comes from one static device array of
+ * JUBIK_NOALLOC_SCRATCH_BYTES per GPU, held until the process exits; inputs needing
+ * more scratch are rejected with JUBIK_ERR_INVALID_ARGUMENT.  The first call on a
+ * device looks up the array's address (set-up work: make it before any stream
+ * capture).  Every call shares the array: calls that overlap on the GPU race. */
+#define JUBIK_NOALLOC_SCRATCH_BYTES (16 * 1024 * 1024)
+JUBIK_API int jubik_convolve2d_noalloc(const void* kernel, int64_t bk, const void* signal,
+                                       int64_t bs, int32_t h, int32_t w, double dvol,
+                                       int32_t dtype, void* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -78,6 +78,8 @@ _SIGS = {
     "jubik_slice_patches_adjoint": ([_vp, _i64, _i32, _i32, _i32, _i32, _i32, _vp, _vp],
                                     C.c_int),
     "jubik_convolve2d": ([_vp, _i64, _vp, _i64, _i32, _i32, _dbl, _i32, _vp, _vp], C.c_int),
+    "jubik_convolve2d_noalloc": ([_vp, _i64, _vp, _i64, _i32, _i32, _dbl, _i32, _vp, _vp],
+                                 C.c_int),
 }
 
 _lib = None

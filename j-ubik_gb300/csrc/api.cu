@@ -156,6 +156,8 @@ std::vector<double> bilinear_vector(int K) {
   return b;
 }
 
+}  // namespace
+
 template <typename T>
 int convolve2d_run(const void* kernel, int64_t bk, const void* signal, int64_t bs, int64_t hw,
                    double dvol, const Fft1D& fh, const Fft1D& fw, void* zk, void* zs, void* out,
@@ -171,7 +173,13 @@ int convolve2d_run(const void* kernel, int64_t bk, const void* signal, int64_t b
   return cuda_status(cudaGetLastError(), "convolve2d");
 }
 
-}  // namespace
+
+template int convolve2d_run<float>(const void*, int64_t, const void*, int64_t, int64_t, double,
+                                   const Fft1D&, const Fft1D&, void*, void*, void*, cudaStream_t);
+template int convolve2d_run<double>(const void*, int64_t, const void*, int64_t, int64_t, double,
+                                    const Fft1D&, const Fft1D&, void*, void*, void*,
+                                    cudaStream_t);
+
 }  // namespace jubik
 
 using namespace jubik;

@@ -54,6 +54,9 @@ struct Fft1D {
 };
 int fft1d_init(Fft1D* f, int L);
 void fft1d_free(Fft1D* f);
+// Fills f for length L with twiddle tables in caller-provided device memory
+// (L float2 at tw32, L double2 at tw64) computed on the device: no allocation.
+int fft1d_init_external(Fft1D* f, int L, void* tw32, void* tw64, cudaStream_t s);
 bool fft_length_supported(int L);
 
 // In-place batched complex FFT of nseq sequences of length f.L; sequence q
@@ -145,5 +148,12 @@ template <typename T>
 int elementwise_op(int op, const void* a, const void* b, const int32_t* d, int64_t n, void* out,
                    cudaStream_t s);
 int energy_partials_count();
+
+// out (bs,h,w) = dvol * Re(ifft2(fft2(kernel) * fft2(signal))) with complex work
+// buffers zk (bk*h*w) and zs (bs*h*w) supplied by the caller.
+template <typename T>
+int convolve2d_run(const void* kernel, int64_t bk, const void* signal, int64_t bs, int64_t hw,
+                   double dvol, const Fft1D& fh, const Fft1D& fw, void* zk, void* zs, void* out,
+                   cudaStream_t s);
 
 }  // namespace jubik

@@ -209,6 +209,31 @@ int fft1d_init(Fft1D* f, int L) {
   return JUBIK_OK;
 }
 
+// Twiddles w_L^t = exp(-2 pi i t / L) computed on the device in FP64
+// (sincospi) and rounded once to FP32.
+__global__ void k_twiddles(float2* tw32, double2* tw64, int L) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < L; t += gridDim.x * blockDim.x) {
+    double s, c;
+    sincospi(2.0 * (double)t / (double)L, &s, &c);
+    tw64[t] = make_double2(c, -s);
+    tw32[t] = make_float2((float)c, (float)-s);
+  }
+}
+
+int fft1d_init_external(Fft1D* f, int L, void* tw32, void* tw64, cudaStream_t s) {
+  if (!fft_length_supported(L)) {
+    set_error("FFT length %d unsupported (needs prime factors <= %d and L <= %d)", L,
+              kMaxGenericRadix, kMaxL);
+    return JUBIK_ERR_UNSUPPORTED;
+  }
+  f->L = L;
+  factorize(L, &f->st);
+  f->tw32 = tw32;
+  f->tw64 = tw64;
+  k_twiddles<<<(L + 255) / 256, 256, 0, s>>>((float2*)tw32, (double2*)tw64, L);
+  return cuda_status(cudaGetLastError(), "k_twiddles");
+}
+
 void fft1d_free(Fft1D* f) {
   if (f->tw32) cudaFree(f->tw32);
   if (f->tw64) cudaFree(f->tw64);
