@@ -34,6 +34,15 @@ WORKLOAD = {"workload": "response_fwd_vjp_poisson", "field": [1024, 1024], "modu
 METRIC = "Mpix/s response fwd+VJP (1024²×7 modules×3 E); FP32 vs FP64, rel err ≤1e-6"
 
 
+def workload(nx):
+    """The workload dict for field side ``nx`` (n = nx / 64 patches per axis)."""
+    if nx == WORKLOAD["field"][0]:
+        return dict(WORKLOAD)
+    n = nx // WORKLOAD["patch_stride"]
+    return dict(WORKLOAD, field=[nx, nx], patches_per_axis=n,
+                l2=f"PSF spectra {7 * 3 * n * n * (192 * 96 + 192) * 8 / 1e6:.0f} MB per pass")
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -103,8 +112,10 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ CPU legs
-def cpu_sample(inst, data, reps=1):
-    """The float64 CPU restatement on module 0, energy 0 of the workload."""
+def cpu_sample(inst, data, min_seconds=0.0, max_reps=1000):
+    """The float64 CPU restatement on module 0, energy 0 of the workload,
+    repeated until ``min_seconds`` have passed (at least once).  Returns
+    (Mpix/s over all repetitions, seconds, repetitions)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import jubik_oracle as O
 
@@ -113,14 +124,14 @@ def cpu_sample(inst, data, reps=1):
     R = O.Response(dom, inst.psf[:1, :, :1], inst.n_patches, inst.margin,
                    inst.exposure[:1, :1], inst.readmask[:1, :1])
     x = inst.sky[:1].astype(np.float64)
-    best = None
-    for _ in range(reps):
-        t0 = time.perf_counter()
+    reps, t0 = 0, time.perf_counter()
+    while True:
         R.energy_and_grad(x, [data])
+        reps += 1
         dt = time.perf_counter() - t0
-        best = dt if best is None else min(best, dt)
-    mpix = nx * nx / 1e6
-    return mpix / best, best, mpix
+        if dt >= min_seconds or reps >= max_reps:
+            break
+    return reps * nx * nx / 1e6 / dt, dt, reps
 
 
 def run_reference(args, rank, world):
@@ -131,20 +142,23 @@ def run_reference(args, rank, world):
     inst = synthetic.config2(nx=args.nx, n_modules=1, n_energies=1)
     rng = np.random.default_rng(1)
     data = rng.poisson(inst.exposure[0, 0][inst.readmask[0, 0]] * 2.0).astype(np.int64)
-    for _ in range(max(0, min(args.warmup, 1))):
-        cpu_sample(inst, data)
-    times = []
-    steps = max(1, min(args.steps, 5))
-    for _ in range(steps):
-        v, dt, mpix = cpu_sample(inst, data)
-        times.append(dt)
+    # one step = one (module, energy) plane of the workload; the number of
+    # timed steps is capped so that the run stays within about two minutes
+    t_one = None
+    for _ in range(max(1, args.warmup)):
+        _, dt, _ = cpu_sample(inst, data)
+        t_one = dt if t_one is None else min(t_one, dt)
+        if dt > 20.0:
+            break
+    steps = max(1, min(args.steps, int(120.0 / max(t_one, 1e-3))))
+    times = [cpu_sample(inst, data)[1] for _ in range(steps)]
     t = statistics.median(times)
-    value = mpix / t
+    value = inst.shape[0] * inst.shape[1] / 1e6 / t
     cores = os.cpu_count()
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mpix/s",
-            "n_gpus": world, "steps": steps, "warmup": min(args.warmup, 1),
+            "n_gpus": world, "steps": steps, "warmup": max(1, args.warmup),
             "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": WORKLOAD,
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload(args.nx),
             "cpu_baseline": {"value": value, "unit": "Mpix/s", "cores": cores, "kind": "port",
                              "sample": "float64 numpy/scipy.fft restatement, module 0 x energy 0 "
                                        f"of the workload ({args.nx}^2 px, "
@@ -308,7 +322,8 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded GRF sky, Moffat PSFs, Poisson counts)",
-        "config": dict(WORKLOAD, path=plan.path, parallelism="replicas" if world > 1 else "1gpu"),
+        "config": dict(workload(args.nx), path=plan.path,
+                       parallelism="replicas" if world > 1 else "1gpu"),
         "e2e": {"value": world * mpix / (e2e_ms / 1e3), "unit": "Mpix/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
         "gpu_launches": int(round(launches_per_step * args.steps)),
@@ -359,12 +374,12 @@ def main():
         # CPU baseline: the float64 restatement on a bounded sample
         d0 = data[: plan.readout_sizes[0]]
         per_e = d0.size // E
-        v, dt, smp = cpu_sample(inst, d0[:per_e], reps=1)
+        v, dt, reps = cpu_sample(inst, d0[:per_e], min_seconds=10.0)
         line["cpu_baseline"] = {"value": v, "unit": "Mpix/s", "cores": os.cpu_count(),
                                 "kind": "port",
                                 "sample": f"float64 numpy/scipy.fft restatement, module 0 x "
                                           f"energy 0 ({nx}^2 px, {inst.n_patches ** 2} units), "
-                                          f"{dt:.2f} s"}
+                                          f"{reps} repetitions in {dt:.1f} s"}
     plan.close()
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -234,6 +234,14 @@ class ResponsePlan:
         _lib.call("jubik_response_forward", self._h, ptr(x), ptr(out), self._s())
         return out
 
+    def response_jvp(self, t, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """Tangent of the (linear) response at any point: R(t)."""
+        t = self._sky(t)
+        if out is None:
+            out = torch.empty(self.readout_total, dtype=self.dtype, device=self.device)
+        _lib.call("jubik_response_jvp", self._h, ptr(t), ptr(out), self._s())
+        return out
+
     def response_vjp(self, cot, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         c = as_device(cot, self.dtype, self.device).reshape(-1)
         if c.numel() != self.readout_total:

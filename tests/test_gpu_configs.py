@@ -1,0 +1,225 @@
+"""The named workloads end to end on the GPU, against the float64 oracle.
+
+- 256^2, one module, one energy, 8x8 patches of stride 32 with margin 16
+  (FFT side 96): response and Poisson likelihood in FP64 and FP32, and the
+  literal full-field kernel path.
+- 1024^2 x 3 energies, correlated-field sky, 16x16 patches, margin 32:
+  JVP, VJP and MGVI metric, and central finite differences (eps = 1e-4) of
+  the Poisson energy along 32 random directions.
+- 2048^2 x 3 energies with 0.1 % point sources (flux 1e1 .. 1e5) and
+  power-law PSF wings, 32x32 patches: FP32 against FP64 per energy.
+- 1024^2 x 7 modules x 3 energies (the benchmark workload) at full size:
+  size-independent properties (adjoint identity, linearity, FP32 vs FP64)
+  and one module x energy plane against the oracle.
+
+Tolerances: FP64 1e-12 relative L2 (1e-11 for gradients, 1e-10 for the
+metric), FP32 1e-6; the FP32 Poisson gradient is bounded by the conditioning
+of 1 - d/lam (5e-4).
+"""
+import numpy as np
+import pytest
+import torch
+
+import jubik_oracle as O
+import jubik_gb300 as ju
+from jubik_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+
+F32, F64 = torch.float32, torch.float64
+
+
+def rel(a, b):
+    a = a.detach().double().cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+    b = b.detach().double().cpu().numpy() if isinstance(b, torch.Tensor) else np.asarray(b)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def make_plan(inst, dtype, path="auto", pixel_area=1.0, psf=None, layout="auto"):
+    plan = ju.ResponsePlan(inst.n_modules, inst.n_energies, inst.shape, inst.n_patches,
+                           inst.margin, dtype=dtype, path=path, pixel_area=pixel_area)
+    plan.set_psf(inst.psf if psf is None else psf, layout)
+    plan.set_exposure(inst.exposure, inst.readmask)
+    return plan
+
+
+# ------------------------------------------------------------------ 256^2, P = 96
+@pytest.fixture(scope="module")
+def small_case():
+    inst = synthetic.config1()
+    dom = O.Domain((1, 256, 256), (1.0, 1.0, 1.0))
+    R = O.Response(dom, inst.psf, inst.n_patches, inst.margin, inst.exposure, inst.readmask)
+    lam = R(inst.sky)
+    data = [synthetic.poisson_data(lam[0], 1)]
+    e, g = R.energy_and_grad(inst.sky, data)
+    return dict(inst=inst, R=R, lam=lam[0], data=data[0], energy=e, grad=g)
+
+
+@pytest.mark.parametrize("dtype", [F64, F32], ids=["f64", "f32"])
+@pytest.mark.parametrize("path", ["fused", "plain"])
+def test_small_field_response_and_likelihood(cuda, small_case, dtype, path):
+    c = small_case
+    plan = make_plan(c["inst"], dtype, path)
+    try:
+        plan.set_data(c["data"])
+        tol = 1e-12 if dtype == F64 else 1e-6
+        assert rel(plan.response(c["inst"].sky), c["lam"]) < tol
+        e, g = plan.energy_and_grad(c["inst"].sky)
+        assert abs(float(e) - c["energy"]) / abs(c["energy"]) < tol
+        assert rel(g, c["grad"]) < (1e-11 if dtype == F64 else 5e-4)
+    finally:
+        plan.close()
+
+
+def test_small_field_full_kernels_literal_path(cuda, small_case):
+    """Full-field (n^2, E, N, N) kernels through the literal shift / cut / pad
+    sequence of the oracle, against the GPU plan fed the same full kernels."""
+    inst = small_case["inst"]
+    nx, n = inst.shape[0], inst.n_patches
+    dx = nx // n
+    K = 2 * dx
+    full = np.zeros(inst.psf.shape[:3] + (nx, nx))
+    a = (np.arange(K) - dx) % nx
+    full[..., a[:, None], a[None, :]] = inst.psf
+    dom = O.Domain((1, nx, nx), (1.0, 1.0, 1.0))
+    ref = O.linpatch_convolve(inst.sky, dom, full[0], n, inst.margin, precut=False)
+    for dtype, tol in ((F64, 1e-12), (F32, 1e-6)):
+        plan = make_plan(inst, dtype, psf=full, layout="full")
+        assert rel(plan.psf_forward(inst.sky)[0], ref) < tol
+        plan.close()
+
+
+# ------------------------------------------------------ 1024^2 x 3, derivatives
+@pytest.fixture(scope="module")
+def deriv_case():
+    inst = synthetic.config3()
+    E, nx = inst.n_energies, inst.shape[0]
+    dom = O.Domain((E, nx, nx), (1.0, 1.0, 1.0))
+    R = O.Response(dom, inst.psf, inst.n_patches, inst.margin, inst.exposure, inst.readmask)
+    lam = R(inst.sky)
+    data = [synthetic.poisson_data(lam[0], 3)]
+    rng = np.random.default_rng(33)
+    t = rng.normal(size=inst.sky.shape)
+    cot = rng.normal(size=lam[0].size)
+    e, g = R.energy_and_grad(inst.sky, data)
+    return dict(inst=inst, lam=lam[0], data=data[0], jvp=R(t)[0], t=t, cot=cot,
+                vjp=R.adjoint([cot]), energy=e, grad=g, metric=R.metric(inst.sky, t))
+
+
+@pytest.mark.parametrize("dtype", [F64, F32], ids=["f64", "f32"])
+def test_derivatives_jvp_vjp_metric(cuda, deriv_case, dtype):
+    c = deriv_case
+    plan = make_plan(c["inst"], dtype)
+    try:
+        plan.set_data(c["data"])
+        tol = 1e-12 if dtype == F64 else 1e-6
+        assert rel(plan.response(c["inst"].sky), c["lam"]) < tol
+        assert rel(plan.response_jvp(c["t"]), c["jvp"]) < tol
+        assert rel(plan.response_vjp(c["cot"]), c["vjp"]) < tol
+        e, g = plan.energy_and_grad(c["inst"].sky)
+        assert abs(float(e) - c["energy"]) / abs(c["energy"]) < tol
+        assert rel(g, c["grad"]) < (1e-11 if dtype == F64 else 5e-4)
+        assert rel(plan.metric(c["inst"].sky, c["t"]), c["metric"]) < (1e-10 if dtype == F64
+                                                                         else 1e-5)
+    finally:
+        plan.close()
+
+
+def test_derivatives_central_finite_differences(cuda, deriv_case):
+    """(H(x + eps v) - H(x - eps v)) / (2 eps) against <grad, v> on 32 random
+    directions, eps = 1e-4, FP64.  The error of a difference quotient is the
+    rounding of H (~1e-16 |H|) over eps, so it is measured against the typical
+    size |grad| |v| / sqrt(n) of <grad, v>."""
+    c = deriv_case
+    plan = make_plan(c["inst"], F64)
+    try:
+        plan.set_data(c["data"])
+        x = torch.as_tensor(c["inst"].sky, device=cuda)
+        _, g = plan.energy_and_grad(x)
+        rng = np.random.default_rng(34)
+        eps = 1e-4
+        worst = 0.0
+        for _ in range(32):
+            v = torch.as_tensor(rng.normal(size=x.shape), device=cuda)
+            ep = float(plan.energy_and_grad(x + eps * v, need_grad=False)[0])
+            em = float(plan.energy_and_grad(x - eps * v, need_grad=False)[0])
+            fd = (ep - em) / (2 * eps)
+            an = float((g * v).sum())
+            scale = float(torch.linalg.norm(g) * torch.linalg.norm(v)) / np.sqrt(x.numel())
+            worst = max(worst, abs(fd - an) / scale)
+        assert worst < 1e-5, worst
+    finally:
+        plan.close()
+
+
+# -------------------------------------------- 2048^2 x 3, point sources and wings
+def test_point_sources_fp32_vs_fp64_per_energy(cuda):
+    inst = synthetic.config4()
+    p64 = make_plan(inst, F64)
+    p32 = make_plan(inst, F32)
+    try:
+        x64 = torch.as_tensor(inst.sky, device=cuda)
+        i64 = p64.psf_forward(x64)
+        i32 = p32.psf_forward(x64.float())
+        errs = [rel(i32[0, e], i64[0, e]) for e in range(inst.n_energies)]
+        assert max(errs) < 1e-6, errs
+        rng = np.random.default_rng(44)
+        cot = torch.as_tensor(rng.normal(size=(1,) + tuple(x64.shape)), device=cuda)
+        a64 = p64.psf_adjoint(cot)
+        a32 = p32.psf_adjoint(cot.float())
+        errs = [rel(a32[e], a64[e]) for e in range(inst.n_energies)]
+        assert max(errs) < 1e-6, errs
+        # the FP64 GPU path against the oracle on the first energy plane
+        sl = inst.sky[:1]
+        dom = O.Domain((1,) + inst.shape, (1.0, 1.0, 1.0))
+        ref = O.linpatch_convolve(sl, dom, inst.psf[0, :, :1], inst.n_patches, inst.margin,
+                                  precut=True)
+        assert rel(i64[0, 0], ref[0]) < 1e-12
+    finally:
+        p64.close()
+        p32.close()
+
+
+# ------------------------------------------- 1024^2 x 7 x 3 (benchmark workload)
+@pytest.fixture(scope="module")
+def bench_case():
+    return synthetic.config2()
+
+
+def test_benchmark_workload_properties(cuda, bench_case):
+    inst = bench_case
+    p32 = make_plan(inst, F32)
+    p64 = make_plan(inst, F64, path="plain")
+    try:
+        rng = np.random.default_rng(22)
+        x = torch.as_tensor(inst.sky, device=cuda)
+        y = torch.as_tensor(rng.normal(size=p32.readout_total), device=cuda)
+        # FP32 against the FP64 unfused GPU path
+        r32 = p32.response(x.float())
+        r64 = p64.response(x)
+        assert rel(r32, r64) < 1e-6
+        v32 = p32.response_vjp(y.float())
+        v64 = p64.response_vjp(y)
+        assert rel(v32, v64) < 1e-6
+        # adjoint identity <R x, y> = <x, R^T y>
+        lhs = float((r64 * y).sum())
+        rhs = float((x * v64).sum())
+        assert abs(lhs - rhs) < 1e-12 * float(torch.linalg.norm(r64) * torch.linalg.norm(y))
+        lhs32 = float((r32.double() * y).sum())
+        rhs32 = float((x * v32.double()).sum())
+        assert abs(lhs32 - rhs32) < 1e-6 * float(torch.linalg.norm(r64) * torch.linalg.norm(y))
+        # linearity
+        z = torch.as_tensor(rng.normal(size=inst.sky.shape), device=cuda)
+        lin = p64.response(2.0 * x - 0.5 * z)
+        assert rel(lin, 2.0 * r64 - 0.5 * p64.response(z)) < 1e-12
+        # one module x energy plane against the oracle
+        img32 = p32.psf_forward(x.float())
+        img64 = p64.psf_forward(x)
+        dom = O.Domain((1,) + inst.shape, (1.0, 1.0, 1.0))
+        ref = O.linpatch_convolve(inst.sky[:1], dom, inst.psf[0, :, :1], inst.n_patches,
+                                  inst.margin, precut=True)
+        assert rel(img64[0, 0], ref[0]) < 1e-12
+        assert rel(img32[0, 0], ref[0]) < 1e-6
+    finally:
+        p32.close()
+        p64.close()
