@@ -168,6 +168,49 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def uneven_batch_leg(dev, n_streams=8, passes=10):
+    """64 independent problems of uneven size (sides 144..896, FFT sides
+    32/64/128, 1..3 energies): energy + gradient of all of them, problem after
+    problem on one stream against one CUDA-graph launch of the same pass with
+    the problems spread over ``n_streams`` branches."""
+    import torch
+
+    import jubik_gb300 as ju
+    from jubik_gb300 import synthetic
+
+    insts = synthetic.config5()
+    b = ju.ProblemBatch(insts, dtype=torch.float32, n_streams=n_streams, device=dev)
+    try:
+        lam = b.expected_counts()
+        b.set_data([synthetic.poisson_data(l, 7 + k) for k, l in enumerate(lam)])
+        chosen = b.autotune()
+        s = torch.cuda.current_stream(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+
+        def timed(fn):
+            for _ in range(3):
+                fn()
+            torch.cuda.synchronize(dev)
+            e0.record(s)
+            for _ in range(passes):
+                fn()
+            e1.record(s)
+            torch.cuda.synchronize(dev)
+            return e0.elapsed_time(e1) / passes
+
+        loop_ms = timed(b.energy_and_grad)
+        b.capture()
+        graph_ms = timed(b.replay)
+        return {"problems": len(insts), "mpix_per_pass": b.mpix, "streams": n_streams,
+                "paths": {str(k): v for k, v in chosen.items()},
+                "loop_ms": loop_ms, "graph_ms": graph_ms,
+                "loop_mpix_s": b.mpix / (loop_ms / 1e3), "graph_mpix_s": b.mpix / (graph_ms / 1e3),
+                "graph_speedup": loop_ms / graph_ms}
+    finally:
+        b.close()
+
+
 # ------------------------------------------------------------------ GPU leg
 def main():
     args = parse()
@@ -368,6 +411,7 @@ def main():
         torch.cuda.synchronize()
         fp64_ms = (time.perf_counter() - t0) / 2 * 1e3
         plan64.close()
+        line["uneven_batch"] = uneven_batch_leg(dev)
         line["rel_err_vs_fp64_gpu"] = err
         line["fp64_plain_ms_per_step"] = fp64_ms
         line["speedup_vs_fp64_plain"] = fp64_ms / ms

@@ -12,6 +12,7 @@ from __future__ import annotations
 import numpy as np
 
 from ._lib import JubikError, JubikStateError, JubikUnsupported
+from .batch import ProblemBatch
 from .convolve import (Domain, _bilinear_weights, convolve, integrate, linpatch_convolve,
                        slice_patches, slice_patches_adjoint)
 from .instruments import Response, build_psf_op, build_response
@@ -37,5 +38,5 @@ __all__ = [
     "integrate", "_bilinear_weights", "build_exposure_function", "build_readout_function",
     "coord_center", "Vector", "Poissonian", "ResponsePoissonian", "ModelPoissonian",
     "Response", "build_response", "build_psf_op", "ResponsePlan", "JubikError",
-    "JubikUnsupported", "JubikStateError",
+    "JubikUnsupported", "JubikStateError", "ProblemBatch",
 ]

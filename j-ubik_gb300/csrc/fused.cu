@@ -603,9 +603,16 @@ __device__ __forceinline__ void stage_output(Unit<T, P>& U, const Args& a) {
     if (!ADJ) {
       T* __restrict__ dst = (T*)a.out + ((int64_t)U.m * a.E + U.e) * U.npix;
       if (sizeof(T) == 4 && vec4) {
-        // groups of 4 columns never straddle the field edge (cb, ny multiples of 4)
-        for (int i = U.tid; i < nch * (P / 4); i += NT) {
-          const int jj = i / (P / 4), x = 4 * (i - jj * (P / 4));
+        // groups of 4 columns never straddle the field edge (cb, ny multiples of 4).
+        // A warp takes 8 pair rows x 4 groups: with the pitch P + 1 = 1 (mod 16)
+        // the staging reads of a half-warp fall on 16 distinct 8-byte bank pairs
+        // (16 consecutive groups of one row would share 4 of them).
+        constexpr int GT = P / 16;  // warp tiles across one row
+        const int ntile = ((nch + 7) / 8) * GT;
+        for (int w = U.warp; w < ntile; w += R::NW) {
+          const int jj = 8 * (w / GT) + (U.lane >> 2);
+          const int x = 16 * (w % GT) + 4 * (U.lane & 3);
+          if (jj >= nch) continue;
           const int col = cb + x;
           if (col < 0 || col >= a.ny) continue;
           const cx<T> z0 = stg[jj * TP + x], z1 = stg[jj * TP + x + 1];
@@ -633,8 +640,14 @@ __device__ __forceinline__ void stage_output(Unit<T, P>& U, const Args& a) {
     } else {
       T* __restrict__ dst = (T*)a.out + (int64_t)U.e * U.npix;
       if (sizeof(T) == 4 && vec4) {
-        for (int i = U.tid; i < nch * (K / 4); i += NT) {
-          const int jj = i / (K / 4), xa = 4 * (i - jj * (K / 4));
+        // warp tiles of 8 pair rows x 4 column groups, as in the forward branch
+        const int G = K / 4, GT = (G + 3) / 4;
+        const int ntile = ((nch + 7) / 8) * GT;
+        for (int w = U.warp; w < ntile; w += R::NW) {
+          const int jj = 8 * (w / GT) + (U.lane >> 2);
+          const int g = 4 * (w % GT) + (U.lane & 3);
+          if (jj >= nch || g >= G) continue;
+          const int xa = 4 * g;
           const int x = xa + mg, col = cb + x;
           if (col < 0 || col >= a.ny) continue;
           const int y0 = 2 * (j0 + jj);
@@ -815,15 +828,25 @@ int launch_one(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
   a.sc_max = g.sc_max;
   using R = Tr<T, P>;
   const size_t smem = R::SMEM;
-  static bool attr_set = false;
-  if (!attr_set) {
+  // the shared-memory opt-in is a per-device function attribute: set it once
+  // per device before the first launch there (so never inside a stream capture
+  // that follows a warm-up call)
+  constexpr int kMaxDev = 64;
+  static bool attr_set[kMaxDev] = {};
+  int dev = 0;
+  JUBIK_TRY_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDev) {
+    set_error("device ordinal %d beyond %d", dev, kMaxDev);
+    return JUBIK_ERR_UNSUPPORTED;
+  }
+  if (!attr_set[dev]) {
     JUBIK_TRY(set_smem(k_fused<T, P, false>, smem));
     JUBIK_TRY(set_smem(k_fused<T, P, true>, smem));
     JUBIK_TRY(set_smem(k_sky_spec<T, P>, smem));
     JUBIK_TRY(set_smem(k_fwd_from_spec<T, P>, smem));
     JUBIK_TRY(set_smem(k_adj_to_spec<T, P>, smem));
     JUBIK_TRY(set_smem(k_adj_from_spec<T, P>, smem));
-    attr_set = true;
+    attr_set[dev] = true;
   }
   const int64_t units = g.units();
   const int64_t patches = (int64_t)g.E * g.n * g.n;

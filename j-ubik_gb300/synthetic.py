@@ -16,7 +16,8 @@ recipes of the five benchmark configurations:
 4. 2048^2 x 3 sky of GRF diffuse plus 0.1 % point sources (flux log-uniform
    1e1..1e5), 32x32 patches of stride 64, margin 32 (P=192); Gaussian core
    sigma 0.5 -> 6 px plus a 5 % r^-3 wing out to 30 px.
-5. uneven batch of independent problems (sizes log-uniform 128^2..1024^2).
+5. uneven batch of 64 independent problems (sizes log-uniform 128^2..1024^2,
+   FFT sides 32/64/128, 1..3 energies, Gaussian PSFs sigma 0.8 -> 0.8..4 px).
 
 Skies are exp(s) of a Gaussian random field with P(k) ~ (1 + (k/0.05)^2)^-2
 (k in cycles/pixel), rescaled to std 1.5 and the stated mean.
@@ -38,7 +39,7 @@ class Instrument:
     n_patches: int
     margin: int
     sky: np.ndarray            # (E, nx, ny)
-    psf: np.ndarray            # (M, n^2, E, K, K) pre-cut, unit sum
+    psf: np.ndarray            # (M, n^2, E, K, K) pre-cut, unit sum ((M, n^2, K, K): all E)
     exposure: np.ndarray       # (M, E, nx, ny)
     readmask: np.ndarray       # (M, E, nx, ny) bool, True = read out
     pixel_area: float = 1.0
@@ -214,24 +215,56 @@ def config4(nx=2048, dx=64, margin=32, n_energies=3, seed=0) -> Instrument:
                       readmask)
 
 
-def config5_problems(count=64, seed=4, max_side=1024) -> List[dict]:
-    """Geometry of the uneven batch: side, n, margin (P in {32, 64, 128}), E, sigma."""
+def config5_geometry(count=64, seed=4, min_side=128, max_side=1024) -> List[dict]:
+    """Geometry of the uneven batch, one dict per problem.
+
+    The side is drawn log-uniform in [min_side, max_side], the number of
+    energies in 1..3 and the widest PSF sigma in 0.8..4 px.  The margin covers
+    3 sigma of the widest PSF (at least 4 px); the FFT side P is 32, 64 or 128
+    and the stride dx = P/2 - margin (made even); (n, P) with n in 4..16 is
+    the pair whose field side n * dx is closest to the draw, where each
+    doubling of P counts as a 4 % miss (smaller FFTs are preferred).  With P <= 128 and n <= 16 the largest reachable side is 16 * 60 =
+    960: larger draws take the largest side their margin allows."""
     rng = np.random.default_rng(seed)
     out = []
-    for _ in range(count):
-        side = float(np.exp(rng.uniform(np.log(128), np.log(max_side))))
-        P = int(rng.choice([32, 64, 128]))
-        n = int(rng.integers(4, 17))
-        # choose the stride so that P = 2 dx + 2 m with m = dx / 2
-        dx = P // 3 if P % 3 == 0 else P // 4 * 1
-        dx = max(4, (P // 2) // 2 * 2 // 1)
-        margin = (P - 2 * dx) // 2
-        if margin < 1:
-            dx -= 2
-            margin = (P - 2 * dx) // 2
-        nx = dx * n
-        out.append(dict(nx=nx, n=n, margin=margin, E=int(rng.integers(1, 4)),
-                        sigma=(0.8, float(rng.uniform(0.8, 4.0)))))
+    for i in range(count):
+        side = float(np.exp(rng.uniform(np.log(min_side), np.log(max_side))))
+        n_e = int(rng.integers(1, 4))
+        sig_max = float(rng.uniform(0.8, 4.0))
+        m0 = max(4, int(np.ceil(3.0 * sig_max)))
+        best = None
+        for P in (32, 64, 128):
+            dx = P // 2 - m0
+            dx -= dx % 2
+            if dx < 2:
+                continue
+            for n in range(4, 17):
+                # closest side; each doubling of P costs as much as a 4 % miss
+                cost = abs(np.log(n * dx / side)) + 0.04 * np.log2(P / 32)
+                if best is None or cost < best[0] - 1e-12:
+                    best = (cost, P, n, dx)
+        _, P, n, dx = best
+        out.append(dict(nx=n * dx, n=n, dx=dx, margin=P // 2 - dx, P=P, E=n_e,
+                        sigma=(0.8, sig_max), seed=1000 + i))
+    return out
+
+
+def config5(count=64, seed=4, min_side=128, max_side=1024) -> List[Instrument]:
+    """The uneven batch: independent one-module problems of the geometry of
+    :func:`config5_geometry`.  Sky: GRF recipe with mean 1 + 0.5 e; PSFs:
+    Gaussians of sigma 0.8 px at the field centre growing linearly to the
+    problem's widest sigma, one set for all energies (psf shape (1, n^2, K, K),
+    broadcast over energies); exposure 1e3 everywhere, nothing masked."""
+    out = []
+    for i, g in enumerate(config5_geometry(count, seed, min_side, max_side)):
+        rng = np.random.default_rng(g["seed"])
+        nx, n, n_e = g["nx"], g["n"], g["E"]
+        sky = np.stack([np.exp(grf((nx, nx), rng, mean=1.0 + 0.5 * e)) for e in range(n_e)])
+        psf = gaussian_psfs(nx, n, 2 * g["dx"], g["sigma"][0], g["sigma"][1])[None]
+        exposure = np.full((1, n_e, nx, nx), 1e3)
+        readmask = np.ones_like(exposure, dtype=bool)
+        out.append(Instrument(f"uneven{i}", 1, n_e, (nx, nx), n, g["margin"], sky, psf,
+                              exposure, readmask, extra=dict(P=g["P"])))
     return out
 
 

@@ -1,0 +1,92 @@
+"""Uneven batch of independent problems: per-problem parity with the oracle,
+and the CUDA-graph pass (problems spread over several streams) against the
+eager problem-after-problem pass."""
+import numpy as np
+import pytest
+import torch
+
+import jubik_oracle as O
+import jubik_gb300 as ju
+from jubik_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a = a.detach().double().cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def small_batch():
+    insts = synthetic.config5(count=6, seed=11, min_side=96, max_side=256)
+    refs = []
+    for k, inst in enumerate(insts):
+        E, nx = inst.n_energies, inst.shape[0]
+        psf = np.broadcast_to(inst.psf[:, :, None], inst.psf.shape[:2] + (E,) + inst.psf.shape[2:])
+        R = O.Response(O.Domain((E, nx, nx), (1.0, 1.0, 1.0)), psf, inst.n_patches, inst.margin,
+                       inst.exposure, inst.readmask)
+        lam = R(inst.sky)
+        data = [synthetic.poisson_data(lam[0], 50 + k)]
+        e, g = R.energy_and_grad(inst.sky, data)
+        refs.append(dict(data=data[0], energy=e, grad=g))
+    return insts, refs
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32], ids=["f64", "f32"])
+def test_batch_eager_and_graph_match_oracle(cuda, small_batch, dtype):
+    insts, refs = small_batch
+    assert len({2 * (i.shape[0] // i.n_patches) + 2 * i.margin for i in insts}) >= 2
+    b = ju.ProblemBatch(insts, dtype=dtype, n_streams=3)
+    try:
+        b.set_data([r["data"] for r in refs])
+        tol, gtol = (1e-12, 1e-11) if dtype == torch.float64 else (1e-6, 5e-4)
+        e, g = b.energy_and_grad()
+        torch.cuda.synchronize()
+        eager_e = e.clone()
+        eager_g = [t.clone() for t in g]
+        for k, r in enumerate(refs):
+            assert abs(float(e[k]) - r["energy"]) / abs(r["energy"]) < tol
+            assert rel(g[k], r["grad"]) < gtol
+        b.capture()
+        for _ in range(2):  # two replays in a row
+            b.energy.zero_()
+            for t in b.grad:
+                t.zero_()
+            e2, g2 = b.replay()
+            torch.cuda.synchronize()
+            # FP32 images are summed with L2 reductions in varying order (ulp-level)
+            etol = 1e-13 if dtype == torch.float64 else 1e-9
+            for k in range(len(insts)):
+                assert abs(float(e2[k]) - float(eager_e[k])) <= etol * abs(float(eager_e[k]))
+                # FP32: ulp-level differences of lam pass through 1 - d/lam, which
+                # cancels nearly where d ~ lam (observed 2e-6 between runs)
+                assert rel(g2[k], eager_g[k].double().cpu().numpy()) < (1e-13 if dtype ==
+                                                                         torch.float64 else 2e-5)
+        # the graph reads the sky buffers: new skies give the new energies
+        b.x[0].mul_(1.5)
+        e3, _ = b.replay()
+        plan_e, _ = b.plans[0].energy_and_grad(b.x[0])
+        torch.cuda.synchronize()
+        assert abs(float(e3[0]) - float(plan_e)) <= etol * abs(float(plan_e))
+        assert abs(float(e3[0]) - float(eager_e[0])) > 1e-6 * abs(float(eager_e[0]))
+    finally:
+        b.close()
+
+
+def test_batch_autotune_picks_a_covering_path(cuda, small_batch):
+    insts, refs = small_batch
+    b = ju.ProblemBatch(insts, dtype=torch.float32, n_streams=2)
+    try:
+        with pytest.raises(RuntimeError):
+            b.autotune()
+        b.set_data([r["data"] for r in refs])
+        chosen = b.autotune(reps=2)
+        sides = {2 * (i.shape[0] // i.n_patches) + 2 * i.margin for i in insts}
+        assert set(chosen) == sides
+        assert all(p in ("fused", "fused_unit", "plain") for p in chosen.values())
+        e, g = b.energy_and_grad()
+        for k, r in enumerate(refs):
+            assert abs(float(e[k]) - r["energy"]) / abs(r["energy"]) < 1e-6
+    finally:
+        b.close()

@@ -13,8 +13,12 @@
   and one module x energy plane against the oracle.
 
 Tolerances: FP64 1e-12 relative L2 (1e-11 for gradients, 1e-10 for the
-metric), FP32 1e-6; the FP32 Poisson gradient is bounded by the conditioning
-of 1 - d/lam (5e-4).
+metric), FP32 1e-6.  The Poisson gradient R^T(1 - d/lam) is a difference of
+two terms that nearly cancel where d is close to lam, so its FP32 error is
+measured against the size of the cancelling term, |R^T(d/lam)|: 3e-6.  (FP32
+FFT convolution errors are absolute, of order 1e-7 of the largest lam, so
+faint pixels carry larger relative errors of lam, which d/lam passes on; the
+observed level is 1.1e-6.)
 """
 import numpy as np
 import pytest
@@ -35,6 +39,13 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
+def grad_err(g, ref, cancel, dtype):
+    """FP64: relative L2 error.  FP32: error relative to |R^T(d/lam)|."""
+    a = g.detach().double().cpu().numpy()
+    scale = np.linalg.norm(ref) if dtype == F64 else np.linalg.norm(cancel)
+    return float(np.linalg.norm(a - ref) / scale)
+
+
 def make_plan(inst, dtype, path="auto", pixel_area=1.0, psf=None, layout="auto"):
     plan = ju.ResponsePlan(inst.n_modules, inst.n_energies, inst.shape, inst.n_patches,
                            inst.margin, dtype=dtype, path=path, pixel_area=pixel_area)
@@ -52,7 +63,8 @@ def small_case():
     lam = R(inst.sky)
     data = [synthetic.poisson_data(lam[0], 1)]
     e, g = R.energy_and_grad(inst.sky, data)
-    return dict(inst=inst, R=R, lam=lam[0], data=data[0], energy=e, grad=g)
+    cancel = R.adjoint([data[0] / lam[0]])
+    return dict(inst=inst, R=R, lam=lam[0], data=data[0], energy=e, grad=g, cancel=cancel)
 
 
 @pytest.mark.parametrize("dtype", [F64, F32], ids=["f64", "f32"])
@@ -66,7 +78,7 @@ def test_small_field_response_and_likelihood(cuda, small_case, dtype, path):
         assert rel(plan.response(c["inst"].sky), c["lam"]) < tol
         e, g = plan.energy_and_grad(c["inst"].sky)
         assert abs(float(e) - c["energy"]) / abs(c["energy"]) < tol
-        assert rel(g, c["grad"]) < (1e-11 if dtype == F64 else 5e-4)
+        assert grad_err(g, c["grad"], c["cancel"], dtype) < (1e-11 if dtype == F64 else 3e-6)
     finally:
         plan.close()
 
@@ -103,7 +115,8 @@ def deriv_case():
     cot = rng.normal(size=lam[0].size)
     e, g = R.energy_and_grad(inst.sky, data)
     return dict(inst=inst, lam=lam[0], data=data[0], jvp=R(t)[0], t=t, cot=cot,
-                vjp=R.adjoint([cot]), energy=e, grad=g, metric=R.metric(inst.sky, t))
+                vjp=R.adjoint([cot]), energy=e, grad=g, metric=R.metric(inst.sky, t),
+                cancel=R.adjoint([data[0] / lam[0]]))
 
 
 @pytest.mark.parametrize("dtype", [F64, F32], ids=["f64", "f32"])
@@ -118,7 +131,7 @@ def test_derivatives_jvp_vjp_metric(cuda, deriv_case, dtype):
         assert rel(plan.response_vjp(c["cot"]), c["vjp"]) < tol
         e, g = plan.energy_and_grad(c["inst"].sky)
         assert abs(float(e) - c["energy"]) / abs(c["energy"]) < tol
-        assert rel(g, c["grad"]) < (1e-11 if dtype == F64 else 5e-4)
+        assert grad_err(g, c["grad"], c["cancel"], dtype) < (1e-11 if dtype == F64 else 3e-6)
         assert rel(plan.metric(c["inst"].sky, c["t"]), c["metric"]) < (1e-10 if dtype == F64
                                                                          else 1e-5)
     finally:
@@ -127,9 +140,13 @@ def test_derivatives_jvp_vjp_metric(cuda, deriv_case, dtype):
 
 def test_derivatives_central_finite_differences(cuda, deriv_case):
     """(H(x + eps v) - H(x - eps v)) / (2 eps) against <grad, v> on 32 random
-    directions, eps = 1e-4, FP64.  The error of a difference quotient is the
-    rounding of H (~1e-16 |H|) over eps, so it is measured against the typical
-    size |grad| |v| / sqrt(n) of <grad, v>."""
+    directions, eps = 1e-4, FP64.  The quotient's error is the rounding of H
+    over 2 eps: here |H| ~ 1e11 and FP64 FFT convolution rounds lam (and so H)
+    at a few 1e-15, i.e. an absolute error of order 1 against a typical
+    |<grad, v>| = |grad| |v| / sqrt(n) ~ 3e4.  The bound 2e-4 of that size
+    leaves a margin of 4 over the observed 5e-5; a wrong derivative (a missing
+    exposure, pixel-area or weight factor) is off by O(1).  The FP64 gradient
+    itself matches the oracle to 1e-11 in test_derivatives_jvp_vjp_metric."""
     c = deriv_case
     plan = make_plan(c["inst"], F64)
     try:
@@ -147,7 +164,7 @@ def test_derivatives_central_finite_differences(cuda, deriv_case):
             an = float((g * v).sum())
             scale = float(torch.linalg.norm(g) * torch.linalg.norm(v)) / np.sqrt(x.numel())
             worst = max(worst, abs(fd - an) / scale)
-        assert worst < 1e-5, worst
+        assert worst < 2e-4, worst
     finally:
         plan.close()
 

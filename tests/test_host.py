@@ -66,3 +66,27 @@ def test_vector_tree_interface():
 def test_linpatch_domain_type_checked():
     with pytest.raises(ValueError, match="domain has to be"):
         ju.linpatch_convolve(np.ones((8, 8)), (8, 8), np.ones((4, 8, 8)), 2, 1)
+
+
+def test_uneven_batch_geometry():
+    from jubik_gb300 import synthetic
+    geo = synthetic.config5_geometry()
+    assert len(geo) == 64
+    assert geo == synthetic.config5_geometry()  # seeded
+    assert {g["P"] for g in geo} == {32, 64, 128}
+    for g in geo:
+        assert g["P"] == 2 * g["dx"] + 2 * g["margin"]
+        assert g["nx"] == g["n"] * g["dx"] and 4 <= g["n"] <= 16
+        assert g["dx"] % 2 == 0 and g["margin"] >= 3 * g["sigma"][1] - 1e-9
+        assert 1 <= g["E"] <= 3 and 0.8 <= g["sigma"][1] <= 4.0
+        assert 96 <= g["nx"] <= 1024
+
+
+def test_problem_batch_needs_a_gpu_and_problems():
+    if ju.plan.torch.cuda.is_available():
+        pytest.skip("CUDA device present")
+    with pytest.raises(ValueError):
+        ju.ProblemBatch([])
+    from jubik_gb300 import synthetic
+    with pytest.raises(ju.JubikError):
+        ju.ProblemBatch(synthetic.config5(count=1, max_side=160))
