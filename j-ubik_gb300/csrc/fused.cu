@@ -85,6 +85,16 @@ __device__ __forceinline__ void cp_async(T* dst, const T* src, bool ok) {
                  : "memory");
   }
 }
+// Unpredicated 4/8-byte global->shared copy (the source is known in bounds).
+template <typename T>
+__device__ __forceinline__ void cp_async_in(T* dst, const T* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  if constexpr (sizeof(T) == 4) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+  } else {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+  }
+}
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
 }
@@ -228,10 +238,21 @@ __device__ __forceinline__ void stage_input(Unit<T, P>& U, const Args& a) {
   }
   const T* __restrict__ src =
       (const T*)a.in + (ADJ ? ((int64_t)U.m * a.E + U.e) : (int64_t)U.e) * U.npix;
+  // adjoint units whose P x P window lies inside the field need no bounds checks
+  const bool interior = ADJ && U.rb >= 0 && U.rb + P <= a.nx && U.cb >= 0 && U.cb + P <= a.ny;
   auto issue = [&](int c) {
     const int j0 = jlo + c * CH;
     const int nch = min(CH, jhi - j0);
-    if (NT % width == 0) {
+    if (ADJ && interior && NT % width == 0) {
+      const int xs = U.tid % width, jstep = NT / width;
+      const T* gcol = src + (int64_t)U.rb * a.ny + U.cb + xs;
+      for (int jj = U.tid / width; jj < nch; jj += jstep) {
+        const T* g0 = gcol + (int64_t)(2 * (j0 + jj)) * a.ny;
+        T* d = reinterpret_cast<T*>(bufp(c, jj) + xs);
+        cp_async_in<T>(d, g0);
+        cp_async_in<T>(d + 1, g0 + a.ny);
+      }
+    } else if (NT % width == 0) {
       // each thread owns one staged column and every (NT / width)-th pair row
       const int xs = U.tid % width, jstep = NT / width;
       const int col = U.cb + xoff + xs;
@@ -609,6 +630,21 @@ __device__ __forceinline__ void stage_output(Unit<T, P>& U, const Args& a) {
         // (16 consecutive groups of one row would share 4 of them).
         constexpr int GT = P / 16;  // warp tiles across one row
         const int ntile = ((nch + 7) / 8) * GT;
+        if (rb >= 0 && rb + P <= a.nx && cb >= 0 && cb + P <= a.ny) {
+          // the whole P x P patch lies inside the field: no bounds checks
+          T* base = dst + (int64_t)(rb + 2 * j0) * a.ny + cb;
+          for (int w = U.warp; w < ntile; w += R::NW) {
+            const int jj = 8 * (w / GT) + (U.lane >> 2);
+            const int x = 16 * (w % GT) + 4 * (U.lane & 3);
+            if (jj >= nch) continue;
+            const cx<T>* sp = stg + jj * TP + x;
+            const cx<T> z0 = sp[0], z1 = sp[1], z2 = sp[2], z3 = sp[3];
+            T* p = base + (int64_t)(2 * jj) * a.ny + x;
+            red_add_v4((float*)p, scale * z0.x, scale * z1.x, scale * z2.x, scale * z3.x);
+            red_add_v4((float*)(p + a.ny), scale * z0.y, scale * z1.y, scale * z2.y,
+                       scale * z3.y);
+          }
+        } else
         for (int w = U.warp; w < ntile; w += R::NW) {
           const int jj = 8 * (w / GT) + (U.lane >> 2);
           const int x = 16 * (w % GT) + 4 * (U.lane & 3);
