@@ -438,6 +438,28 @@ def main():
         torch.cuda.synchronize()
         fp64_ms = (time.perf_counter() - t0) / 2 * 1e3
         plan64.close()
+        # the other operator calls of the workload, each timed alone (Mpix/s of 22.02 Mpix)
+        cot32 = cot.float()
+        vt = torch.as_tensor(rng.normal(size=x.shape), device=dev, dtype=torch.float32)
+        rout = torch.empty(plan.readout_total, dtype=torch.float32, device=dev)
+        xout = torch.empty_like(x)
+        calls = {"forward R(x)": lambda: plan.response(x, out=rout),
+                 "vjp R^T(c)": lambda: plan.response_vjp(cot32, out=xout),
+                 "energy only": lambda: plan.energy_and_grad(x, need_grad=False, energy=energy),
+                 "metric R^T diag(1/lam) R v": lambda: plan.metric(None, vt, out=xout)}
+        comp = {}
+        for name, fn in calls.items():
+            for _ in range(3):
+                fn()
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            for _ in range(20):
+                fn()
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            t = ev0.elapsed_time(ev1) / 20
+            comp[name] = {"ms": t, "mpix_s": mpix / (t / 1e3)}
+        line["operators"] = comp
         line["uneven_batch"] = uneven_batch_leg(dev)
         line["rel_err_vs_fp64_gpu"] = err
         line["fp64_plain_ms_per_step"] = fp64_ms

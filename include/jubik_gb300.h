@@ -187,6 +187,30 @@ JUBIK_API int jubik_slice_patches_adjoint(const void* patches, int64_t batch, in
 JUBIK_API int jubik_convolve2d(const void* kernel, int64_t bk, const void* signal, int64_t bs, int32_t h,
                      int32_t w, double dvol, int32_t dtype, void* out, void* stream);
 
+/* Sampling and global reductions for the callers of the response.
+ * Random numbers: counter-based Philox4x32-10 (Salmon et al., SC'11) keyed by
+ * `seed`; element i of a call uses its own counter, so results do not depend
+ * on the launch shape, and `offset` selects an independent stream.
+ *
+ * One Philox4x32-10 block on the host (for known-answer checks). */
+JUBIK_API int jubik_philox4x32_10(const uint32_t* counter, const uint32_t* key, uint32_t* out);
+/* n standard normal deviates (Box-Muller) into out (dtype): the xi ~ N(0, 1)
+ * draws of an MGVI linear sample (jax.random.normal inside NIFTy.re's
+ * draw_linear_residual, configured at jubik/minimization_parser.py:337-420). */
+JUBIK_API int jubik_random_normal(void* out, int64_t n, int32_t dtype, uint64_t seed,
+                                  uint64_t offset, void* stream);
+/* Poisson deviates of expected counts lam (dtype, length n) into out (int32):
+ * inversion below 10, transformed rejection (PTRS) above; -1 where lam is
+ * negative, NaN or >= 2e9.  The mock-data draw of jubik/data.py:143-146
+ * (jax.random.poisson of each module's masked expected counts). */
+JUBIK_API int jubik_random_poisson(const void* lam, int64_t n, int32_t dtype, uint64_t seed,
+                                   uint32_t offset, int32_t* out, void* stream);
+/* out (device double[1]) = sum_i a[i] b[i], accumulated in FP64 in a fixed
+ * order (deterministic): the global dot products of the conjugate-gradient
+ * solve of an MGVI linear sample.  n = 0 writes 0 (a, b may then be NULL). */
+JUBIK_API int jubik_dot(const void* a, const void* b, int64_t n, int32_t dtype, double* out,
+                        void* stream);
+
 /* jubik_convolve2d without any device allocation (no counterpart in the reference).
  * For callers that cannot allocate device memory -- code under a framework that owns
  * all device memory through its own pool (e.g. an XLA FFI handler), or a loop where

@@ -80,6 +80,10 @@ _SIGS = {
     "jubik_convolve2d": ([_vp, _i64, _vp, _i64, _i32, _i32, _dbl, _i32, _vp, _vp], C.c_int),
     "jubik_convolve2d_noalloc": ([_vp, _i64, _vp, _i64, _i32, _i32, _dbl, _i32, _vp, _vp],
                                  C.c_int),
+    "jubik_philox4x32_10": ([_vp, _vp, _vp], C.c_int),
+    "jubik_random_normal": ([_vp, _i64, _i32, C.c_uint64, C.c_uint64, _vp], C.c_int),
+    "jubik_random_poisson": ([_vp, _i64, _i32, C.c_uint64, C.c_uint32, _vp, _vp], C.c_int),
+    "jubik_dot": ([_vp, _vp, _i64, _i32, _vp, _vp], C.c_int),
 }
 
 _lib = None

@@ -149,7 +149,8 @@ def build_response(domain, kernel, n_patch: int, margin: int, exposures=None, fl
                    effective_area=None, dtype: torch.dtype = torch.float32, path: str = "auto"):
     """Response dictionary with the keys of ``build_erosita_response``
     (``erosita_response.py:352-358``): 'pix_area', 'psf', 'exposure', 'mask',
-    'kernel', 'R'."""
+    'kernel', 'R', plus 'mask_adj', the readout transpose that the reference's
+    diagnostics expect the caller to add (``diagnostics.py:101``)."""
     R = Response(domain, kernel, n_patch, margin, exposures=exposures, flags=flags,
                  exposure_cut=exposure_cut, threshold=threshold, keys=keys,
                  pixel_area=pixel_area, effective_area=effective_area, dtype=dtype, path=path)
@@ -157,5 +158,12 @@ def build_response(domain, kernel, n_patch: int, margin: int, exposures=None, fl
     def psf_func(x, k=None):
         return R.psf(x, k)
 
+    def mask_adj(vec):
+        """Readout transpose in the form ``jax.linear_transpose`` returns it: a
+        1-tuple holding the (M, E, N, N) image (``diagnostics.py:101``)."""
+        if R.mask_func is None:
+            raise ValueError("the response has no readout mask")
+        return (R.mask_func.adjoint(vec),)
+
     return {"pix_area": R.pixel_area, "psf": psf_func, "exposure": R.exposure,
-            "mask": R.mask_func, "kernel": R.kernel, "R": R}
+            "mask": R.mask_func, "mask_adj": mask_adj, "kernel": R.kernel, "R": R}

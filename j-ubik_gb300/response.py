@@ -124,6 +124,29 @@ def build_readout_function(flags, threshold=None, keys=None):
         parts = torch.split(out, sizes)
         return Vector({key: parts[i] for i, key in enumerate(keys)})
 
+    def _adjoint(vec):
+        """Transpose of the readout (``jax.linear_transpose`` of it, as the
+        reference's callers build at ``data.py:156``, ``diagnostics.py:101``):
+        the readout vectors scattered back into zero (n, m, q, l) images."""
+        dev = require_cuda()
+        if isinstance(vec, Vector):
+            parts = [vec.tree[k] for k in keys]
+        elif isinstance(vec, dict):
+            parts = [vec[k] for k in keys]
+        else:
+            parts = list(vec)
+        flat = torch.cat([as_device(v, None, dev).reshape(-1) for v in parts])
+        if not flat.is_floating_point():
+            flat = flat.to(torch.float64)
+        idx, sizes = _index(dev)
+        if flat.numel() != idx.numel():
+            raise ValueError("readout vectors do not match the mask")
+        img = torch.zeros(mask.shape, dtype=flat.dtype, device=dev)
+        _lib.call("jubik_readout_scatter", ptr(flat), None, ptr(idx), idx.numel(),
+                  dtype_code(flat.dtype), ptr(img), stream_handle(dev))
+        return img
+
     _apply_readout.mask = mask
     _apply_readout.keys = list(keys)
+    _apply_readout.adjoint = _adjoint
     return _apply_readout
