@@ -187,6 +187,22 @@ JUBIK_API int jubik_slice_patches_adjoint(const void* patches, int64_t batch, in
 JUBIK_API int jubik_convolve2d(const void* kernel, int64_t bk, const void* signal, int64_t bs, int32_t h,
                      int32_t w, double dvol, int32_t dtype, void* out, void* stream);
 
+/* eROSITA PSF patches interpolated from gridded PSFs at a few off-axis radii
+ * (psf_interpolator of jubik/instruments/erosita/erosita_psf_utils.py:198-264,
+ * with get_psf :90-172).  Device arrays, float64, radii ascending per energy:
+ * psfs (E, R, psf_h, psf_w), rs (E, R), center_ids (E, R, 2), deltas (E, 2),
+ * pointing (E, 2).  Field nx x ny with pixel distances (dist_x, dist_y),
+ * npatch patches per axis.  layout JUBIK_PSF_FULL: out (npatch^2, E, nx, ny),
+ * the reference's rolled full-field array; JUBIK_PSF_PRECUT: out (npatch^2,
+ * E, 2 nx/npatch, 2 ny/npatch), the windows jubik_plan_set_psf takes, without
+ * forming the full field.  out in `dtype`; arithmetic in FP64. */
+JUBIK_API int jubik_psf_interpolate(const double* psfs, const double* rs,
+                                    const double* center_ids, const double* deltas,
+                                    const double* pointing, int32_t n_energies, int32_t n_radii,
+                                    int32_t psf_h, int32_t psf_w, int32_t nx, int32_t ny,
+                                    double dist_x, double dist_y, int32_t npatch, int32_t layout,
+                                    int32_t dtype, void* out, void* stream);
+
 /* Sampling and global reductions for the callers of the response.
  * Random numbers: counter-based Philox4x32-10 (Salmon et al., SC'11) keyed by
  * `seed`; element i of a call uses its own counter, so results do not depend

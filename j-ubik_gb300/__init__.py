@@ -13,7 +13,7 @@ import numpy as np
 
 from ._lib import JubikError, JubikStateError, JubikUnsupported
 from .batch import ProblemBatch
-from . import diagnostics, minimization, sampling
+from . import diagnostics, minimization, psf, sampling
 from .convolve import (Domain, _bilinear_weights, convolve, integrate, linpatch_convolve,
                        slice_patches, slice_patches_adjoint)
 from .instruments import Response, build_psf_op, build_response

@@ -20,7 +20,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libjubik_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["fused.cu", "plain_fft.cu", "ops.cu", "api.cu", "noalloc.cu", "sampling.cu"]
+SOURCES = ["fused.cu", "plain_fft.cu", "ops.cu", "api.cu", "noalloc.cu", "sampling.cu",
+           "psf_interp.cu"]
 
 
 def _nvcc():

@@ -84,6 +84,8 @@ _SIGS = {
     "jubik_random_normal": ([_vp, _i64, _i32, C.c_uint64, C.c_uint64, _vp], C.c_int),
     "jubik_random_poisson": ([_vp, _i64, _i32, C.c_uint64, C.c_uint32, _vp, _vp], C.c_int),
     "jubik_dot": ([_vp, _vp, _i64, _i32, _vp, _vp], C.c_int),
+    "jubik_psf_interpolate": ([_vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32,
+                               _dbl, _dbl, _i32, _i32, _i32, _vp, _vp], C.c_int),
 }
 
 _lib = None

@@ -272,3 +272,33 @@ def poisson_data(lam_readout: np.ndarray, seed: int = 1) -> np.ndarray:
     """Poisson counts (int32) of expected counts in readout order."""
     rng = np.random.default_rng(seed)
     return rng.poisson(np.maximum(np.asarray(lam_readout, np.float64), 0.0)).astype(np.int32)
+
+
+def erosita_like_psf_infos(n_energies=2, n_radii=5, grid=64, field=(256, 256),
+                           distances=(1.0, 1.0), seed=0) -> List[dict]:
+    """Gridded PSFs at a few off-axis radii in the layout of
+    ``eROSITA_PSF._get_psf_infos`` (one dict per energy): elongated Gaussians
+    whose width grows with the radius and with the energy, sampled on a
+    ``grid`` x ``grid`` PSF grid of half the sky pixel, centre indices near
+    the grid centre, radii given out of order, pointing at the field centre."""
+    rng = np.random.default_rng(seed)
+    infos = []
+    for e in range(n_energies):
+        rs = np.linspace(0.0, 0.6 * field[0] * distances[0], n_radii)
+        order = rng.permutation(n_radii)
+        delta = (0.5 * distances[0], 0.5 * distances[1])
+        cids = np.stack([np.full(n_radii, grid / 2) + rng.integers(-2, 3, n_radii),
+                         np.full(n_radii, grid / 2) + rng.integers(-2, 3, n_radii)], -1)
+        psfs = []
+        for j in range(n_radii):
+            sig = (1.0 + 0.08 * rs[j] / distances[0]) * (1.0 + 0.2 * e)
+            u = (np.arange(grid) - cids[j, 0]) * delta[0]
+            v = (np.arange(grid) - cids[j, 1]) * delta[1]
+            uu, vv = np.meshgrid(u, v, indexing="ij")
+            p = np.exp(-0.5 * ((uu / (1.6 * sig)) ** 2 + (vv / sig) ** 2))
+            psfs.append(p / p.sum())
+        infos.append({"psfs": np.array(psfs)[order], "rs": rs[order],
+                      "patch_center_ids": cids[order], "patch_deltas": delta,
+                      "pointing_center": (field[0] / 2 * distances[0],
+                                          field[1] / 2 * distances[1])})
+    return infos

@@ -327,4 +327,5 @@ def test_response_vector_interface(cuda):
     ref = O.Response(dom, inst.psf, nx // dx, m, inst.exposure, inst.readmask, pixel_area=0.5)
     for i, k in enumerate(["tm1", "tm2"]):
         assert rel(out.tree[k], ref(inst.sky)[i]) < 1e-12
-    assert set(rd) == {"pix_area", "psf", "exposure", "mask", "kernel", "R"}
+    # the reference's keys, plus the readout transpose its diagnostics expect
+    assert set(rd) == {"pix_area", "psf", "exposure", "mask", "kernel", "R", "mask_adj"}
