@@ -201,6 +201,8 @@ struct jubik_plan {
   void* hnyq = nullptr;
   void* hfull = nullptr;
   void* spec = nullptr;  // per-(energy, patch) spectra shared by the modules
+  void* acc = nullptr;   // per-(energy, patch) adjoint sums over modules; all zero between
+                         // calls (zeroed when allocated, cleared by their reader)
   // images (M,E,nx,ny)
   void* conv = nullptr;
   void* conv_v = nullptr;
@@ -282,19 +284,30 @@ int check_plan(const jubik_plan* p) {
 int64_t image_elems(const jubik_plan* p) { return (int64_t)p->g.M * p->g.E * p->g.pixels(); }
 
 // forward of the PSF operator: out (M,E,nx,ny) = scale * sum_k patch convolutions
-int do_forward(jubik_plan* p, const void* x, void* out, double scale, cudaStream_t s) {
+// `also_zero` (module-shared path only): a buffer of `also_zero_bytes` for the
+// sky-spectrum kernel to clear as well -- the gradient that a later do_adjoint
+// with out_zeroed adds into.  Returns whether it was cleared.
+int do_forward(jubik_plan* p, const void* x, void* out, double scale, cudaStream_t s,
+               void* also_zero = nullptr, int64_t also_zero_bytes = 0,
+               bool* zeroed = nullptr) {
   const Geom& g = p->g;
+  if (zeroed) *zeroed = false;
   if (p->path == JUBIK_PATH_FUSED) {
-    {
-      Phase ph(p, 3, s);
-      JUBIK_TRY_CUDA(cudaMemsetAsync(out, 0, image_elems(p) * p->esz, s));
-    }
     FusedLaunch a{x, out, p->hmain, p->hnyq, p->tw, p->wt, scale, p->spec};
+    if (p->spec && also_zero) {
+      a.aux = also_zero;
+      a.aux_bytes = also_zero_bytes;
+      if (zeroed) *zeroed = true;
+    }
     if (!p->spec) {
+      {
+        Phase ph(p, 3, s);
+        JUBIK_TRY_CUDA(cudaMemsetAsync(out, 0, image_elems(p) * p->esz, s));
+      }
       Phase ph(p, 0, s);
       return fused_run(g, p->dtype, a, FUSED_FWD_UNITS, s);
     }
-    {
+    {  // the sky-spectrum kernel also clears `out` for the overlap-add
       Phase ph(p, 4, s);
       JUBIK_TRY(fused_run(g, p->dtype, a, FUSED_FWD_SKY, s));
     }
@@ -321,28 +334,34 @@ int do_forward(jubik_plan* p, const void* x, void* out, double scale, cudaStream
 }
 
 // transpose: out_x (E,nx,ny) = scale * sum_m psf_m^T cot[m]
-int do_adjoint(jubik_plan* p, const void* cot, void* out_x, double scale, cudaStream_t s) {
+int do_adjoint(jubik_plan* p, const void* cot, void* out_x, double scale, cudaStream_t s,
+               bool out_zeroed = false) {
   const Geom& g = p->g;
   if (p->path == JUBIK_PATH_FUSED) {
-    {
-      Phase ph(p, 3, s);
-      JUBIK_TRY_CUDA(cudaMemsetAsync(out_x, 0, (size_t)g.E * g.pixels() * p->esz, s));
-    }
-    FusedLaunch a{cot, out_x, p->hmain, p->hnyq, p->tw, p->wt, scale, p->spec};
     if (!p->spec) {
+      {
+        Phase ph(p, 3, s);
+        JUBIK_TRY_CUDA(cudaMemsetAsync(out_x, 0, (size_t)g.E * g.pixels() * p->esz, s));
+      }
+      FusedLaunch a{cot, out_x, p->hmain, p->hnyq, p->tw, p->wt, scale, nullptr};
       Phase ph(p, 1, s);
       return fused_run(g, p->dtype, a, FUSED_ADJ_UNITS, s);
     }
-    {
-      Phase ph(p, 3, s);
-      JUBIK_TRY_CUDA(cudaMemsetAsync(p->spec, 0, fused_spec_bytes(g, p->dtype), s));
-    }
+    // per-unit kernel: clears out_x and adds into the (zero) accumulator; per-patch
+    // kernel: reads and clears the accumulator, adds into out_x
+    FusedLaunch a{cot, out_x, p->hmain, p->hnyq, p->tw, p->wt, scale, p->acc};
+    a.zero_out = !out_zeroed;
+    int st;
     {
       Phase ph(p, 1, s);
-      JUBIK_TRY(fused_run(g, p->dtype, a, FUSED_ADJ_TO_SPEC, s));
+      st = fused_run(g, p->dtype, a, FUSED_ADJ_TO_SPEC, s);
     }
-    Phase ph(p, 5, s);
-    return fused_run(g, p->dtype, a, FUSED_ADJ_FROM_SPEC, s);
+    if (!st) {
+      Phase ph(p, 5, s);
+      st = fused_run(g, p->dtype, a, FUSED_ADJ_FROM_SPEC, s);
+    }
+    if (st) cudaMemsetAsync(p->acc, 0, fused_spec_bytes(g, p->dtype), s);  // restore the zeros
+    return st;
   }
   Phase ph(p, 1, s);
   const bool f32 = p->dtype == JUBIK_F32;
@@ -488,6 +507,10 @@ int jubik_plan_create(const jubik_plan_desc* d, jubik_plan** out) {
     if ((st = p->alloc(&p->hmain, (size_t)units * g.P * (g.P / 2) * csz))) return fail(st);
     if ((st = p->alloc(&p->hnyq, (size_t)units * g.P * csz))) return fail(st);
     if (share && (st = p->alloc(&p->spec, fused_spec_bytes(g, p->dtype)))) return fail(st);
+    if (share && (st = p->alloc(&p->acc, fused_spec_bytes(g, p->dtype)))) return fail(st);
+    if (share && (st = cuda_status(cudaMemset(p->acc, 0, fused_spec_bytes(g, p->dtype)),
+                                   "memset accumulator")))
+      return fail(st);
   } else {
     if ((st = p->alloc(&p->hfull, (size_t)units * g.P * g.P * csz))) return fail(st);
     const int64_t n2p = (int64_t)g.n * g.n;
@@ -749,7 +772,9 @@ int jubik_poisson_energy_grad(jubik_plan* p, const void* x, double* energy, void
   JUBIK_TRY(need(p->psf_set, "PSF"));
   JUBIK_TRY(need(p->data_set, "data"));
   cudaStream_t s = S(stream);
-  JUBIK_TRY(do_forward(p, x, p->conv, p->desc.pixel_area, s));
+  bool grad_zeroed = false;
+  JUBIK_TRY(do_forward(p, x, p->conv, p->desc.pixel_area, s, grad_x,
+                       (int64_t)p->g.E * p->g.pixels() * (int64_t)p->esz, &grad_zeroed));
   const int64_t img = image_elems(p);
   {
   Phase ph(p, 2, s);
@@ -763,7 +788,7 @@ int jubik_poisson_energy_grad(jubik_plan* p, const void* x, double* energy, void
   }
   p->lam_valid = true;
   if (!grad_x) return JUBIK_OK;
-  return do_adjoint(p, p->resid, grad_x, p->desc.pixel_area, s);
+  return do_adjoint(p, p->resid, grad_x, p->desc.pixel_area, s, grad_zeroed);
 }
 
 int jubik_metric_apply(jubik_plan* p, const void* x, const void* v, void* out, void* stream) {
@@ -785,7 +810,9 @@ int jubik_metric_apply(jubik_plan* p, const void* x, const void* v, void* out, v
     p->lam_valid = true;
   }
   JUBIK_TRY(need(p->lam_valid, "lambda (call with x or after poisson_energy_grad)"));
-  JUBIK_TRY(do_forward(p, v, p->conv_v, p->desc.pixel_area, s));
+  bool out_zeroed = false;
+  JUBIK_TRY(do_forward(p, v, p->conv_v, p->desc.pixel_area, s, out,
+                       (int64_t)p->g.E * p->g.pixels() * (int64_t)p->esz, &out_zeroed));
   {
     Phase ph(p, 2, s);
     JUBIK_TRY(p->dtype == JUBIK_F32
@@ -793,7 +820,7 @@ int jubik_metric_apply(jubik_plan* p, const void* x, const void* v, void* out, v
                   : metric_weights<double>(p->conv_v, p->eps, p->ridx, p->lam, img, p->resid,
                                            s));
   }
-  return do_adjoint(p, p->resid, out, p->desc.pixel_area, s);
+  return do_adjoint(p, p->resid, out, p->desc.pixel_area, s, out_zeroed);
 }
 
 int jubik_poisson_energy(const void* lam, const int32_t* data, int64_t n, int32_t dtype,

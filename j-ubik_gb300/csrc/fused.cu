@@ -61,6 +61,10 @@ struct Args {
   const void* wt;
   void* spec;  // (E n^2, P, P/2) spectra shared by the modules of a patch
   double scale;
+  int64_t zchunk;  // bytes of `out` each CTA clears (sky-spectrum and adjoint per-unit kernels)
+  void* aux;       // sky-spectrum kernel: a further buffer to clear (aux_bytes, aux_chunk per CTA)
+  int64_t aux_bytes, aux_chunk;
+  int zero_out;    // adjoint per-unit kernel: clear `out` first
   int M, E, nx, ny, n, dx, margin, half, sr_max, sc_max;
 };
 
@@ -97,6 +101,33 @@ __device__ __forceinline__ void cp_async_in(T* dst, const T* src) {
 }
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
+}
+
+// Programmatic dependent launch: every kernel of a step lets the next one be
+// scheduled as soon as all of its CTAs run (launch_dependents), and waits for
+// the previous kernel's completion and memory (wait) before it touches
+// anything that kernel, or one before it, writes or reads.
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// CTA blockIdx.x of the grid clears its share (chunk bytes, a multiple of 16,
+// computed on the host) of nbytes at base (16-byte stores when base is
+// 16-byte aligned).
+__device__ __forceinline__ void zero_slice(void* base, int64_t nbytes, int64_t chunk) {
+  const int64_t lo = (int64_t)blockIdx.x * chunk;
+  const int64_t hi = lo + chunk < nbytes ? lo + chunk : nbytes;
+  if (lo >= hi) return;
+  unsigned char* p = static_cast<unsigned char*>(base);
+  int64_t b = lo;
+  if ((reinterpret_cast<uintptr_t>(p) & 15) == 0) {
+    const int64_t n16 = (hi - lo) >> 4;
+    float4* q = reinterpret_cast<float4*>(p + lo);
+    for (int64_t i = threadIdx.x; i < n16; i += blockDim.x) q[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    b = lo + (n16 << 4);
+  }
+  for (int64_t i = b + threadIdx.x; i < hi; i += blockDim.x) p[i] = 0;
 }
 
 // 4 consecutive floats added to global memory in one reduction (16-byte aligned)
@@ -753,8 +784,10 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fused(Args a) {
   using R = Tr<T, P>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Unit<T, P> U;
+  pdl_trigger();
   U.init(a, smem_raw, true);
   prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
+  pdl_wait();
   stage_input<T, P, ADJ>(U, a);
   stage_split<T, P>(U);
   __syncthreads();
@@ -769,12 +802,17 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fused(Args a) {
   stage_output<T, P, ADJ>(U, a);
 }
 
-// Forward, module-shared: the sky spectrum of each (energy, patch) once ...
+// Forward, module-shared: the sky spectrum of each (energy, patch) once; the
+// CTAs also clear the (M,E,nx,ny) output that the next kernel adds into ...
 template <typename T, int P>
 __global__ void __launch_bounds__(Tr<T, P>::NT) k_sky_spec(Args a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Unit<T, P> U;
+  pdl_trigger();
   U.init(a, smem_raw, false);
+  pdl_wait();
+  zero_slice(a.out, (int64_t)a.M * a.E * a.nx * a.ny * (int64_t)sizeof(T), a.zchunk);
+  if (a.aux) zero_slice(a.aux, a.aux_bytes, a.aux_chunk);
   stage_input<T, P, false>(U, a);
   stage_split<T, P>(U);
   __syncthreads();
@@ -789,8 +827,10 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_from_spec(Args a) {
   using R = Tr<T, P>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Unit<T, P> U;
+  pdl_trigger();
   U.init(a, smem_raw, true);
   prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
+  pdl_wait();
   if (threadIdx.x == 32) prefetch_l2(U.spec, sizeof(cx<T>) * P * R::H);
   stage_mid<T, P, MID_FROM_SPEC, false>(U);
   __syncthreads();
@@ -802,14 +842,18 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_from_spec(Args a) {
 }
 
 // Adjoint, module-shared: per unit, cotangent spectrum * conj(PSF spectrum)
-// added into the patch's accumulator ...
+// added into the patch's (zero) accumulator; the CTAs also clear the
+// (E,nx,ny) output that the next kernel adds into ...
 template <typename T, int P>
 __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_to_spec(Args a) {
   using R = Tr<T, P>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Unit<T, P> U;
+  pdl_trigger();
   U.init(a, smem_raw, true);
   prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
+  pdl_wait();
+  if (a.zero_out) zero_slice(a.out, (int64_t)a.E * a.nx * a.ny * (int64_t)sizeof(T), a.zchunk);
   stage_input<T, P, true>(U, a);
   stage_split<T, P>(U);
   __syncthreads();
@@ -818,13 +862,16 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_to_spec(Args a) {
   stage_mid<T, P, MID_TO_ACC, true>(U);
 }
 
-// ... then, per (energy, patch), one inverse transform -> window -> gradient.
+// ... then, per (energy, patch), one inverse transform -> window -> gradient;
+// the accumulator is cleared as it is read.
 template <typename T, int P>
 __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_from_spec(Args a) {
   using R = Tr<T, P>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Unit<T, P> U;
+  pdl_trigger();
   U.init(a, smem_raw, false);
+  pdl_wait();
   stage_mid<T, P, MID_FROM_ACC, true>(U);
   __syncthreads();
   stage_invB<T, P, 0>(U, U.tid, R::NT);
@@ -832,6 +879,10 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_from_spec(Args a) {
   stage_combine<T, P>(U, U.mg / 2, (U.mg + U.K + 1) / 2);
   __syncthreads();
   stage_output<T, P, true>(U, a);
+  // leave this patch's accumulator zero for the next call (read in the first stage)
+  float4* z = reinterpret_cast<float4*>(U.spec);
+  constexpr int n16 = (int)(sizeof(cx<T>) * P * R::H / 16);
+  for (int i = threadIdx.x; i < n16; i += R::NT) z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 template <typename KernelT>
@@ -886,6 +937,16 @@ int launch_one(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
   }
   const int64_t units = g.units();
   const int64_t patches = (int64_t)g.E * g.n * g.n;
+  {
+    const int64_t grid = which == FUSED_FWD_SKY ? patches : units;
+    const int64_t zbytes = (which == FUSED_FWD_SKY ? (int64_t)g.M : 1) * g.E * g.pixels() *
+                           (int64_t)sizeof(T);
+    a.zchunk = grid > 0 ? ((zbytes + grid - 1) / grid + 15) & ~(int64_t)15 : 0;
+    a.aux = f.aux;
+    a.aux_bytes = f.aux ? f.aux_bytes : 0;
+    a.aux_chunk = grid > 0 ? ((a.aux_bytes + grid - 1) / grid + 15) & ~(int64_t)15 : 0;
+    a.zero_out = f.zero_out ? 1 : 0;
+  }
   if (units <= 0) return JUBIK_OK;
   if (units > 0x7fffffffLL) {
     set_error("too many patch units for one launch");
@@ -895,30 +956,32 @@ int launch_one(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
     set_error("module-shared kernels need the spectrum workspace");
     return JUBIK_ERR_STATE;
   }
+  // launched with programmatic stream serialisation: the kernel may be
+  // scheduled while the previous kernel of the stream drains (see pdl_wait)
+  auto launch = [&](auto kern, int64_t grid) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(R::NT);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cuda_status(cudaLaunchKernelEx(&cfg, kern, a), "fused kernel launch");
+  };
   switch (which) {
-    case FUSED_FWD_UNITS:
-      k_fused<T, P, false><<<(unsigned)units, R::NT, smem, s>>>(a);
-      break;
-    case FUSED_ADJ_UNITS:
-      k_fused<T, P, true><<<(unsigned)units, R::NT, smem, s>>>(a);
-      break;
-    case FUSED_FWD_SKY:
-      k_sky_spec<T, P><<<(unsigned)patches, R::NT, smem, s>>>(a);
-      break;
-    case FUSED_FWD_FROM_SPEC:
-      k_fwd_from_spec<T, P><<<(unsigned)units, R::NT, smem, s>>>(a);
-      break;
-    case FUSED_ADJ_TO_SPEC:
-      k_adj_to_spec<T, P><<<(unsigned)units, R::NT, smem, s>>>(a);
-      break;
-    case FUSED_ADJ_FROM_SPEC:
-      k_adj_from_spec<T, P><<<(unsigned)patches, R::NT, smem, s>>>(a);
-      break;
+    case FUSED_FWD_UNITS: return launch(k_fused<T, P, false>, units);
+    case FUSED_ADJ_UNITS: return launch(k_fused<T, P, true>, units);
+    case FUSED_FWD_SKY: return launch(k_sky_spec<T, P>, patches);
+    case FUSED_FWD_FROM_SPEC: return launch(k_fwd_from_spec<T, P>, units);
+    case FUSED_ADJ_TO_SPEC: return launch(k_adj_to_spec<T, P>, units);
+    case FUSED_ADJ_FROM_SPEC: return launch(k_adj_from_spec<T, P>, patches);
     default:
       set_error("unknown fused stage %d", which);
       return JUBIK_ERR_INVALID_ARGUMENT;
   }
-  return cuda_status(cudaGetLastError(), "fused kernel launch");
 }
 
 template <typename T>

@@ -82,6 +82,9 @@ struct FusedLaunch {
   const void* wt;       // (2*dx) bilinear weight vector
   double scale;
   void* spec = nullptr; // (E n^2, P, P/2) shared spectra: module-shared kernels when set
+  void* aux = nullptr;  // module-shared forward: a further buffer the sky-spectrum kernel clears
+  int64_t aux_bytes = 0;
+  bool zero_out = true; // module-shared adjoint: the per-unit kernel clears `out` first
 };
 size_t fused_spec_bytes(const Geom& g, int dtype);
 enum FusedStage {

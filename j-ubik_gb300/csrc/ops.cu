@@ -495,6 +495,10 @@ __global__ void __launch_bounds__(kBlock)
                     const int32_t* __restrict__ dimg, int64_t npix, T* __restrict__ lam_cache,
                     T* __restrict__ resid, double* partials, unsigned int* counter,
                     double* energy) {
+  // launched with programmatic stream serialisation after the forward kernels:
+  // let the adjoint be scheduled early, wait for the forward image
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   Kahan<T> s_lam, s_dlog;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t p0 = 0;
@@ -706,10 +710,19 @@ template <typename T>
 int poisson_image(const void* conv, const void* eps, const int32_t* dimg, int64_t npix,
                   void* lam_cache, void* resid, double* partials, unsigned int* counter,
                   double* energy, cudaStream_t s) {
-  k_poisson_image<T><<<kRedBlocks, kBlock, 0, s>>>((const T*)conv, (const T*)eps, dimg, npix,
-                                                   (T*)lam_cache, (T*)resid, partials, counter,
-                                                   energy);
-  return cuda_status(cudaGetLastError(), "k_poisson_image");
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kRedBlocks);
+  cfg.blockDim = dim3(kBlock);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cuda_status(cudaLaunchKernelEx(&cfg, k_poisson_image<T>, (const T*)conv, (const T*)eps,
+                                        dimg, npix, (T*)lam_cache, (T*)resid, partials, counter,
+                                        energy),
+                     "k_poisson_image");
 }
 
 int count_image(const int32_t* ridx, const int32_t* data, int64_t npix, int32_t* dimg,
