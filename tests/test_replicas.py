@@ -30,7 +30,7 @@ def _rank(rank, world, port, out):
 
 def test_two_gloo_replicas_take_the_slowest_rank():
     port = _free_port()
-    manager = mp.Manager()
+    manager = mp.get_context("spawn").Manager()  # no fork of a threaded process
     out = manager.dict()
     mp.spawn(_rank, args=(2, port, out), nprocs=2, join=True)
     for r in range(2):
