@@ -505,18 +505,28 @@ __global__ void __launch_bounds__(kBlock)
   if constexpr (sizeof(T) == 4) {
     // 4 pixels per thread with 16-byte accesses (all image bases are 16-byte aligned)
     const int64_t n4 = npix / 4;
-    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n4; g += stride) {
-      const float4 c = reinterpret_cast<const float4*>(conv)[g];
-      const float4 ep = eps ? reinterpret_cast<const float4*>(eps)[g] : make_float4(1, 1, 1, 1);
-      const int4 d = reinterpret_cast<const int4*>(dimg)[g];
+    const float4* c4 = reinterpret_cast<const float4*>(conv);
+    const float4* e4 = reinterpret_cast<const float4*>(eps);
+    const int4* d4 = reinterpret_cast<const int4*>(dimg);
+    auto px4 = [&](int64_t g, float4 c, float4 ep, int4 d) {
       float4 l, r;
       poisson_px<T>(c.x, ep.x, d.x, l.x, r.x, s_lam, s_dlog);
       poisson_px<T>(c.y, ep.y, d.y, l.y, r.y, s_lam, s_dlog);
       poisson_px<T>(c.z, ep.z, d.z, l.z, r.z, s_lam, s_dlog);
       poisson_px<T>(c.w, ep.w, d.w, l.w, r.w, s_lam, s_dlog);
       if (resid) reinterpret_cast<float4*>(resid)[g] = r;
-      if (lam_cache) reinterpret_cast<float4*>(lam_cache)[g] = l;
+      if (lam_cache) __stcs(reinterpret_cast<float4*>(lam_cache) + g, l);
+    };
+    int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    for (; g + stride < n4; g += 2 * stride) {
+      const float4 ca = __ldcs(c4 + g), cb = __ldcs(c4 + g + stride);
+      const float4 ea = eps ? __ldcs(e4 + g) : make_float4(1, 1, 1, 1);
+      const float4 eb = eps ? __ldcs(e4 + g + stride) : make_float4(1, 1, 1, 1);
+      const int4 da = __ldcs(d4 + g), db = __ldcs(d4 + g + stride);
+      px4(g, ca, ea, da);
+      px4(g + stride, cb, eb, db);
     }
+    if (g < n4) px4(g, __ldcs(c4 + g), eps ? __ldcs(e4 + g) : make_float4(1, 1, 1, 1), __ldcs(d4 + g));
     p0 = n4 * 4;
   }
   for (int64_t p = p0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npix; p += stride) {
