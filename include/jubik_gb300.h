@@ -147,6 +147,13 @@ JUBIK_API int jubik_metric_apply(jubik_plan* plan, const void* x, const void* v,
  * 3 memsets, 4 forward per-patch sky-spectrum kernel, 5 adjoint per-patch
  * inverse kernel (4 and 5 run when modules share patch spectra). */
 #define JUBIK_PHASES 6
+/* Programmatic dependent launch between the kernels of one plan call (default
+ * on; no counterpart in the reference): each kernel may be scheduled onto the
+ * SMs the previous kernel's last wave frees, and waits there for that kernel's
+ * results.  Plans whose calls run side by side on several streams (e.g. the
+ * branches of one CUDA graph) may switch it off, so that waiting kernels do
+ * not hold SMs the other streams could use. */
+JUBIK_API int jubik_plan_set_dependent_launch(jubik_plan* plan, int32_t on);
 JUBIK_API int jubik_plan_set_profiling(jubik_plan* plan, int32_t on);
 /* ms and launch counts per phase accumulated since profiling was switched on. */
 JUBIK_API int jubik_plan_profile(const jubik_plan* plan, double* ms, int64_t* launches);

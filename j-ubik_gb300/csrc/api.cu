@@ -201,6 +201,7 @@ struct jubik_plan {
   void* hnyq = nullptr;
   void* hfull = nullptr;
   void* spec = nullptr;  // per-(energy, patch) spectra shared by the modules
+  bool pdl = true;       // programmatic dependent launch between the kernels of a call
   void* acc = nullptr;   // per-(energy, patch) adjoint sums over modules; all zero between
                          // calls (zeroed when allocated, cleared by their reader)
   // images (M,E,nx,ny)
@@ -294,6 +295,7 @@ int do_forward(jubik_plan* p, const void* x, void* out, double scale, cudaStream
   if (zeroed) *zeroed = false;
   if (p->path == JUBIK_PATH_FUSED) {
     FusedLaunch a{x, out, p->hmain, p->hnyq, p->tw, p->wt, scale, p->spec};
+    a.pdl = p->pdl;
     if (p->spec && also_zero) {
       a.aux = also_zero;
       a.aux_bytes = also_zero_bytes;
@@ -344,6 +346,7 @@ int do_adjoint(jubik_plan* p, const void* cot, void* out_x, double scale, cudaSt
         JUBIK_TRY_CUDA(cudaMemsetAsync(out_x, 0, (size_t)g.E * g.pixels() * p->esz, s));
       }
       FusedLaunch a{cot, out_x, p->hmain, p->hnyq, p->tw, p->wt, scale, nullptr};
+      a.pdl = p->pdl;
       Phase ph(p, 1, s);
       return fused_run(g, p->dtype, a, FUSED_ADJ_UNITS, s);
     }
@@ -351,6 +354,7 @@ int do_adjoint(jubik_plan* p, const void* cot, void* out_x, double scale, cudaSt
     // kernel: reads and clears the accumulator, adds into out_x
     FusedLaunch a{cot, out_x, p->hmain, p->hnyq, p->tw, p->wt, scale, p->acc};
     a.zero_out = !out_zeroed;
+    a.pdl = p->pdl;
     int st;
     {
       Phase ph(p, 1, s);
@@ -562,6 +566,12 @@ int jubik_plan_workspace_bytes(const jubik_plan* plan, int64_t* bytes) {
 int jubik_plan_path(const jubik_plan* plan, int32_t* path) {
   JUBIK_TRY(check_plan(plan));
   if (path) *path = plan->path;
+  return JUBIK_OK;
+}
+
+int jubik_plan_set_dependent_launch(jubik_plan* p, int32_t on) {
+  JUBIK_TRY(check_plan(p));
+  p->pdl = on != 0;
   return JUBIK_OK;
 }
 
@@ -781,10 +791,10 @@ int jubik_poisson_energy_grad(jubik_plan* p, const void* x, double* energy, void
   JUBIK_TRY(p->dtype == JUBIK_F32
                 ? poisson_image<float>(p->conv, p->eps, p->dimg, img, p->lam,
                                        grad_x ? p->resid : nullptr, p->partials, p->counter,
-                                       energy, s)
+                                       energy, p->pdl, s)
                 : poisson_image<double>(p->conv, p->eps, p->dimg, img, p->lam,
                                         grad_x ? p->resid : nullptr, p->partials, p->counter,
-                                        energy, s));
+                                        energy, p->pdl, s));
   }
   p->lam_valid = true;
   if (!grad_x) return JUBIK_OK;

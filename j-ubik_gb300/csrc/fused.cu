@@ -966,7 +966,7 @@ int launch_one(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    attr[0].val.programmaticStreamSerializationAllowed = f.pdl ? 1 : 0;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     return cuda_status(cudaLaunchKernelEx(&cfg, kern, a), "fused kernel launch");

@@ -85,6 +85,7 @@ struct FusedLaunch {
   void* aux = nullptr;  // module-shared forward: a further buffer the sky-spectrum kernel clears
   int64_t aux_bytes = 0;
   bool zero_out = true; // module-shared adjoint: the per-unit kernel clears `out` first
+  bool pdl = true;      // launch with programmatic stream serialisation
 };
 size_t fused_spec_bytes(const Geom& g, int dtype);
 enum FusedStage {
@@ -138,7 +139,7 @@ int readout_scatter(const void* vec, const void* eps, const int64_t* idx, int64_
 template <typename T>
 int poisson_image(const void* conv, const void* eps, const int32_t* dimg, int64_t npix,
                   void* lam_cache, void* resid, double* partials, unsigned int* counter,
-                  double* energy, cudaStream_t s);
+                  double* energy, bool pdl, cudaStream_t s);
 int count_image(const int32_t* ridx, const int32_t* data, int64_t npix, int32_t* dimg,
                 cudaStream_t s);
 template <typename T>

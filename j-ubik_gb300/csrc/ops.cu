@@ -719,14 +719,14 @@ int readout_scatter(const void* vec, const void* eps, const int64_t* idx, int64_
 template <typename T>
 int poisson_image(const void* conv, const void* eps, const int32_t* dimg, int64_t npix,
                   void* lam_cache, void* resid, double* partials, unsigned int* counter,
-                  double* energy, cudaStream_t s) {
+                  double* energy, bool pdl, cudaStream_t s) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(kRedBlocks);
   cfg.blockDim = dim3(kBlock);
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  attr[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   return cuda_status(cudaLaunchKernelEx(&cfg, k_poisson_image<T>, (const T*)conv, (const T*)eps,
@@ -789,7 +789,7 @@ int elementwise_op(int op, const void* a, const void* b, const int32_t* d, int64
   template int readout_scatter<T>(const void*, const void*, const int64_t*, int64_t, void*,      \
                                   cudaStream_t);                                                 \
   template int poisson_image<T>(const void*, const void*, const int32_t*, int64_t, void*, void*, \
-                                double*, unsigned int*, double*, cudaStream_t);                  \
+                                double*, unsigned int*, double*, bool, cudaStream_t);            \
   template int metric_weights<T>(const void*, const void*, const int32_t*, const void*, int64_t, \
                                  void*, cudaStream_t);                                           \
   template int poisson_vec<T>(const void*, const int32_t*, int64_t, double*, unsigned int*,      \

@@ -118,6 +118,11 @@ class ResponsePlan:
 
     PHASES = ("forward", "adjoint", "likelihood", "memset", "forward_patch", "adjoint_patch")
 
+    def set_dependent_launch(self, on: bool = True) -> "ResponsePlan":
+        """Programmatic dependent launch between the kernels of a call (default on)."""
+        _lib.call("jubik_plan_set_dependent_launch", self._h, 1 if on else 0)
+        return self
+
     def set_profiling(self, on: bool = True) -> None:
         """Bracket every kernel phase with CUDA events (resets the totals)."""
         _lib.call("jubik_plan_set_profiling", self._h, int(bool(on)))

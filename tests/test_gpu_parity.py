@@ -329,3 +329,24 @@ def test_response_vector_interface(cuda):
         assert rel(out.tree[k], ref(inst.sky)[i]) < 1e-12
     # the reference's keys, plus the readout transpose its diagnostics expect
     assert set(rd) == {"pix_area", "psf", "exposure", "mask", "kernel", "R", "mask_adj"}
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32], ids=["f64", "f32"])
+def test_dependent_launch_switch_keeps_results(cuda, dtype):
+    """The module-shared step runs as one chain of dependent launches; with the
+    chain switched off the same kernels run fully serialised."""
+    nx, dx, m, M, E = 128, 32, 16, 3, 2
+    inst = synthetic.config2(nx=nx, dx=dx, margin=m, n_modules=M, n_energies=E)
+    plan = ju.ResponsePlan(M, E, (nx, nx), nx // dx, m, dtype=dtype).set_psf(inst.psf)
+    plan.set_exposure(inst.exposure, inst.readmask)
+    lam = plan.response(inst.sky).double().cpu().numpy()
+    plan.set_data(synthetic.poisson_data(lam, 2))
+    tol = 1e-13 if dtype == torch.float64 else 1e-6
+    e1, g1 = plan.energy_and_grad(inst.sky)
+    g1 = g1.clone()
+    plan.set_dependent_launch(False)
+    for _ in range(2):  # twice: the adjoint accumulator is left zero after each call
+        e2, g2 = plan.energy_and_grad(inst.sky)
+        assert abs(float(e2) - float(e1)) <= tol * abs(float(e1))
+        assert rel(g2, g1.double().cpu().numpy()) < (1e-13 if dtype == torch.float64 else 1e-5)
+    plan.close()
