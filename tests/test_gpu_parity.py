@@ -350,3 +350,52 @@ def test_dependent_launch_switch_keeps_results(cuda, dtype):
         assert abs(float(e2) - float(e1)) <= tol * abs(float(e1))
         assert rel(g2, g1.double().cpu().numpy()) < (1e-13 if dtype == torch.float64 else 1e-5)
     plan.close()
+
+
+def test_fully_masked_module_and_empty_readout(cuda):
+    """A module whose every pixel is masked reads out nothing: its readout is
+    empty, it adds nothing to the energy and nothing to the gradient."""
+    nx, dx, m, M, E = 128, 32, 16, 3, 2
+    inst = synthetic.config2(nx=nx, dx=dx, margin=m, n_modules=M, n_energies=E)
+    readmask = inst.readmask.copy()
+    readmask[1] = False
+    exposure = inst.exposure * readmask
+    dom = O.Domain((E, nx, nx), (1.0, 1.0, 1.0))
+    R = O.Response(dom, inst.psf, nx // dx, m, exposure, readmask)
+    lam = R(inst.sky)
+    assert lam[1].size == 0
+    data = [synthetic.poisson_data(l, 9 + i) if l.size else np.zeros(0, np.int32)
+            for i, l in enumerate(lam)]
+    e_ref, g_ref = R.energy_and_grad(inst.sky, data)
+    for dtype in (torch.float64, torch.float32):
+        plan = ju.ResponsePlan(M, E, (nx, nx), nx // dx, m, dtype=dtype).set_psf(inst.psf)
+        plan.set_exposure(exposure, readmask).set_data(np.concatenate(data))
+        assert plan.readout_sizes[1] == 0
+        e, g = plan.energy_and_grad(inst.sky)
+        tol = 1e-12 if dtype == torch.float64 else 1e-6
+        assert abs(float(e) - e_ref) / abs(e_ref) < tol
+        assert rel(plan.response(inst.sky), np.concatenate(lam)) < tol
+        plan.close()
+
+
+def test_large_field_adjoint_identity(cuda):
+    """4096^2 field, 64 x 64 patches (4096 units, P = 192): the adjoint
+    identity and FP32 against FP64 at a size far beyond the oracle's reach."""
+    nx, dx, m = 4096, 64, 32
+    rng = np.random.default_rng(12)
+    K = 2 * dx
+    u = np.arange(K) - dx
+    g = np.exp(-0.5 * (u[:, None] ** 2 + u[None, :] ** 2) / 9.0)
+    psf = np.broadcast_to((g / g.sum())[None, None], (1, (nx // dx) ** 2, K, K)).copy()
+    x = torch.as_tensor(rng.random((1, nx, nx)), device=cuda)
+    y = torch.as_tensor(rng.normal(size=(1, 1, nx, nx)), device=cuda)
+    p64 = ju.ResponsePlan(1, 1, (nx, nx), nx // dx, m, dtype=torch.float64).set_psf(psf)
+    p32 = ju.ResponsePlan(1, 1, (nx, nx), nx // dx, m, dtype=torch.float32).set_psf(psf)
+    a64 = p64.psf_forward(x)
+    b64 = p64.psf_adjoint(y)
+    lhs, rhs = float((a64 * y).sum()), float((x * b64).sum())
+    assert abs(lhs - rhs) <= 1e-12 * float(torch.linalg.norm(a64) * torch.linalg.norm(y))
+    assert rel(p32.psf_forward(x.float()), a64.cpu().numpy()) < 1e-6
+    assert rel(p32.psf_adjoint(y.float()), b64.cpu().numpy()) < 1e-6
+    p64.close()
+    p32.close()
