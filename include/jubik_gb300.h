@@ -135,6 +135,15 @@ JUBIK_API int jubik_response_vjp(jubik_plan* plan, const void* cot_readout, void
  * in the plan for jubik_metric_apply. */
 JUBIK_API int jubik_poisson_energy_grad(jubik_plan* plan, const void* x, double* energy, void* grad_x,
                               void* stream);
+/* The same for a sky given as the exp of the (E, nx, ny) crop of a log-sky
+ * array s (e_pad, nx_pad, ny_pad): sky = exp(s[:E, :nx, :ny]), the
+ * exp_padding of J-UBIK's diffuse sky model (jubik/sky_models.py:340-341).
+ * The exp and the crop happen inside the response's first kernel;
+ * grad_s (shape of s, may be NULL) = exp(s) * R^T(1 - d/lam) on the crop and 0
+ * elsewhere. */
+JUBIK_API int jubik_poisson_energy_grad_logsky(jubik_plan* plan, const void* s, int32_t e_pad,
+                                               int32_t nx_pad, int32_t ny_pad, double* energy,
+                                               void* grad_s, void* stream);
 /* MGVI metric product out = R^T diag(1/lam) R v, lam = R(x).  x == NULL
  * reuses lam from the last jubik_poisson_energy_grad call. */
 JUBIK_API int jubik_metric_apply(jubik_plan* plan, const void* x, const void* v, void* out,

@@ -53,3 +53,19 @@ class PoissonEnergyFn(torch.autograd.Function):
     def backward(ctx, ge):
         (g,) = ctx.saved_tensors
         return (ge.to(g.dtype) * g), None
+
+
+class LogSkyPoissonEnergyFn(torch.autograd.Function):
+    """s -> H(R(exp(s[:E, :nx, :ny]))) (float64 scalar) for a padded log-sky s,
+    the exp_padding of ``jubik/sky_models.py:340-341``; dH/ds from the fused pass."""
+
+    @staticmethod
+    def forward(ctx, s, plan):
+        e, g = plan.energy_and_grad_logsky(s, need_grad=True)
+        ctx.save_for_backward(g)
+        return e
+
+    @staticmethod
+    def backward(ctx, ge):
+        (g,) = ctx.saved_tensors
+        return (ge.to(g.dtype) * g), None

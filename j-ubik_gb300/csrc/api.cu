@@ -130,6 +130,32 @@ __global__ void k_real_out(const cx<T>* __restrict__ z, int64_t n, T scale, T* _
     out[i] = scale * z[i].x;
 }
 
+// sky = exp(s) on the (E, nx, ny) crop of a log-sky array s with plane
+// stride ps and row stride rs (the unfused path reads a materialised sky)
+template <typename T>
+__global__ void k_exp_crop(const T* __restrict__ s, int E, int nx, int ny, int64_t ps,
+                           int64_t rs, T* __restrict__ x) {
+  const int64_t n = (int64_t)E * nx * ny;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = i / ((int64_t)nx * ny), r = (i / ny) % nx, c = i % ny;
+    x[i] = exp(s[e * ps + r * rs + c]);
+  }
+}
+
+// chain rule through sky = exp(s[:E, :nx, :ny]): grad_s = exp(s) * grad_x on the
+// crop, 0 on the rest of the (Ep, n0p, n1p) log-sky array
+template <typename T>
+__global__ void k_logsky_grad(const T* __restrict__ s, const T* __restrict__ gx, int E, int nx,
+                              int ny, int Ep, int n0p, int n1p, T* __restrict__ gs) {
+  const int64_t n = (int64_t)Ep * n0p * n1p;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = i / ((int64_t)n0p * n1p), r = (i / n1p) % n0p, c = i % n1p;
+    gs[i] = (e < E && r < nx && c < ny) ? exp(s[i]) * gx[(e * nx + r) * ny + c] : (T)0;
+  }
+}
+
 inline unsigned blocks_for(int64_t n) {
   int64_t b = (n + 255) / 256;
   if (b > 1048576) b = 1048576;
@@ -210,6 +236,8 @@ struct jubik_plan {
   void* resid = nullptr;
   void* lam = nullptr;
   void* eps = nullptr;
+  void* xsky = nullptr;   // (E,nx,ny) sky from a log-sky input (unfused path)
+  void* xgrad = nullptr;  // (E,nx,ny) sky gradient before the chain rule to a log-sky
   int32_t* ridx = nullptr;
   int64_t* rlist = nullptr;
   int32_t* data = nullptr;
@@ -288,14 +316,35 @@ int64_t image_elems(const jubik_plan* p) { return (int64_t)p->g.M * p->g.E * p->
 // `also_zero` (module-shared path only): a buffer of `also_zero_bytes` for the
 // sky-spectrum kernel to clear as well -- the gradient that a later do_adjoint
 // with out_zeroed adds into.  Returns whether it was cleared.
+// How the forward reads its sky: the field itself (default), or exp of the
+// (E, nx, ny) crop of a log-sky array with plane stride ps and row stride rs.
+struct SkyView {
+  int64_t ps = 0, rs = 0;
+  bool exp = false;
+};
+
 int do_forward(jubik_plan* p, const void* x, void* out, double scale, cudaStream_t s,
                void* also_zero = nullptr, int64_t also_zero_bytes = 0,
-               bool* zeroed = nullptr) {
+               bool* zeroed = nullptr, SkyView view = SkyView()) {
   const Geom& g = p->g;
   if (zeroed) *zeroed = false;
+  if (view.exp && p->path != JUBIK_PATH_FUSED) {  // materialise the sky for the unfused path
+    const int64_t n = (int64_t)g.E * g.pixels();
+    if (p->dtype == JUBIK_F32)
+      k_exp_crop<float><<<blocks_for(n), 256, 0, s>>>((const float*)x, g.E, g.nx, g.ny, view.ps,
+                                                       view.rs, (float*)p->xsky);
+    else
+      k_exp_crop<double><<<blocks_for(n), 256, 0, s>>>((const double*)x, g.E, g.nx, g.ny,
+                                                        view.ps, view.rs, (double*)p->xsky);
+    JUBIK_TRY(cuda_status(cudaGetLastError(), "k_exp_crop"));
+    x = p->xsky;
+  }
   if (p->path == JUBIK_PATH_FUSED) {
     FusedLaunch a{x, out, p->hmain, p->hnyq, p->tw, p->wt, scale, p->spec};
     a.pdl = p->pdl;
+    a.in_ps = view.ps;
+    a.in_rs = view.rs;
+    a.in_exp = view.exp;
     if (p->spec && also_zero) {
       a.aux = also_zero;
       a.aux_bytes = also_zero_bytes;
@@ -528,6 +577,8 @@ int jubik_plan_create(const jubik_plan_desc* d, jubik_plan** out) {
   if ((st = p->alloc(&p->conv_v, img * p->esz))) return fail(st);
   if ((st = p->alloc(&p->resid, img * p->esz))) return fail(st);
   if ((st = p->alloc(&p->lam, img * p->esz))) return fail(st);
+  if ((st = p->alloc(&p->xsky, (size_t)g.E * g.pixels() * p->esz))) return fail(st);
+  if ((st = p->alloc(&p->xgrad, (size_t)g.E * g.pixels() * p->esz))) return fail(st);
   if ((st = p->alloc((void**)&p->ridx, img * sizeof(int32_t)))) return fail(st);
   if ((st = p->alloc((void**)&p->rlist, img * sizeof(int64_t)))) return fail(st);
   if ((st = p->alloc((void**)&p->partials, 2 * energy_partials_count() * sizeof(double))))
@@ -799,6 +850,53 @@ int jubik_poisson_energy_grad(jubik_plan* p, const void* x, double* energy, void
   p->lam_valid = true;
   if (!grad_x) return JUBIK_OK;
   return do_adjoint(p, p->resid, grad_x, p->desc.pixel_area, s, grad_zeroed);
+}
+
+int jubik_poisson_energy_grad_logsky(jubik_plan* p, const void* s_log, int32_t e_pad,
+                                     int32_t nx_pad, int32_t ny_pad, double* energy,
+                                     void* grad_s, void* stream) {
+  JUBIK_TRY(check_plan(p));
+  JUBIK_TRY(need(p->psf_set, "PSF"));
+  JUBIK_TRY(need(p->data_set, "data"));
+  const Geom& g = p->g;
+  if (!s_log || !energy || e_pad < g.E || nx_pad < g.nx || ny_pad < g.ny) {
+    set_error("log-sky array (%d, %d, %d) must cover the (%d, %d, %d) sky", e_pad, nx_pad,
+              ny_pad, g.E, g.nx, g.ny);
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  cudaStream_t s = S(stream);
+  SkyView view;
+  view.rs = ny_pad;
+  view.ps = (int64_t)nx_pad * ny_pad;
+  view.exp = true;
+  bool grad_zeroed = false;
+  JUBIK_TRY(do_forward(p, s_log, p->conv, p->desc.pixel_area, s, grad_s ? p->xgrad : nullptr,
+                       (int64_t)g.E * g.pixels() * (int64_t)p->esz, &grad_zeroed, view));
+  const int64_t img = image_elems(p);
+  {
+    Phase ph(p, 2, s);
+    JUBIK_TRY(p->dtype == JUBIK_F32
+                  ? poisson_image<float>(p->conv, p->eps, p->dimg, img, p->lam,
+                                         grad_s ? p->resid : nullptr, p->partials, p->counter,
+                                         energy, p->pdl, s)
+                  : poisson_image<double>(p->conv, p->eps, p->dimg, img, p->lam,
+                                          grad_s ? p->resid : nullptr, p->partials,
+                                          p->counter, energy, p->pdl, s));
+  }
+  p->lam_valid = true;
+  if (!grad_s) return JUBIK_OK;
+  JUBIK_TRY(do_adjoint(p, p->resid, p->xgrad, p->desc.pixel_area, s, grad_zeroed));
+  const int64_t n = (int64_t)e_pad * nx_pad * ny_pad;
+  if (p->dtype == JUBIK_F32)
+    k_logsky_grad<float><<<blocks_for(n), 256, 0, s>>>((const float*)s_log,
+                                                        (const float*)p->xgrad, g.E, g.nx, g.ny,
+                                                        e_pad, nx_pad, ny_pad, (float*)grad_s);
+  else
+    k_logsky_grad<double><<<blocks_for(n), 256, 0, s>>>((const double*)s_log,
+                                                         (const double*)p->xgrad, g.E, g.nx,
+                                                         g.ny, e_pad, nx_pad, ny_pad,
+                                                         (double*)grad_s);
+  return cuda_status(cudaGetLastError(), "k_logsky_grad");
 }
 
 int jubik_metric_apply(jubik_plan* p, const void* x, const void* v, void* out, void* stream) {

@@ -65,6 +65,8 @@ struct Args {
   void* aux;       // sky-spectrum kernel: a further buffer to clear (aux_bytes, aux_chunk per CTA)
   int64_t aux_bytes, aux_chunk;
   int zero_out;    // adjoint per-unit kernel: clear `out` first
+  int64_t in_rs, in_ps;  // forward input: row and plane strides (a crop of a larger array)
+  int in_exp;            // forward input holds log-sky values: the sky is their exp
   int M, E, nx, ny, n, dx, margin, half, sr_max, sc_max;
 };
 
@@ -261,14 +263,19 @@ __device__ __forceinline__ void stage_input(Unit<T, P>& U, const Args& a) {
   };
   const int xoff = ADJ ? 0 : mg;
   const int width = ADJ ? P : K;
+  // column weights, zero outside the window and outside the field (where the
+  // staged values are the zero fill, whose exp would not be zero)
   T wc[16];
 #pragma unroll
   for (int q = 0; q < 16; ++q) {
     const int xa = U.cls + L1 * q - mg;
-    wc[q] = (!ADJ && xa >= 0 && xa < K) ? U.wt[xa] : (T)0;
+    const int col = U.cb + U.cls + L1 * q;
+    wc[q] = (!ADJ && xa >= 0 && xa < K && col >= 0 && col < a.ny) ? U.wt[xa] : (T)0;
   }
+  // forward input: element (row, col) of energy e at e * in_ps + row * in_rs + col
+  const int64_t rs = ADJ ? (int64_t)a.ny : a.in_rs;
   const T* __restrict__ src =
-      (const T*)a.in + (ADJ ? ((int64_t)U.m * a.E + U.e) : (int64_t)U.e) * U.npix;
+      (const T*)a.in + (ADJ ? ((int64_t)U.m * a.E + U.e) * U.npix : (int64_t)U.e * a.in_ps);
   // adjoint units whose P x P window lies inside the field need no bounds checks
   const bool interior = ADJ && U.rb >= 0 && U.rb + P <= a.nx && U.cb >= 0 && U.cb + P <= a.ny;
   auto issue = [&](int c) {
@@ -276,12 +283,12 @@ __device__ __forceinline__ void stage_input(Unit<T, P>& U, const Args& a) {
     const int nch = min(CH, jhi - j0);
     if (ADJ && interior && NT % width == 0) {
       const int xs = U.tid % width, jstep = NT / width;
-      const T* gcol = src + (int64_t)U.rb * a.ny + U.cb + xs;
+      const T* gcol = src + (int64_t)U.rb * rs + U.cb + xs;
       for (int jj = U.tid / width; jj < nch; jj += jstep) {
-        const T* g0 = gcol + (int64_t)(2 * (j0 + jj)) * a.ny;
+        const T* g0 = gcol + (int64_t)(2 * (j0 + jj)) * rs;
         T* d = reinterpret_cast<T*>(bufp(c, jj) + xs);
         cp_async_in<T>(d, g0);
-        cp_async_in<T>(d + 1, g0 + a.ny);
+        cp_async_in<T>(d + 1, g0 + rs);
       }
     } else if (NT % width == 0) {
       // each thread owns one staged column and every (NT / width)-th pair row
@@ -296,8 +303,8 @@ __device__ __forceinline__ void stage_input(Unit<T, P>& U, const Args& a) {
         const bool ok1 = cok && row + 1 >= 0 && row + 1 < a.nx &&
                          (ADJ || (y0 + 1 - mg >= 0 && y0 + 1 - mg < K));
         T* d = reinterpret_cast<T*>(bufp(c, jj) + xs);
-        cp_async<T>(d, ok0 ? gcol + (int64_t)row * a.ny : src, ok0);
-        cp_async<T>(d + 1, ok1 ? gcol + (int64_t)(row + 1) * a.ny : src, ok1);
+        cp_async<T>(d, ok0 ? gcol + (int64_t)row * rs : src, ok0);
+        cp_async<T>(d + 1, ok1 ? gcol + (int64_t)(row + 1) * rs : src, ok1);
       }
     } else {
       for (int i = U.tid; i < nch * width; i += NT) {
@@ -311,8 +318,8 @@ __device__ __forceinline__ void stage_input(Unit<T, P>& U, const Args& a) {
         const bool ok1 = cok && row + 1 >= 0 && row + 1 < a.nx &&
                          (ADJ || (y0 + 1 - mg >= 0 && y0 + 1 - mg < K));
         T* d = reinterpret_cast<T*>(bufp(c, jj) + xs);
-        cp_async<T>(d, ok0 ? src + (int64_t)row * a.ny + col : src, ok0);
-        cp_async<T>(d + 1, ok1 ? src + (int64_t)(row + 1) * a.ny + col : src, ok1);
+        cp_async<T>(d, ok0 ? src + (int64_t)row * rs + col : src, ok0);
+        cp_async<T>(d + 1, ok1 ? src + (int64_t)(row + 1) * rs + col : src, ok1);
       }
     }
     cp_async_commit();
@@ -336,15 +343,20 @@ __device__ __forceinline__ void stage_input(Unit<T, P>& U, const Args& a) {
     __syncthreads();
     for (int jj = U.lane; jj < nch; jj += 32) {
       const int y0 = 2 * (j0 + jj);
-      const T wr0 = (!ADJ && y0 - mg >= 0 && y0 - mg < K) ? U.wt[y0 - mg] : (T)0;
-      const T wr1 = (!ADJ && y0 + 1 - mg >= 0 && y0 + 1 - mg < K) ? U.wt[y0 + 1 - mg] : (T)0;
+      const int row0 = U.rb + y0;
+      const T wr0 = (!ADJ && y0 - mg >= 0 && y0 - mg < K && row0 >= 0 && row0 < a.nx)
+                        ? U.wt[y0 - mg] : (T)0;
+      const T wr1 = (!ADJ && y0 + 1 - mg >= 0 && y0 + 1 - mg < K && row0 + 1 >= 0 &&
+                     row0 + 1 < a.nx)
+                        ? U.wt[y0 + 1 - mg] : (T)0;
       const cx<T>* bsrc = bufp(c, jj);
       cx<T> v[16];
 #pragma unroll
       for (int q = 0; q < 16; ++q) {
         const int xs = U.cls + L1 * q - xoff;
         if (xs >= 0 && xs < width) {
-          const cx<T> t = bsrc[xs];
+          cx<T> t = bsrc[xs];
+          if (!ADJ && a.in_exp) t = mkc<T>(exp(t.x), exp(t.y));
           // (w_row * w_col) * x, the order of weights * slices in convolve.py:89-90
           v[q] = ADJ ? t : mkc<T>((wr0 * wc[q]) * t.x, (wr1 * wc[q]) * t.y);
         } else {
@@ -946,6 +958,9 @@ int launch_one(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
     a.aux_bytes = f.aux ? f.aux_bytes : 0;
     a.aux_chunk = grid > 0 ? ((a.aux_bytes + grid - 1) / grid + 15) & ~(int64_t)15 : 0;
     a.zero_out = f.zero_out ? 1 : 0;
+    a.in_rs = f.in_rs > 0 ? f.in_rs : (int64_t)g.ny;
+    a.in_ps = f.in_ps > 0 ? f.in_ps : g.pixels();
+    a.in_exp = f.in_exp ? 1 : 0;
   }
   if (units <= 0) return JUBIK_OK;
   if (units > 0x7fffffffLL) {

@@ -86,6 +86,10 @@ struct FusedLaunch {
   int64_t aux_bytes = 0;
   bool zero_out = true; // module-shared adjoint: the per-unit kernel clears `out` first
   bool pdl = true;      // launch with programmatic stream serialisation
+  // forward input as a crop of a larger (E', N0', N1') array: row and plane
+  // strides (0 = the field's own), and whether it holds log-sky values
+  int64_t in_rs = 0, in_ps = 0;
+  bool in_exp = false;
 };
 size_t fused_spec_bytes(const Geom& g, int dtype);
 enum FusedStage {

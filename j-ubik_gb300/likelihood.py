@@ -156,6 +156,17 @@ class ResponsePoissonian:
         from .autograd import PoissonEnergyFn
         return PoissonEnergyFn.apply(x, self.response.plan)
 
+    def energy_and_gradient_logsky(self, s):
+        """Energy and dE/ds for the sky exp(s[:E, :nx, :ny]) of a padded log-sky
+        (the exp_padding of ``jubik/sky_models.py:340-341``), exp and crop fused
+        into the response's first kernel."""
+        return self.response.plan.energy_and_grad_logsky(s)
+
+    def energy_autograd_logsky(self, s: torch.Tensor) -> torch.Tensor:
+        """Differentiable energy of a padded log-sky s (for a torch sky model)."""
+        from .autograd import LogSkyPoissonEnergyFn
+        return LogSkyPoissonEnergyFn.apply(s, self.response.plan)
+
 
 class ModelPoissonian:
     """``Poissonian(d).amend(f)`` for an arbitrary differentiable torch model."""

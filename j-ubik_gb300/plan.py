@@ -270,6 +270,27 @@ class ResponsePlan:
                   ptr(grad if need_grad else None), self._s())
         return energy, (grad if need_grad else None)
 
+    def energy_and_grad_logsky(self, s, need_grad: bool = True,
+                               energy: Optional[torch.Tensor] = None,
+                               grad: Optional[torch.Tensor] = None):
+        """Poisson energy and gradient for the sky exp(s[:E, :nx, :ny]) of a
+        (possibly padded) log-sky array s (``sky_models.py:340-341``): the exp
+        and the crop run inside the response's first kernel.  Returns the energy
+        (float64 0-d) and dE/ds (shape of s, zero outside the crop)."""
+        t = as_device(s, self.dtype, self.device)
+        if t.dim() == 2:
+            t = t.unsqueeze(0)
+        if t.dim() != 3:
+            raise ValueError("log-sky must have shape (E', nx', ny')")
+        ep, n0, n1 = (int(v) for v in t.shape)
+        if energy is None:
+            energy = torch.empty((), dtype=torch.float64, device=self.device)
+        if need_grad and grad is None:
+            grad = torch.empty_like(t)
+        _lib.call("jubik_poisson_energy_grad_logsky", self._h, ptr(t), ep, n0, n1, ptr(energy),
+                  ptr(grad if need_grad else None), self._s())
+        return energy, (grad if need_grad else None)
+
     def metric(self, x, v, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         """R^T diag(1/lam) R v with lam = R(x); x=None reuses the last lam."""
         xx = None if x is None else self._sky(x)
