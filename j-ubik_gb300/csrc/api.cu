@@ -7,6 +7,8 @@
 #include <new>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "internal.h"
 #include "jubik_common.cuh"
 
@@ -281,6 +283,13 @@ namespace {
 
 inline cudaStream_t S(void* s) { return (cudaStream_t)s; }
 
+// NVTX range named after the entry point (visible in Nsight timelines; a
+// no-op unless a tool is attached)
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
+
 // Brackets one kernel phase with events when the plan profiles.
 struct Phase {
   jubik_plan* p;
@@ -456,6 +465,7 @@ int jubik_fused_supported(int32_t P, int32_t dtype) { return fused_supported(P, 
 int jubik_fft_length_supported(int32_t L) { return fft_length_supported(L) ? 1 : 0; }
 
 int jubik_plan_create(const jubik_plan_desc* d, jubik_plan** out) {
+  NvtxRange nvtx_("jubik_plan_create");
   if (!d || !out) {
     set_error("NULL argument");
     return JUBIK_ERR_INVALID_ARGUMENT;
@@ -653,6 +663,7 @@ int jubik_plan_profile(const jubik_plan* p, double* ms, int64_t* launches) {
 
 int jubik_plan_set_psf(jubik_plan* p, const void* psf, int32_t layout, int32_t e_broadcast,
                        void* stream) {
+  NvtxRange nvtx_("jubik_plan_set_psf");
   JUBIK_TRY(check_plan(p));
   if (!psf || (layout != JUBIK_PSF_PRECUT && layout != JUBIK_PSF_FULL)) {
     set_error("psf must be non-NULL with a valid layout");
@@ -699,6 +710,7 @@ int jubik_plan_set_psf(jubik_plan* p, const void* psf, int32_t layout, int32_t e
 
 int jubik_plan_set_exposure(jubik_plan* p, const void* exposure, const uint8_t* readmask,
                             void* stream) {
+  NvtxRange nvtx_("jubik_plan_set_exposure");
   JUBIK_TRY(check_plan(p));
   cudaStream_t s = S(stream);
   const Geom& g = p->g;
@@ -770,6 +782,7 @@ int jubik_plan_readout_index(const jubik_plan* p, const int64_t** device_index) 
 }
 
 int jubik_plan_set_data(jubik_plan* p, const int32_t* counts, void* stream) {
+  NvtxRange nvtx_("jubik_plan_set_data");
   JUBIK_TRY(check_plan(p));
   if (!counts) {
     set_error("counts is NULL");
@@ -785,18 +798,21 @@ int jubik_plan_set_data(jubik_plan* p, const int32_t* counts, void* stream) {
 }
 
 int jubik_psf_forward(jubik_plan* p, const void* x, void* out, void* stream) {
+  NvtxRange nvtx_("jubik_psf_forward");
   JUBIK_TRY(check_plan(p));
   JUBIK_TRY(need(p->psf_set, "PSF"));
   return do_forward(p, x, out, 1.0, S(stream));
 }
 
 int jubik_psf_adjoint(jubik_plan* p, const void* cot, void* out_x, void* stream) {
+  NvtxRange nvtx_("jubik_psf_adjoint");
   JUBIK_TRY(check_plan(p));
   JUBIK_TRY(need(p->psf_set, "PSF"));
   return do_adjoint(p, cot, out_x, 1.0, S(stream));
 }
 
 int jubik_response_forward(jubik_plan* p, const void* x, void* out_readout, void* stream) {
+  NvtxRange nvtx_("jubik_response_forward");
   JUBIK_TRY(check_plan(p));
   JUBIK_TRY(need(p->psf_set, "PSF"));
   cudaStream_t s = S(stream);
@@ -808,10 +824,12 @@ int jubik_response_forward(jubik_plan* p, const void* x, void* out_readout, void
 }
 
 int jubik_response_jvp(jubik_plan* p, const void* t, void* out_readout, void* stream) {
+  NvtxRange nvtx_("jubik_response_jvp");
   return jubik_response_forward(p, t, out_readout, stream);
 }
 
 int jubik_response_vjp(jubik_plan* p, const void* cot_readout, void* out_x, void* stream) {
+  NvtxRange nvtx_("jubik_response_vjp");
   JUBIK_TRY(check_plan(p));
   JUBIK_TRY(need(p->psf_set, "PSF"));
   cudaStream_t s = S(stream);
@@ -829,6 +847,7 @@ int jubik_response_vjp(jubik_plan* p, const void* cot_readout, void* out_x, void
 
 int jubik_poisson_energy_grad(jubik_plan* p, const void* x, double* energy, void* grad_x,
                               void* stream) {
+  NvtxRange nvtx_("jubik_poisson_energy_grad");
   JUBIK_TRY(check_plan(p));
   JUBIK_TRY(need(p->psf_set, "PSF"));
   JUBIK_TRY(need(p->data_set, "data"));
@@ -855,6 +874,7 @@ int jubik_poisson_energy_grad(jubik_plan* p, const void* x, double* energy, void
 int jubik_poisson_energy_grad_logsky(jubik_plan* p, const void* s_log, int32_t e_pad,
                                      int32_t nx_pad, int32_t ny_pad, double* energy,
                                      void* grad_s, void* stream) {
+  NvtxRange nvtx_("jubik_poisson_energy_grad_logsky");
   JUBIK_TRY(check_plan(p));
   JUBIK_TRY(need(p->psf_set, "PSF"));
   JUBIK_TRY(need(p->data_set, "data"));
@@ -900,6 +920,7 @@ int jubik_poisson_energy_grad_logsky(jubik_plan* p, const void* s_log, int32_t e
 }
 
 int jubik_metric_apply(jubik_plan* p, const void* x, const void* v, void* out, void* stream) {
+  NvtxRange nvtx_("jubik_metric_apply");
   JUBIK_TRY(check_plan(p));
   JUBIK_TRY(need(p->psf_set, "PSF"));
   cudaStream_t s = S(stream);
@@ -933,6 +954,7 @@ int jubik_metric_apply(jubik_plan* p, const void* x, const void* v, void* out, v
 
 int jubik_poisson_energy(const void* lam, const int32_t* data, int64_t n, int32_t dtype,
                          double* energy, void* grad, void* stream) {
+  NvtxRange nvtx_("jubik_poisson_energy");
   if (!lam || !data || !energy || n < 0) {
     set_error("invalid argument");
     return JUBIK_ERR_INVALID_ARGUMENT;
@@ -992,6 +1014,7 @@ int jubik_slice_patches_adjoint(const void* patches, int64_t batch, int32_t nx, 
 
 int jubik_convolve2d(const void* kernel, int64_t bk, const void* signal, int64_t bs, int32_t h,
                      int32_t w, double dvol, int32_t dtype, void* out, void* stream) {
+  NvtxRange nvtx_("jubik_convolve2d");
   if (!kernel || !signal || !out || bk < 1 || bs < 1 || h < 1 || w < 1 || bs % bk != 0) {
     set_error("convolve2d: invalid shapes (kernel batch must divide the signal batch)");
     return JUBIK_ERR_INVALID_ARGUMENT;

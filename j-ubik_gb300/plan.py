@@ -9,6 +9,7 @@ All arrays are PyTorch CUDA tensors; the library only sees raw pointers.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from typing import Optional, Sequence
 
 import numpy as np
@@ -64,7 +65,8 @@ class ResponsePlan:
     (``jubik/convolve.py:66``).  ``path`` picks the fused path ("auto"/"fused":
     patch spectra shared across modules when there are several), the fused path
     with one kernel per unit and no sharing ("fused_unit"), or the unfused one
-    ("plain").
+    ("plain").  With ``path="auto"`` the environment variable ``JUBIK_PATH``
+    (one of the path names) overrides the automatic choice, for debugging.
     """
 
     def __init__(self, n_modules: int, n_energies: int, shape: Sequence[int], n_patches: int,
@@ -72,6 +74,10 @@ class ResponsePlan:
                  pixel_area: float = 1.0, device: Optional[torch.device] = None):
         self.device = device if device is not None else require_cuda()
         self.dtype = dtype
+        if path == "auto":  # debugging override of the automatic choice
+            path = os.environ.get("JUBIK_PATH", "auto")
+        if path not in _PATHS:
+            raise ValueError(f"path must be one of {sorted(_PATHS)}, got {path!r}")
         self.n_modules, self.n_energies = int(n_modules), int(n_energies)
         self.shape = (int(shape[0]), int(shape[1]))
         self.n_patches, self.margin = int(n_patches), int(margin)

@@ -399,3 +399,37 @@ def test_large_field_adjoint_identity(cuda):
     assert rel(p32.psf_adjoint(y.float()), b64.cpu().numpy()) < 1e-6
     p64.close()
     p32.close()
+
+
+def test_non_finite_sky_propagates_without_fault(cuda):
+    """NaN or Inf in the sky gives a non-finite energy and gradient, raises no
+    CUDA error, and leaves the plan usable for the next finite call."""
+    nx, dx, m, M, E = 64, 16, 8, 2, 1
+    inst = synthetic.config2(nx=nx, dx=dx, margin=m, n_modules=M, n_energies=E)
+    plan = ju.ResponsePlan(M, E, (nx, nx), nx // dx, m, dtype=torch.float32).set_psf(inst.psf)
+    plan.set_exposure(inst.exposure, inst.readmask)
+    lam = plan.response(inst.sky).double().cpu().numpy()
+    plan.set_data(synthetic.poisson_data(lam, 3))
+    e0, g0 = plan.energy_and_grad(inst.sky)
+    e0, g0 = float(e0), g0.clone()
+    for bad in (np.nan, np.inf):
+        x = inst.sky.copy()
+        x[0, 10, 10] = bad
+        e, g = plan.energy_and_grad(x)
+        torch.cuda.synchronize()
+        assert not np.isfinite(float(e))
+        assert not bool(torch.isfinite(g).all())
+    e1, g1 = plan.energy_and_grad(inst.sky)
+    assert abs(float(e1) - e0) <= 1e-9 * abs(e0)
+    assert rel(g1, g0.double().cpu().numpy()) < 1e-5
+    plan.close()
+
+
+def test_path_override_from_environment(cuda, monkeypatch):
+    monkeypatch.setenv("JUBIK_PATH", "plain")
+    plan = ju.ResponsePlan(1, 1, (64, 64), 4, 8, dtype=torch.float32)
+    assert plan.path == "plain"
+    plan.close()
+    monkeypatch.setenv("JUBIK_PATH", "bogus")
+    with pytest.raises(ValueError):
+        ju.ResponsePlan(1, 1, (64, 64), 4, 8, dtype=torch.float32)
