@@ -376,17 +376,17 @@ int do_forward(jubik_plan* p, const void* x, void* out, double scale, cudaStream
   }
   Phase ph(p, 0, s);
   const bool f32 = p->dtype == JUBIK_F32;
-  const int64_t n2p = (int64_t)g.n * g.n;
   JUBIK_TRY(f32 ? plain_sky_patches<float>(g, x, p->wt, p->zs, s)
                 : plain_sky_patches<double>(g, x, p->wt, p->zs, s));
-  JUBIK_TRY(f32 ? fft2_batched<float>(p->fft, p->fft, p->zs, g.E * n2p, false, s)
-                : fft2_batched<double>(p->fft, p->fft, p->zs, g.E * n2p, false, s));
+  JUBIK_TRY(f32 ? fft2_batched<float>(p->fft, p->fft, p->zs, plain_pairs(g), false, s)
+                : fft2_batched<double>(p->fft, p->fft, p->zs, plain_pairs(g), false, s));
   for (int m0 = 0; m0 < g.M; m0 += p->zu_modules) {
     const int nm = std::min(p->zu_modules, g.M - m0);
     JUBIK_TRY(f32 ? plain_mul_modules<float>(g, p->zs, p->hfull, m0, nm, p->zu, s)
                   : plain_mul_modules<double>(g, p->zs, p->hfull, m0, nm, p->zu, s));
-    JUBIK_TRY(f32 ? fft2_batched<float>(p->fft, p->fft, p->zu, (int64_t)nm * g.E * n2p, true, s)
-                  : fft2_batched<double>(p->fft, p->fft, p->zu, (int64_t)nm * g.E * n2p, true, s));
+    const int64_t batch = (int64_t)nm * plain_pairs(g);
+    JUBIK_TRY(f32 ? fft2_batched<float>(p->fft, p->fft, p->zu, batch, true, s)
+                  : fft2_batched<double>(p->fft, p->fft, p->zu, batch, true, s));
     JUBIK_TRY(f32 ? plain_overlap_gather<float>(g, p->zu, m0, nm, scale, out, s)
                   : plain_overlap_gather<double>(g, p->zu, m0, nm, scale, out, s));
   }
@@ -427,19 +427,18 @@ int do_adjoint(jubik_plan* p, const void* cot, void* out_x, double scale, cudaSt
   }
   Phase ph(p, 1, s);
   const bool f32 = p->dtype == JUBIK_F32;
-  const int64_t n2p = (int64_t)g.n * g.n;
   for (int m0 = 0; m0 < g.M; m0 += p->zu_modules) {
     const int nm = std::min(p->zu_modules, g.M - m0);
     JUBIK_TRY(f32 ? plain_cot_patches<float>(g, cot, m0, nm, p->zu, s)
                   : plain_cot_patches<double>(g, cot, m0, nm, p->zu, s));
-    JUBIK_TRY(f32 ? fft2_batched<float>(p->fft, p->fft, p->zu, (int64_t)nm * g.E * n2p, false, s)
-                  : fft2_batched<double>(p->fft, p->fft, p->zu, (int64_t)nm * g.E * n2p, false,
-                                         s));
+    const int64_t batch = (int64_t)nm * plain_pairs(g);
+    JUBIK_TRY(f32 ? fft2_batched<float>(p->fft, p->fft, p->zu, batch, false, s)
+                  : fft2_batched<double>(p->fft, p->fft, p->zu, batch, false, s));
     JUBIK_TRY(f32 ? plain_mulconj_accum<float>(g, p->zu, p->hfull, m0, nm, m0 == 0, p->zs, s)
                   : plain_mulconj_accum<double>(g, p->zu, p->hfull, m0, nm, m0 == 0, p->zs, s));
   }
-  JUBIK_TRY(f32 ? fft2_batched<float>(p->fft, p->fft, p->zs, g.E * n2p, true, s)
-                : fft2_batched<double>(p->fft, p->fft, p->zs, g.E * n2p, true, s));
+  JUBIK_TRY(f32 ? fft2_batched<float>(p->fft, p->fft, p->zs, plain_pairs(g), true, s)
+                : fft2_batched<double>(p->fft, p->fft, p->zs, plain_pairs(g), true, s));
   return f32 ? plain_grad_gather<float>(g, p->zs, p->wt, scale, out_x, s)
              : plain_grad_gather<double>(g, p->zs, p->wt, scale, out_x, s);
 }
@@ -576,10 +575,9 @@ int jubik_plan_create(const jubik_plan_desc* d, jubik_plan** out) {
       return fail(st);
   } else {
     if ((st = p->alloc(&p->hfull, (size_t)units * g.P * g.P * csz))) return fail(st);
-    const int64_t n2p = (int64_t)g.n * g.n;
-    if ((st = p->alloc(&p->zs, (size_t)g.E * n2p * g.P * g.P * csz))) return fail(st);
+    if ((st = p->alloc(&p->zs, (size_t)plain_pairs(g) * g.P * g.P * csz))) return fail(st);
     // bound the per-chunk unit buffer to ~2 GiB
-    const size_t per_module = (size_t)g.E * n2p * g.P * g.P * csz;
+    const size_t per_module = (size_t)plain_pairs(g) * g.P * g.P * csz;
     p->zu_modules = (int)std::max<size_t>(1, std::min<size_t>(g.M, (2ull << 30) / per_module));
     if ((st = p->alloc(&p->zu, per_module * p->zu_modules))) return fail(st);
   }

@@ -34,6 +34,9 @@ struct Geom {
   int64_t units() const { return (int64_t)M * E * n * n; }
   int64_t pixels() const { return (int64_t)nx * ny; }
 };
+// unfused path: real patches are transformed two per complex array
+inline int64_t plain_pairs(const Geom& g) { return ((int64_t)g.E * g.n * g.n + 1) / 2; }
+
 
 // ------------------------------------------------------------------ plain FFT
 constexpr int kMaxStages = 24;

@@ -117,26 +117,43 @@ __global__ void k_spectra_store(const double2* __restrict__ buf, int P, int64_t 
 }
 
 // --------------------------------------------------------------- plain path
+// Real patches travel two per complex transform: patch p = e n^2 + k is the
+// real part (p even) or the imaginary part (p odd) of pair p / 2.  With
+// Z = FFT(a + i b), A = (Z(k) + conj Z(-k)) / 2 and i B = (Z(k) - conj Z(-k)) / 2
+// are the spectra of the two real patches; products with the (Hermitian) PSF
+// spectra stay Hermitian, so one inverse transform of A Ha + i B Hb returns
+// both real results as its real and imaginary parts.
+__device__ __forceinline__ int64_t mirror_index(int64_t rem, int P) {
+  const int ky = (int)(rem / P), kx = (int)(rem - (int64_t)ky * P);
+  return (int64_t)((P - ky) % P) * P + (P - kx) % P;
+}
+
 template <typename T>
 __global__ void k_plain_sky_patches(const T* __restrict__ x, const T* __restrict__ wt, int E,
                                     int n, int nx, int ny, int dx, int margin, int half,
                                     int sr_max, int sc_max, int P, cx<T>* __restrict__ zs) {
   const int n2p = n * n;
-  const int64_t total = (int64_t)E * n2p * P * P;
+  const int np = E * n2p, nph = (np + 1) / 2;
+  const int64_t total = (int64_t)nph * P * P;
   const int K = 2 * dx;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t ek = i / ((int64_t)P * P);
-    const int rem = (int)(i - ek * P * P);
+    const int64_t j = i / ((int64_t)P * P);
+    const int rem = (int)(i - j * P * P);
     const int y = rem / P, xx = rem % P;
-    const int k = (int)(ek % n2p), e = (int)(ek / n2p);
-    const int rb = img_row_base(k % n, dx, sr_max, half, margin);
-    const int cb = img_row_base(k / n, dx, sc_max, half, margin);
-    const int ya = y - margin, xa = xx - margin, row = rb + y, col = cb + xx;
-    T v = (T)0;
-    if (ya >= 0 && ya < K && xa >= 0 && xa < K && row >= 0 && row < nx && col >= 0 && col < ny)
-      v = (wt[ya] * wt[xa]) * x[((int64_t)e * nx + row) * ny + col];
-    zs[i] = mkc<T>(v, (T)0);
+    T v[2] = {(T)0, (T)0};
+    for (int part = 0; part < 2; ++part) {
+      const int p = (int)(2 * j + part);
+      if (p >= np) break;
+      const int k = p % n2p, e = p / n2p;
+      const int rb = img_row_base(k % n, dx, sr_max, half, margin);
+      const int cb = img_row_base(k / n, dx, sc_max, half, margin);
+      const int ya = y - margin, xa = xx - margin, row = rb + y, col = cb + xx;
+      if (ya >= 0 && ya < K && xa >= 0 && xa < K && row >= 0 && row < nx && col >= 0 &&
+          col < ny)
+        v[part] = (wt[ya] * wt[xa]) * x[((int64_t)e * nx + row) * ny + col];
+    }
+    zs[i] = mkc<T>(v[0], v[1]);
   }
 }
 
@@ -145,17 +162,25 @@ __global__ void k_plain_mul_modules(const cx<T>* __restrict__ zs, const cx<T>* _
                                     int m0, int nm, int E, int n2p, int P,
                                     cx<T>* __restrict__ zu) {
   const int64_t pp = (int64_t)P * P;
-  const int64_t total = (int64_t)nm * E * n2p * pp;
+  const int np = E * n2p, nph = (np + 1) / 2;
+  const int64_t total = (int64_t)nm * nph * pp;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t unit = i / pp;
-    const int64_t rem = i - unit * pp;
-    const int k = (int)(unit % n2p);
-    const int64_t me = unit / n2p;
-    const int e = (int)(me % E);
-    const int m = m0 + (int)(me / E);
-    const int64_t hu = ((int64_t)m * n2p + k) * E + e;
-    zu[i] = cmul<T>(zs[((int64_t)e * n2p + k) * pp + rem], hfull[hu * pp + rem]);
+    const int64_t up = i / pp;
+    const int64_t rem = i - up * pp;
+    const int64_t j = up % nph;
+    const int m = m0 + (int)(up / nph);
+    const cx<T> z = zs[j * pp + rem], zm = cconj<T>(zs[j * pp + mirror_index(rem, P)]);
+    const cx<T> a = cscale<T>(cadd<T>(z, zm), (T)0.5);   // spectrum of patch 2j
+    const cx<T> ib = cscale<T>(csub<T>(z, zm), (T)0.5);  // i x spectrum of patch 2j + 1
+    const int pa = (int)(2 * j), pb = pa + 1;
+    const int64_t ha = ((int64_t)m * n2p + pa % n2p) * E + pa / n2p;
+    cx<T> w = cmul<T>(a, hfull[ha * pp + rem]);
+    if (pb < np) {
+      const int64_t hb = ((int64_t)m * n2p + pb % n2p) * E + pb / n2p;
+      w = cadd<T>(w, cmul<T>(ib, hfull[hb * pp + rem]));
+    }
+    zu[i] = w;
   }
 }
 
@@ -168,6 +193,7 @@ __global__ void k_plain_overlap_gather(const cx<T>* __restrict__ zu, int m0, int
                                        int sr_max, int sc_max, int P, T scale,
                                        T* __restrict__ out) {
   const int n2p = n * n;
+  const int nph = (E * n2p + 1) / 2;
   const int64_t pp = (int64_t)P * P;
   const int64_t total = (int64_t)nm * E * nx * ny;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
@@ -176,6 +202,8 @@ __global__ void k_plain_overlap_gather(const cx<T>* __restrict__ zu, int m0, int
     const int64_t t = i / ny;
     const int r = (int)(t % nx);
     const int64_t me = t / nx;  // (m - m0) * E + e
+    const int64_t mm = me / E;
+    const int e = (int)(me % E);
     const int tr = r + half + margin, tc = c + half + margin;
     const int ri_hi = min(n - 1, tr / dx), ci_hi = min(n - 1, tc / dx);
     const int ri_lo = tr - P + 1 <= 0 ? 0 : (tr - P + 1 + dx - 1) / dx;
@@ -186,7 +214,9 @@ __global__ void k_plain_overlap_gather(const cx<T>* __restrict__ zu, int m0, int
       const int cb = img_row_base(pj, dx, sc_max, half, margin);
       const int y = r - rb, xx = c - cb;
       if (y < 0 || y >= P || xx < 0 || xx >= P) return;
-      const T v = zu[(me * n2p + (int64_t)pj * n + pi) * pp + (int64_t)y * P + xx].x;
+      const int p = e * n2p + pj * n + pi;
+      const cx<T> z = zu[(mm * nph + (p >> 1)) * pp + (int64_t)y * P + xx];
+      const T v = (p & 1) ? z.y : z.x;
       const T yk = v - comp;
       const T tt = s + yk;
       comp = (tt - s) - yk;
@@ -200,8 +230,7 @@ __global__ void k_plain_overlap_gather(const cx<T>* __restrict__ zu, int m0, int
       for (int pi = ri_lo; pi <= ri_hi; ++pi) visit(pi, n - 1);
       if (ri_hi < n - 1) visit(n - 1, n - 1);
     }
-    const int64_t m = m0 + me / E;
-    const int e = (int)(me % E);
+    const int64_t m = m0 + mm;
     out[((m * E + e) * nx + r) * (int64_t)ny + c] = scale * s;
   }
 }
@@ -211,25 +240,28 @@ __global__ void k_plain_cot_patches(const T* __restrict__ cot, int m0, int nm, i
                                     int nx, int ny, int dx, int margin, int half, int sr_max,
                                     int sc_max, int P, cx<T>* __restrict__ zu) {
   const int n2p = n * n;
+  const int np = E * n2p, nph = (np + 1) / 2;
   const int64_t pp = (int64_t)P * P;
-  const int64_t total = (int64_t)nm * E * n2p * pp;
+  const int64_t total = (int64_t)nm * nph * pp;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t unit = i / pp;
-    const int rem = (int)(i - unit * pp);
+    const int64_t up = i / pp;
+    const int rem = (int)(i - up * pp);
     const int y = rem / P, xx = rem % P;
-    const int k = (int)(unit % n2p);
-    const int64_t me = unit / n2p;
-    const int rb = img_row_base(k % n, dx, sr_max, half, margin);
-    const int cb = img_row_base(k / n, dx, sc_max, half, margin);
-    const int row = rb + y, col = cb + xx;
-    T v = (T)0;
-    if (row >= 0 && row < nx && col >= 0 && col < ny) {
-      const int64_t m = m0 + me / E;
-      const int e = (int)(me % E);
-      v = cot[((m * E + e) * nx + row) * (int64_t)ny + col];
+    const int64_t j = up % nph;
+    const int64_t m = m0 + up / nph;
+    T v[2] = {(T)0, (T)0};
+    for (int part = 0; part < 2; ++part) {
+      const int p = (int)(2 * j + part);
+      if (p >= np) break;
+      const int k = p % n2p, e = p / n2p;
+      const int rb = img_row_base(k % n, dx, sr_max, half, margin);
+      const int cb = img_row_base(k / n, dx, sc_max, half, margin);
+      const int row = rb + y, col = cb + xx;
+      if (row >= 0 && row < nx && col >= 0 && col < ny)
+        v[part] = cot[((m * E + e) * nx + row) * (int64_t)ny + col];
     }
-    zu[i] = mkc<T>(v, (T)0);
+    zu[i] = mkc<T>(v[0], v[1]);
   }
 }
 
@@ -238,17 +270,26 @@ __global__ void k_plain_mulconj_accum(const cx<T>* __restrict__ zu, const cx<T>*
                                       int m0, int nm, int E, int n2p, int P, int first,
                                       cx<T>* __restrict__ zs) {
   const int64_t pp = (int64_t)P * P;
-  const int64_t total = (int64_t)E * n2p * pp;
+  const int np = E * n2p, nph = (np + 1) / 2;
+  const int64_t total = (int64_t)nph * pp;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t ek = i / pp;
-    const int64_t rem = i - ek * pp;
-    const int k = (int)(ek % n2p), e = (int)(ek / n2p);
+    const int64_t j = i / pp;
+    const int64_t rem = i - j * pp;
+    const int64_t mrem = mirror_index(rem, P);
+    const int pa = (int)(2 * j), pb = pa + 1;
     cx<T> acc = first ? mkc<T>((T)0, (T)0) : zs[i];
     for (int mm = 0; mm < nm; ++mm) {
-      const int64_t hu = ((int64_t)(m0 + mm) * n2p + k) * E + e;
-      const cx<T> z = zu[(((int64_t)mm * E + e) * n2p + k) * pp + rem];
-      acc = cadd<T>(acc, cmulc<T>(z, hfull[hu * pp + rem]));
+      const int64_t base = ((int64_t)mm * nph + j) * pp;
+      const cx<T> z = zu[base + rem], zm = cconj<T>(zu[base + mrem]);
+      const cx<T> a = cscale<T>(cadd<T>(z, zm), (T)0.5);
+      const cx<T> ib = cscale<T>(csub<T>(z, zm), (T)0.5);
+      const int64_t ha = ((int64_t)(m0 + mm) * n2p + pa % n2p) * E + pa / n2p;
+      acc = cadd<T>(acc, cmulc<T>(a, hfull[ha * pp + rem]));
+      if (pb < np) {
+        const int64_t hb = ((int64_t)(m0 + mm) * n2p + pb % n2p) * E + pb / n2p;
+        acc = cadd<T>(acc, cmulc<T>(ib, hfull[hb * pp + rem]));
+      }
     }
     zs[i] = acc;
   }
@@ -278,9 +319,9 @@ __global__ void k_plain_grad_gather(const cx<T>* __restrict__ zs, const T* __res
       const int cb = img_row_base(pj, dx, sc_max, half, margin);
       const int ya = r - rb - margin, xa = c - cb - margin;
       if (ya < 0 || ya >= K || xa < 0 || xa >= K) return;
-      const T v = (wt[ya] * wt[xa]) *
-                  zs[((int64_t)e * n2p + (int64_t)pj * n + pi) * pp +
-                     (int64_t)(ya + margin) * P + (xa + margin)].x;
+      const int p = e * n2p + pj * n + pi;
+      const cx<T> z = zs[(int64_t)(p >> 1) * pp + (int64_t)(ya + margin) * P + (xa + margin)];
+      const T v = (wt[ya] * wt[xa]) * ((p & 1) ? z.y : z.x);
       const T yk = v - comp;
       const T tt = s + yk;
       comp = (tt - s) - yk;
@@ -620,7 +661,7 @@ int spectra_store(const Geom& g, const void* buf, int64_t u0, int64_t nu, void* 
 
 template <typename T>
 int plain_sky_patches(const Geom& g, const void* x, const void* wt, void* zs, cudaStream_t s) {
-  const int64_t total = (int64_t)g.E * g.n * g.n * g.P * g.P;
+  const int64_t total = plain_pairs(g) * g.P * g.P;
   k_plain_sky_patches<T><<<grid_for(total), kBlock, 0, s>>>(
       (const T*)x, (const T*)wt, g.E, g.n, g.nx, g.ny, g.dx, g.margin, g.half, g.sr_max, g.sc_max,
       g.P, (cx<T>*)zs);
@@ -630,7 +671,7 @@ int plain_sky_patches(const Geom& g, const void* x, const void* wt, void* zs, cu
 template <typename T>
 int plain_mul_modules(const Geom& g, const void* zs, const void* hfull, int m0, int nm, void* zu,
                       cudaStream_t s) {
-  const int64_t total = (int64_t)nm * g.E * g.n * g.n * g.P * g.P;
+  const int64_t total = (int64_t)nm * plain_pairs(g) * g.P * g.P;
   k_plain_mul_modules<T><<<grid_for(total), kBlock, 0, s>>>(
       (const cx<T>*)zs, (const cx<T>*)hfull, m0, nm, g.E, g.n * g.n, g.P, (cx<T>*)zu);
   return cuda_status(cudaGetLastError(), "k_plain_mul_modules");
@@ -648,7 +689,7 @@ int plain_overlap_gather(const Geom& g, const void* zu, int m0, int nm, double s
 
 template <typename T>
 int plain_cot_patches(const Geom& g, const void* cot, int m0, int nm, void* zu, cudaStream_t s) {
-  const int64_t total = (int64_t)nm * g.E * g.n * g.n * g.P * g.P;
+  const int64_t total = (int64_t)nm * plain_pairs(g) * g.P * g.P;
   k_plain_cot_patches<T><<<grid_for(total), kBlock, 0, s>>>(
       (const T*)cot, m0, nm, g.E, g.n, g.nx, g.ny, g.dx, g.margin, g.half, g.sr_max, g.sc_max,
       g.P, (cx<T>*)zu);
@@ -658,7 +699,7 @@ int plain_cot_patches(const Geom& g, const void* cot, int m0, int nm, void* zu, 
 template <typename T>
 int plain_mulconj_accum(const Geom& g, const void* zu, const void* hfull, int m0, int nm,
                         bool first, void* zs, cudaStream_t s) {
-  const int64_t total = (int64_t)g.E * g.n * g.n * g.P * g.P;
+  const int64_t total = plain_pairs(g) * g.P * g.P;
   k_plain_mulconj_accum<T><<<grid_for(total), kBlock, 0, s>>>(
       (const cx<T>*)zu, (const cx<T>*)hfull, m0, nm, g.E, g.n * g.n, g.P, first ? 1 : 0,
       (cx<T>*)zs);
