@@ -240,3 +240,29 @@ def test_benchmark_workload_properties(cuda, bench_case):
     finally:
         p32.close()
         p64.close()
+
+
+# --------------------------- the demo geometries beyond the fused tile (P = 320)
+@pytest.mark.parametrize("dtype", [F64, F32], ids=["f64", "f32"])
+def test_chandra_demo_geometry_unfused(cuda, dtype):
+    """512^2 field, 4 x 4 patches (stride 128), margin ceil(0.062 * 512) = 32:
+    P = 320 (demos/configs/chandra_demo.yaml:13,44-45 with the margin rule of
+    erosita_response.py:207), beyond the fused kernels' shared-memory tile, so
+    the unfused path runs."""
+    nx, dx, m, M, E = 512, 128, 32, 1, 2
+    inst = synthetic.config2(nx=nx, dx=dx, margin=m, n_modules=M, n_energies=E)
+    dom = O.Domain((E, nx, nx), (1.0, 1.0, 1.0))
+    R = O.Response(dom, inst.psf, nx // dx, m, inst.exposure, inst.readmask)
+    lam = R(inst.sky)
+    data = [synthetic.poisson_data(lam[0], 5)]
+    e_ref, g_ref = R.energy_and_grad(inst.sky, data)
+    plan = make_plan(inst, dtype)
+    assert plan.path == "plain" and plan.P == 320
+    plan.set_data(data[0])
+    tol = 1e-12 if dtype == F64 else 1e-6
+    assert rel(plan.response(inst.sky), lam[0]) < tol
+    e, g = plan.energy_and_grad(inst.sky)
+    assert abs(float(e) - e_ref) / abs(e_ref) < tol
+    cancel = R.adjoint([data[0] / lam[0]])
+    assert grad_err(g, g_ref, cancel, dtype) < (1e-11 if dtype == F64 else 3e-6)
+    plan.close()
