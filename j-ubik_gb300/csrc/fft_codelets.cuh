@@ -1,5 +1,5 @@
-// Register-resident small DFTs (sizes 1, 2, 3, 4, 6, 8, 12, 16) in natural
-// order, fully unrolled at compile time.  Composite sizes use one level of
+// Register-resident small DFTs (sizes 1, 2, 3, 4, 5, 6, 8, 10, 12, 16, 20, 24,
+// 32) in natural order, fully unrolled at compile time.  Composite sizes use one level of
 // Cooley-Tukey, N = N1 * N2 with n = N2*n1 + n2 and k = k1 + N1*k2:
 //   X[k1 + N1 k2] = sum_n2 w_N2^(n2 k2) w_N^(n2 k1) sum_n1 x[N2 n1 + n2] w_N1^(n1 k1)
 #pragma once
@@ -57,6 +57,37 @@ template <bool INV, typename T> struct Dft<4, INV, T> {
   }
 };
 
+// 5 points: with t1 = x1 + x4, t2 = x2 + x3, t3 = x1 - x4, t4 = x2 - x3,
+//   X1,4 = x0 + c1 t1 + c2 t2 -/+ i (s1 t3 + s2 t4)
+//   X2,3 = x0 + c2 t1 + c1 t2 -/+ i (s2 t3 - s1 t4)
+// (c_k = cos(2 pi k / 5), s_k = sin(2 pi k / 5); the inverse flips the i terms).
+template <bool INV, typename T> struct Dft<5, INV, T> {
+  __device__ __forceinline__ static void run(cx<T>* v) {
+    constexpr T c1 = (T)0.3090169943749474241022934;   // cos(2 pi / 5)
+    constexpr T c2 = (T)-0.8090169943749474241022934;  // cos(4 pi / 5)
+    constexpr T s1 = (T)0.9510565162951535721164393;   // sin(2 pi / 5)
+    constexpr T s2 = (T)0.5877852522924731291687060;   // sin(4 pi / 5)
+    const cx<T> t1 = cadd<T>(v[1], v[4]), t2 = cadd<T>(v[2], v[3]);
+    const cx<T> t3 = csub<T>(v[1], v[4]), t4 = csub<T>(v[2], v[3]);
+    const cx<T> a1 = mkc<T>(v[0].x + c1 * t1.x + c2 * t2.x, v[0].y + c1 * t1.y + c2 * t2.y);
+    const cx<T> a2 = mkc<T>(v[0].x + c2 * t1.x + c1 * t2.x, v[0].y + c2 * t1.y + c1 * t2.y);
+    const cx<T> b1 = mkc<T>(s1 * t3.x + s2 * t4.x, s1 * t3.y + s2 * t4.y);
+    const cx<T> b2 = mkc<T>(s2 * t3.x - s1 * t4.x, s2 * t3.y - s1 * t4.y);
+    v[0] = cadd<T>(v[0], cadd<T>(t1, t2));
+    if (INV) {
+      v[1] = cadd<T>(a1, cmul_i<T>(b1));
+      v[4] = csub<T>(a1, cmul_i<T>(b1));
+      v[2] = cadd<T>(a2, cmul_i<T>(b2));
+      v[3] = csub<T>(a2, cmul_i<T>(b2));
+    } else {
+      v[1] = csub<T>(a1, cmul_i<T>(b1));
+      v[4] = cadd<T>(a1, cmul_i<T>(b1));
+      v[2] = csub<T>(a2, cmul_i<T>(b2));
+      v[3] = cadd<T>(a2, cmul_i<T>(b2));
+    }
+  }
+};
+
 template <int N1, int N2, bool INV, typename T>
 __device__ __forceinline__ void dft_ct(cx<T>* v) {
   constexpr int N = N1 * N2;
@@ -91,6 +122,18 @@ template <bool INV, typename T> struct Dft<12, INV, T> {
 };
 template <bool INV, typename T> struct Dft<16, INV, T> {
   __device__ __forceinline__ static void run(cx<T>* v) { dft_ct<4, 4, INV, T>(v); }
+};
+template <bool INV, typename T> struct Dft<10, INV, T> {
+  __device__ __forceinline__ static void run(cx<T>* v) { dft_ct<5, 2, INV, T>(v); }
+};
+template <bool INV, typename T> struct Dft<20, INV, T> {
+  __device__ __forceinline__ static void run(cx<T>* v) { dft_ct<4, 5, INV, T>(v); }
+};
+template <bool INV, typename T> struct Dft<24, INV, T> {
+  __device__ __forceinline__ static void run(cx<T>* v) { dft_ct<3, 8, INV, T>(v); }
+};
+template <bool INV, typename T> struct Dft<32, INV, T> {
+  __device__ __forceinline__ static void run(cx<T>* v) { dft_ct<4, 8, INV, T>(v); }
 };
 
 }  // namespace jubik

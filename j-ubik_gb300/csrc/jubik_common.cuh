@@ -85,8 +85,62 @@ __host__ __device__ constexpr double cos48(int j) {
 }
 __host__ __device__ constexpr double sin48(int j) { return cos48(j - 12); }
 
+// cos(2*pi*j/160) for j in [0, 40]: for the codelet sizes that divide 160
+// (5, 10, 20, 32), not 48.
+__host__ __device__ constexpr double cos160_q(int j) {
+  return j == 0    ? 1.0
+         : j == 1  ? 0.9992290362407229347371263
+         : j == 2  ? 0.9969173337331279761977734
+         : j == 3  ? 0.9930684569549262956374372
+         : j == 4  ? 0.9876883405951377261900402
+         : j == 5  ? 0.9807852804032304491261822
+         : j == 6  ? 0.9723699203976766018336458
+         : j == 7  ? 0.9624552364536472876302664
+         : j == 8  ? 0.9510565162951535721164393
+         : j == 9  ? 0.9381913359224841344523397
+         : j == 10 ? 0.9238795325112867561281832
+         : j == 11 ? 0.9081431738250812992580858
+         : j == 12 ? 0.8910065241883678623597096
+         : j == 13 ? 0.8724960070727971145251611
+         : j == 14 ? 0.8526401643540922215193835
+         : j == 15 ? 0.8314696123025452370787884
+         : j == 16 ? 0.8090169943749474241022934
+         : j == 17 ? 0.7853169308807449274703403
+         : j == 18 ? 0.7604059656000309381745944
+         : j == 19 ? 0.7343225094356855356361262
+         : j == 20 ? 0.7071067811865475244008444
+         : j == 21 ? 0.6788007455329417413938556
+         : j == 22 ? 0.6494480483301836557263208
+         : j == 23 ? 0.6190939493098339869415609
+         : j == 24 ? 0.587785252292473129168706
+         : j == 25 ? 0.5555702330196022247428308
+         : j == 26 ? 0.5224985647159488649878979
+         : j == 27 ? 0.4886212414969549474201909
+         : j == 28 ? 0.4539904997395467915604084
+         : j == 29 ? 0.4186597375374280866755652
+         : j == 30 ? 0.38268343236508977172846
+         : j == 31 ? 0.346117057077492976468215
+         : j == 32 ? 0.3090169943749474241022934
+         : j == 33 ? 0.2714404498650742533437874
+         : j == 34 ? 0.2334453638559054117677444
+         : j == 35 ? 0.1950903220161282678482849
+         : j == 36 ? 0.1564344650402308690101053
+         : j == 37 ? 0.1175373974578376441055683
+         : j == 38 ? 0.07845909572784494503296025
+         : j == 39 ? 0.03925981575906860902080336
+                   : 0.0;
+}
+__host__ __device__ constexpr double cos160(int j) {
+  j = ((j % 160) + 160) % 160;
+  if (j <= 40) return cos160_q(j);
+  if (j <= 80) return -cos160_q(80 - j);
+  if (j <= 120) return -cos160_q(j - 80);
+  return cos160_q(160 - j);
+}
+__host__ __device__ constexpr double sin160(int j) { return cos160(j - 40); }
+
 // v * w_N^E with w_N = exp(-2 pi i / N) (forward) or its conjugate (INV).
-// N must divide 48.  Exponents that are multiples of N/4 become sign flips.
+// N must divide 48 or 160.  Exponents that are multiples of N/4 become sign flips.
 template <int N, int E, bool INV, typename T>
 __device__ __forceinline__ cx<T> twc(cx<T> v) {
   constexpr int e = ((E % N) + N) % N;
@@ -98,10 +152,16 @@ __device__ __forceinline__ cx<T> twc(cx<T> v) {
     return INV ? cmul_i<T>(v) : cmul_mi<T>(v);
   } else if constexpr (4 * e == 3 * N) {
     return INV ? cmul_mi<T>(v) : cmul_i<T>(v);
-  } else {
+  } else if constexpr (48 % N == 0) {
     constexpr int j = e * (48 / N);
     constexpr T c = (T)cos48(j);
     constexpr T s = INV ? (T)sin48(j) : (T)(-sin48(j));
+    return mkc<T>(v.x * c - v.y * s, v.x * s + v.y * c);
+  } else {
+    static_assert(160 % N == 0, "twiddle table: N must divide 48 or 160");
+    constexpr int j = e * (160 / N);
+    constexpr T c = (T)cos160(j);
+    constexpr T s = INV ? (T)sin160(j) : (T)(-sin160(j));
     return mkc<T>(v.x * c - v.y * s, v.x * s + v.y * c);
   }
 }

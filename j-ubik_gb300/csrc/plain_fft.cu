@@ -1,5 +1,6 @@
 // Batched complex FFTs of arbitrary supported length (mixed radix 4/2/3 with
-// generic odd radices up to 64), Stockham auto-sort in shared memory.
+// generic odd radices up to 64), Stockham auto-sort in shared memory; lengths
+// 16 L1 with a register codelet for L1 use a two-pass four-step kernel.
 //
 // This is the "plain" transform: it stands in for the jnp.fft.fftn / ifftn
 // calls of jubik/convolve.py:165-174 (complex, full size, unnormalised
@@ -20,6 +21,7 @@ namespace jubik {
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kMaxSeqPerBlock = 64;  // sequences one block transforms (spc <= 64)
 
 template <int R, typename T>
 __device__ __forceinline__ void bfly(const cx<T>* __restrict__ src, cx<T>* __restrict__ dst,
@@ -82,6 +84,13 @@ __global__ void __launch_bounds__(kThreads)
   const int64_t s0 = (int64_t)blockIdx.x * spc;
   const int ns = (int)min((int64_t)spc, nseq - s0);
   const bool seq_fast = (se != 1);
+  // start offset of each of the block's sequences (one 64-bit division per sequence)
+  __shared__ int64_t seq_base[kMaxSeqPerBlock];
+  for (int sq = threadIdx.x; sq < ns; sq += blockDim.x) {
+    const int64_t q = s0 + sq;
+    seq_base[sq] = (q / nb) * sa + (q % nb) * sb;
+  }
+  __syncthreads();
   for (int idx = threadIdx.x; idx < ns * L; idx += blockDim.x) {
     int s, i;
     if (seq_fast) {
@@ -91,8 +100,7 @@ __global__ void __launch_bounds__(kThreads)
       i = idx % L;
       s = idx / L;
     }
-    const int64_t q = s0 + s;
-    b0[s * L + i] = data[(q / nb) * sa + (q % nb) * sb + (int64_t)i * se];
+    b0[s * L + i] = data[seq_base[s] + (int64_t)i * se];
   }
   __syncthreads();
   cx<T>* in = b0;
@@ -129,9 +137,137 @@ __global__ void __launch_bounds__(kThreads)
       i = idx % L;
       s = idx / L;
     }
-    const int64_t q = s0 + s;
     cx<T> v = in[s * L + i];
-    data[(q / nb) * sa + (q % nb) * sb + (int64_t)i * se] = mkc<T>(v.x * scale, v.y * scale);
+    data[seq_base[s] + (int64_t)i * se] = mkc<T>(v.x * scale, v.y * scale);
+  }
+}
+
+// Batched complex FFTs of length L = 16 L1 in two register passes (four-step),
+// x[n1 + L1 n2]:
+//   pass 1, per (sequence, n1): DFT-16 over n2, times w_L^(n1 k2)
+//           -> Y[n1 + Q k2]  (row pitch Q = L1 + 1 or L1 + 2, odd: no bank conflicts)
+//   pass 2, per (sequence, k2): DFT-L1 over n1 -> X[k2 + 16 k1]
+// Each pass is compile-time indexed, against the generic kernel's log_r L
+// passes with run-time radix and index arithmetic.
+template <typename T, int L1, bool INV>
+__global__ void __launch_bounds__(kThreads)
+    k_fft4(cx<T>* __restrict__ data, int64_t nseq, int nb, int64_t sa, int64_t sb, int64_t se,
+           const cx<T>* __restrict__ tw, T scale, int spc) {
+  constexpr int L = 16 * L1;
+  constexpr int Q = (L1 % 2 == 0) ? L1 + 1 : L1 + 2;
+  constexpr int LY = 16 * Q;
+  extern __shared__ unsigned char smem_raw[];
+  cx<T>* bx = reinterpret_cast<cx<T>*>(smem_raw);
+  cx<T>* by = bx + (size_t)spc * L;
+  const int64_t s0 = (int64_t)blockIdx.x * spc;
+  const int ns = (int)min((int64_t)spc, nseq - s0);
+  const bool seq_fast = (se != 1);
+  __shared__ int64_t seq_base[kMaxSeqPerBlock];
+  for (int sq = threadIdx.x; sq < ns; sq += blockDim.x) {
+    const int64_t q = s0 + sq;
+    seq_base[sq] = (q / nb) * sa + (q % nb) * sb;
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < ns * L; idx += blockDim.x) {
+    int sq, i;
+    if (seq_fast) {
+      sq = idx % ns;
+      i = idx / ns;
+    } else {
+      i = idx % L;
+      sq = idx / L;
+    }
+    bx[sq * L + i] = data[seq_base[sq] + (int64_t)i * se];
+  }
+  __syncthreads();
+  for (int it = threadIdx.x; it < ns * L1; it += blockDim.x) {
+    const int sq = it / L1, n1 = it - sq * L1;
+    const cx<T>* src = bx + sq * L + n1;
+    cx<T> v[16];
+#pragma unroll
+    for (int n2 = 0; n2 < 16; ++n2) v[n2] = src[L1 * n2];
+    Dft<16, INV, T>::run(v);
+    cx<T>* dst = by + sq * LY + n1;
+    dst[0] = v[0];
+#pragma unroll
+    for (int k2 = 1; k2 < 16; ++k2) {
+      const cx<T> w = tw[n1 * k2];
+      dst[Q * k2] = INV ? cmulc<T>(v[k2], w) : cmul<T>(v[k2], w);
+    }
+  }
+  __syncthreads();
+  for (int it = threadIdx.x; it < ns * 16; it += blockDim.x) {
+    const int sq = it >> 4, k2 = it & 15;
+    const cx<T>* src = by + sq * LY + Q * k2;
+    cx<T> v[L1];
+#pragma unroll
+    for (int n1 = 0; n1 < L1; ++n1) v[n1] = src[n1];
+    Dft<L1, INV, T>::run(v);
+    cx<T>* dst = bx + sq * L + k2;
+#pragma unroll
+    for (int k1 = 0; k1 < L1; ++k1) dst[16 * k1] = v[k1];
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < ns * L; idx += blockDim.x) {
+    int sq, i;
+    if (seq_fast) {
+      sq = idx % ns;
+      i = idx / ns;
+    } else {
+      i = idx % L;
+      sq = idx / L;
+    }
+    const cx<T> v = bx[sq * L + i];
+    data[seq_base[sq] + (int64_t)i * se] = mkc<T>(v.x * scale, v.y * scale);
+  }
+}
+
+template <typename T, int L1, bool INV>
+int launch_fft4(void* data, int64_t nseq, int nb, int64_t sa, int64_t sb, int64_t se,
+                const cx<T>* tw, double scale, int smax, cudaStream_t s) {
+  constexpr int L = 16 * L1;
+  constexpr int Q = (L1 % 2 == 0) ? L1 + 1 : L1 + 2;
+  const size_t per = sizeof(cx<T>) * (size_t)(L + 16 * Q);
+  // (1 KB of the block's shared memory stays for the static sequence offsets)
+  int spc = (int)std::min<size_t>(16, (size_t)(smax - 1024) / per);
+  if (spc < 1) {
+    set_error("FFT length %d needs %zu bytes of shared memory", L, per);
+    return JUBIK_ERR_UNSUPPORTED;
+  }
+  const size_t smem = per * spc;
+  auto kern = k_fft4<T, L1, INV>;
+  if (smem > 47 * 1024)
+    JUBIK_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+  const int64_t blocks = (nseq + spc - 1) / spc;
+  if (blocks > 0x7fffffffLL) {
+    set_error("too many FFT sequences");
+    return JUBIK_ERR_UNSUPPORTED;
+  }
+  kern<<<(unsigned)blocks, kThreads, smem, s>>>((cx<T>*)data, nseq, nb, sa, sb, se, tw, (T)scale,
+                                                spc);
+  return cuda_status(cudaGetLastError(), "k_fft4 launch");
+}
+
+// lengths 16 L1 with a DFT-L1 codelet take the two-pass kernel; 0 = not covered
+template <typename T, bool INV>
+int try_fft4(int L, void* data, int64_t nseq, int nb, int64_t sa, int64_t sb, int64_t se,
+             const cx<T>* tw, double scale, int smax, cudaStream_t s, bool* done) {
+  *done = true;
+  switch (L) {
+    case 32: return launch_fft4<T, 2, INV>(data, nseq, nb, sa, sb, se, tw, scale, smax, s);
+    case 48: return launch_fft4<T, 3, INV>(data, nseq, nb, sa, sb, se, tw, scale, smax, s);
+    case 64: return launch_fft4<T, 4, INV>(data, nseq, nb, sa, sb, se, tw, scale, smax, s);
+    case 80: return launch_fft4<T, 5, INV>(data, nseq, nb, sa, sb, se, tw, scale, smax, s);
+    case 96: return launch_fft4<T, 6, INV>(data, nseq, nb, sa, sb, se, tw, scale, smax, s);
+    case 128: return launch_fft4<T, 8, INV>(data, nseq, nb, sa, sb, se, tw, scale, smax, s);
+    case 160: return launch_fft4<T, 10, INV>(data, nseq, nb, sa, sb, se, tw, scale, smax, s);
+    case 192: return launch_fft4<T, 12, INV>(data, nseq, nb, sa, sb, se, tw, scale, smax, s);
+    case 256: return launch_fft4<T, 16, INV>(data, nseq, nb, sa, sb, se, tw, scale, smax, s);
+    case 320: return launch_fft4<T, 20, INV>(data, nseq, nb, sa, sb, se, tw, scale, smax, s);
+    case 384: return launch_fft4<T, 24, INV>(data, nseq, nb, sa, sb, se, tw, scale, smax, s);
+    case 512: return launch_fft4<T, 32, INV>(data, nseq, nb, sa, sb, se, tw, scale, smax, s);
+    default: *done = false; return JUBIK_OK;
   }
 }
 
@@ -246,15 +382,25 @@ int fft_batched(const Fft1D& f, void* data, int64_t nseq, int nb, int64_t sa, in
                 int64_t se, bool inverse, double scale, cudaStream_t s) {
   if (nseq <= 0) return JUBIK_OK;
   const int L = f.L;
-  const size_t per = 2 * sizeof(cx<T>) * (size_t)L;
   const int smax = max_smem_optin();
-  int spc = (int)std::max<size_t>(1, std::min<size_t>(64, (size_t)(48 * 1024) / per));
-  if (per > (size_t)smax) {
+  {
+    const cx<T>* tw = (const cx<T>*)(sizeof(T) == 4 ? f.tw32 : f.tw64);
+    bool done = false;
+    const int st = inverse ? try_fft4<T, true>(L, data, nseq, nb, sa, sb, se, tw, scale, smax, s,
+                                               &done)
+                           : try_fft4<T, false>(L, data, nseq, nb, sa, sb, se, tw, scale, smax,
+                                                s, &done);
+    if (done) return st;
+  }
+  const size_t per = 2 * sizeof(cx<T>) * (size_t)L;
+  // (1 KB of the block's shared memory stays for the static sequence offsets)
+  int spc = (int)std::max<size_t>(1, std::min<size_t>(64, (size_t)(47 * 1024) / per));
+  if (per + 1024 > (size_t)smax) {
     set_error("FFT length %d needs %zu bytes of shared memory", L, per);
     return JUBIK_ERR_UNSUPPORTED;
   }
   const size_t smem = per * spc;
-  if (smem > 48 * 1024) {
+  if (smem > 47 * 1024) {
     JUBIK_TRY_CUDA(cudaFuncSetAttribute(k_fft_batched<T>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   }
