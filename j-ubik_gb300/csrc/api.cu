@@ -574,7 +574,7 @@ int jubik_plan_create(const jubik_plan_desc* d, jubik_plan** out) {
                                    "memset accumulator")))
       return fail(st);
   } else {
-    if ((st = p->alloc(&p->hfull, (size_t)units * g.P * g.P * csz))) return fail(st);
+    if ((st = p->alloc(&p->hfull, (size_t)units * g.P * (g.P / 2 + 1) * csz))) return fail(st);
     if ((st = p->alloc(&p->zs, (size_t)plain_pairs(g) * g.P * g.P * csz))) return fail(st);
     // bound the per-chunk unit buffer to ~2 GiB
     const size_t per_module = (size_t)plain_pairs(g) * g.P * g.P * csz;

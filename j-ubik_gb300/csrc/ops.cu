@@ -75,7 +75,8 @@ __global__ void k_psf_to_cplx(const T* __restrict__ psf, int layout, int e_bcast
 }
 
 // Spectrum (FP64, natural order) -> plan storage in dtype T, scaled by 1/P^2
-// (the 1/N of ifftn folded in).  hfull: (U,P,P) for the unfused path;
+// (the 1/N of ifftn folded in).  hfull: (U,P,P/2+1), the half plane kx <= P/2, for the
+// unfused path;
 // hmain/hnyq: half-spectrum rows in the fused kernel's 4-step order.  The
 // fused kernels carry the kx = 0 and kx = P/2 columns of a real signal packed
 // as W = A + iN; their product with the PSF is W' = alpha W + beta conj(W(-ky))
@@ -97,7 +98,7 @@ __global__ void k_spectra_store(const double2* __restrict__ buf, int P, int64_t 
     const double2 v = buf[i];
     const cx<T> w = mkc<T>((T)(v.x * sc), (T)(v.y * sc));
     const int64_t hu = u0 + ul;
-    if (hfull) hfull[hu * P * P + rem] = w;
+    if (hfull && kx <= H) hfull[(hu * P + ky) * (H + 1) + kx] = w;
     if (hmain && kx <= H) {
       const int slot = 16 * (ky % L1) + ky / L1;
       if (kx == 0 || kx == H) {
@@ -123,6 +124,17 @@ __global__ void k_spectra_store(const double2* __restrict__ buf, int P, int64_t 
 // are the spectra of the two real patches; products with the (Hermitian) PSF
 // spectra stay Hermitian, so one inverse transform of A Ha + i B Hb returns
 // both real results as its real and imaginary parts.
+// PSF spectrum value at flat frequency index rem of unit hu, from the stored
+// half plane kx <= P/2 (the spectrum of a real kernel is Hermitian).
+template <typename T>
+__device__ __forceinline__ cx<T> h_at(const cx<T>* __restrict__ hh, int64_t hu, int64_t rem,
+                                      int P) {
+  const int H1 = P / 2 + 1;
+  const int ky = (int)(rem / P), kx = (int)(rem - (int64_t)ky * P);
+  if (kx < H1) return hh[(hu * P + ky) * H1 + kx];
+  return cconj<T>(hh[(hu * P + (P - ky) % P) * H1 + (P - kx)]);
+}
+
 __device__ __forceinline__ int64_t mirror_index(int64_t rem, int P) {
   const int ky = (int)(rem / P), kx = (int)(rem - (int64_t)ky * P);
   return (int64_t)((P - ky) % P) * P + (P - kx) % P;
@@ -175,10 +187,10 @@ __global__ void k_plain_mul_modules(const cx<T>* __restrict__ zs, const cx<T>* _
     const cx<T> ib = cscale<T>(csub<T>(z, zm), (T)0.5);  // i x spectrum of patch 2j + 1
     const int pa = (int)(2 * j), pb = pa + 1;
     const int64_t ha = ((int64_t)m * n2p + pa % n2p) * E + pa / n2p;
-    cx<T> w = cmul<T>(a, hfull[ha * pp + rem]);
+    cx<T> w = cmul<T>(a, h_at<T>(hfull, ha, rem, P));
     if (pb < np) {
       const int64_t hb = ((int64_t)m * n2p + pb % n2p) * E + pb / n2p;
-      w = cadd<T>(w, cmul<T>(ib, hfull[hb * pp + rem]));
+      w = cadd<T>(w, cmul<T>(ib, h_at<T>(hfull, hb, rem, P)));
     }
     zu[i] = w;
   }
@@ -285,10 +297,10 @@ __global__ void k_plain_mulconj_accum(const cx<T>* __restrict__ zu, const cx<T>*
       const cx<T> a = cscale<T>(cadd<T>(z, zm), (T)0.5);
       const cx<T> ib = cscale<T>(csub<T>(z, zm), (T)0.5);
       const int64_t ha = ((int64_t)(m0 + mm) * n2p + pa % n2p) * E + pa / n2p;
-      acc = cadd<T>(acc, cmulc<T>(a, hfull[ha * pp + rem]));
+      acc = cadd<T>(acc, cmulc<T>(a, h_at<T>(hfull, ha, rem, P)));
       if (pb < np) {
         const int64_t hb = ((int64_t)(m0 + mm) * n2p + pb % n2p) * E + pb / n2p;
-        acc = cadd<T>(acc, cmulc<T>(ib, hfull[hb * pp + rem]));
+        acc = cadd<T>(acc, cmulc<T>(ib, h_at<T>(hfull, hb, rem, P)));
       }
     }
     zs[i] = acc;
