@@ -109,8 +109,20 @@ class _PlanCache:
 _CACHE = _PlanCache()
 
 
-def _kernel_key(k: torch.Tensor):
-    return (k.data_ptr(), k._version, tuple(k.shape), k.dtype)
+def _kernel_key(src):
+    """Cache key of a PSF kernel as the caller passed it, and the object to keep
+    alive with the cached spectra.  A torch tensor is keyed by its storage and
+    version counter (in-place edits change the version); any other array by
+    its identity plus a sample of its values.  Keeping the source alive stops
+    its storage or identity from being reused by a different kernel while
+    the spectra are cached."""
+    if isinstance(src, torch.Tensor):
+        return ("tensor", src.data_ptr(), src._version, tuple(src.shape), src.dtype,
+                str(src.device)), src
+    a = np.asarray(src)
+    flat = a.reshape(-1)
+    sample = flat[:: max(1, flat.size // 4096)][:4096]
+    return ("array", id(src), a.shape, a.dtype.str, hash(sample.tobytes())), src
 
 
 def linpatch_plan(x_shape, kernel_shape, n_patches_per_axis, margin, dtype, n_modules=1):
@@ -125,11 +137,11 @@ def linpatch_plan(x_shape, kernel_shape, n_patches_per_axis, margin, dtype, n_mo
     return ent
 
 
-def _prepare_kernel(ent, kernel: torch.Tensor, E: int, field):
+def _prepare_kernel(ent, src, kernel: torch.Tensor, E: int, field):
     """Kernels shaped like the field are full-field kernels (the reference's
     input, cut by convolve.py:107-111); any other window is taken as pre-cut."""
     plan: ResponsePlan = ent["plan"]
-    key = _kernel_key(kernel)
+    key, keep = _kernel_key(src)
     if ent["psf_key"] == key:
         return
     n2 = plan.n_patches ** 2
@@ -138,7 +150,7 @@ def _prepare_kernel(ent, kernel: torch.Tensor, E: int, field):
     else:
         k = kernel.reshape(1, n2, E, kernel.shape[-2], kernel.shape[-1])
     plan.set_psf(k, "full" if tuple(kernel.shape[-2:]) == tuple(field) else "precut")
-    ent["psf_key"] = key
+    ent["psf_key"], ent["psf_src"] = key, keep
 
 
 class _LinpatchFn(torch.autograd.Function):
@@ -181,7 +193,7 @@ def linpatch_convolve(x, domain, kernel, n_patches_per_axis, margin):
         print("signal_shape:", (kt.shape[0],) + shape)
         print("Dimension Inconsistency. Broadcasting PSFs")
     ent = linpatch_plan(shape, tuple(kt.shape), n_patches_per_axis, margin, dtype)
-    _prepare_kernel(ent, kt, E, shape[-2:])
+    _prepare_kernel(ent, kernel, kt, E, shape[-2:])
     plan = ent["plan"]
     xin = xt.reshape((E,) + shape[-2:])
     out = _LinpatchFn.apply(xin, plan)

@@ -44,11 +44,11 @@ def build_psf_op(domain, npatch: int, margin: int, dtype: torch.dtype = torch.fl
             plan = ResponsePlan(M, E, shape[-2:], npatch, margin, dtype=dtype, path=path,
                                 device=dev)
             state["plan"], state["key"] = plan, None
-        key = _kernel_key(k)
+        key, keep = _kernel_key(kernel)
         if state["key"] != key:
             kk = k if k.dim() == 4 else k.reshape(M, npatch ** 2, E, k.shape[-2], k.shape[-1])
             plan.set_psf(kk)
-            state["key"] = key
+            state["key"], state["keep"] = key, keep
         xt = x if isinstance(x, torch.Tensor) else torch.as_tensor(np.asarray(x))
         xt = xt.to(device=dev, dtype=dtype).reshape((E,) + shape[-2:])
         out = PsfOpFn.apply(xt, plan)
@@ -86,7 +86,7 @@ class Response:
                                  path=path, pixel_area=self.pixel_area, device=dev)
         self.plan.set_psf(k if k.dim() == 4 else
                           k.reshape(self.M, n_patch ** 2, self.E, k.shape[-2], k.shape[-1]))
-        self._kernel_key = _kernel_key(k)
+        self._kernel_key, self._kernel_keep = _kernel_key(kernel)
         self.kernel = k
         full = (self.M, self.E) + shape[-2:]
         exp = None
@@ -123,12 +123,12 @@ class Response:
 
     def __call__(self, x, k=None) -> Vector:
         if k is not None:
-            kt = as_device(k, self.plan.dtype, self.plan.device)
-            key = _kernel_key(kt)
+            key, keep = _kernel_key(k)
             if key != self._kernel_key:
+                kt = as_device(k, self.plan.dtype, self.plan.device)
                 self.plan.set_psf(kt if kt.dim() == 4 else kt.reshape(
                     self.M, self.plan.n_patches ** 2, self.E, kt.shape[-2], kt.shape[-1]))
-                self._kernel_key = key
+                self._kernel_key, self._kernel_keep = key, keep
         parts = torch.split(self.flat(x), self.plan.readout_sizes)
         return Vector(dict(zip(self.keys, parts)))
 

@@ -434,3 +434,18 @@ def test_path_override_from_environment(cuda, monkeypatch):
     monkeypatch.setenv("JUBIK_PATH", "bogus")
     with pytest.raises(ValueError):
         ju.ResponsePlan(1, 1, (64, 64), 4, 8, dtype=torch.float32)
+
+
+def test_linpatch_convolve_picks_up_a_new_kernel(cuda):
+    """Two calls with different numpy kernels of the same shape: the cached PSF
+    spectra must follow the second kernel (its device copy may reuse the
+    first one's memory)."""
+    nx, dx, m, E = 64, 16, 8, 1
+    inst = synthetic.config2(nx=nx, dx=dx, margin=m, n_modules=1, n_energies=E)
+    dom = O.Domain((E, nx, nx), (1.0, 1.0, 1.0))
+    ka = np.ascontiguousarray(inst.psf[0])
+    for scale in (1.0, 3.0):
+        k = ka ** scale  # a new array each time, same shape
+        got = ju.linpatch_convolve(inst.sky, ju.Domain(dom.shape, dom.distances), k, nx // dx, m)
+        ref = O.linpatch_convolve(inst.sky, dom, k, nx // dx, m, precut=True)
+        assert rel(got, ref) < 1e-12

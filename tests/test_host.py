@@ -90,3 +90,21 @@ def test_problem_batch_needs_a_gpu_and_problems():
     from jubik_gb300 import synthetic
     with pytest.raises(ju.JubikError):
         ju.ProblemBatch(synthetic.config5(count=1, max_side=160))
+
+
+def test_kernel_cache_keys_distinguish_new_arrays():
+    """The PSF-spectrum cache must not take a new kernel for an old one when
+    memory or object identities are reused."""
+    import torch
+    from jubik_gb300.convolve import _kernel_key
+    a = np.ones((4, 8, 8))
+    ka, keep = _kernel_key(a)
+    assert keep is a
+    assert _kernel_key(a)[0] == ka                      # same object, same values
+    b = a.copy()
+    b[0, 0, 0] = 2.0
+    assert _kernel_key(b)[0] != ka                      # a different array
+    t = torch.ones(4, 8, 8)
+    kt, _ = _kernel_key(t)
+    t.mul_(2.0)                                         # in-place edit bumps the version
+    assert _kernel_key(t)[0] != kt
