@@ -217,11 +217,20 @@ def uneven_batch_leg(dev, n_streams=8, passes=10):
         loop_ms = timed(b.energy_and_grad)
         b.capture()
         graph_ms = timed(b.replay)
-        return {"problems": len(insts), "mpix_per_pass": b.mpix, "streams": n_streams,
-                "paths": {str(k): v for k, v in chosen.items()},
-                "loop_ms": loop_ms, "graph_ms": graph_ms,
-                "loop_mpix_s": b.mpix / (loop_ms / 1e3), "graph_mpix_s": b.mpix / (graph_ms / 1e3),
-                "graph_speedup": loop_ms / graph_ms}
+        out = {"problems": len(insts), "mpix_per_pass": b.mpix, "streams": n_streams,
+               "paths": {str(k): v for k, v in chosen.items()},
+               "loop_ms": loop_ms, "graph_ms": graph_ms, "loop_launches": 5 * len(insts),
+               "loop_mpix_s": b.mpix / (loop_ms / 1e3), "graph_mpix_s": b.mpix / (graph_ms / 1e3),
+               "graph_speedup": loop_ms / graph_ms}
+        if b.group():  # one launch per stage and FFT side over all problems
+            grouped_ms = timed(b.energy_and_grad)
+            b.capture()
+            grouped_graph_ms = timed(b.replay)
+            out.update({"grouped_launches": b.launches_per_pass(), "grouped_ms": grouped_ms,
+                        "grouped_graph_ms": grouped_graph_ms,
+                        "grouped_mpix_s": b.mpix / (grouped_ms / 1e3),
+                        "grouped_graph_mpix_s": b.mpix / (grouped_graph_ms / 1e3)})
+        return out
     finally:
         b.close()
 

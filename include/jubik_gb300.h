@@ -219,6 +219,27 @@ JUBIK_API int jubik_psf_interpolate(const double* psfs, const double* rs,
                                     double dist_x, double dist_y, int32_t npatch, int32_t layout,
                                     int32_t dtype, void* out, void* stream);
 
+/* Independent problems evaluated together (no counterpart in the reference,
+ * which evaluates one likelihood per call): plans of one dtype that run the
+ * per-unit fused kernels (one module, or path JUBIK_PATH_FUSED_UNIT, with a
+ * fused FFT side), grouped by FFT side.  One energy+gradient call of the group
+ * is one grouped clearing kernel, one forward and one adjoint launch per FFT
+ * side over all of that side's problems, and one grouped likelihood pass --
+ * the work of jubik_poisson_energy_grad on every plan.  The plans must outlive
+ * the group, and none of them may run another call while a group call is in
+ * flight.
+ * set_io: the device sky and gradient buffer of each problem (x[i], grad[i],
+ * shaped (E,nx,ny) of plan i) and a device double[n] for the energies; they
+ * are read at every later call. */
+typedef struct jubik_group jubik_group;
+JUBIK_API int jubik_group_create(jubik_plan* const* plans, int32_t n, jubik_group** out);
+JUBIK_API int jubik_group_set_io(jubik_group* group, const void* const* x, void* const* grad,
+                                 double* energies);
+JUBIK_API int jubik_group_energy_grad(jubik_group* group, void* stream);
+/* Kernel launches per jubik_group_energy_grad call. */
+JUBIK_API int jubik_group_launches(const jubik_group* group, int32_t* launches);
+JUBIK_API int jubik_group_destroy(jubik_group* group);
+
 /* Sampling and global reductions for the callers of the response.
  * Random numbers: counter-based Philox4x32-10 (Salmon et al., SC'11) keyed by
  * `seed`; element i of a call uses its own counter, so results do not depend

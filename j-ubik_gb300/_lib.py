@@ -85,6 +85,11 @@ _SIGS = {
     "jubik_random_poisson": ([_vp, _i64, _i32, C.c_uint64, C.c_uint32, _vp, _vp], C.c_int),
     "jubik_dot": ([_vp, _vp, _i64, _i32, _vp, _vp], C.c_int),
     "jubik_plan_set_dependent_launch": ([_vp, _i32], C.c_int),
+    "jubik_group_create": ([_vp, _i32, _vp], C.c_int),
+    "jubik_group_set_io": ([_vp, _vp, _vp, _vp], C.c_int),
+    "jubik_group_energy_grad": ([_vp, _vp], C.c_int),
+    "jubik_group_launches": ([_vp, _vp], C.c_int),
+    "jubik_group_destroy": ([_vp], C.c_int),
     "jubik_poisson_energy_grad_logsky": ([_vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp], C.c_int),
     "jubik_psf_interpolate": ([_vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32,
                                _dbl, _dbl, _i32, _i32, _i32, _vp, _vp], C.c_int),

@@ -14,16 +14,23 @@ side by side, and one graph launch replaces every per-problem launch.
 timing the candidates (module-shared fused, per-unit fused, unfused) on the
 largest problem of that side.  Problems with one module take the same kernels
 on both fused paths.
+
+When every problem runs the per-unit fused kernels, :meth:`ProblemBatch.group`
+switches the pass to grouped launches (``jubik_group_*``): one clearing
+kernel, one forward and one adjoint launch per FFT side over all of that
+side's problems, and one likelihood pass over all problems -- a handful of
+launches in place of five per problem.  The grouped pass can be captured too.
 """
 from __future__ import annotations
 
+import ctypes as C
 from typing import Dict, List, Optional, Sequence
 
 import numpy as np
 import torch
 
 from . import _lib
-from .plan import ResponsePlan, require_cuda
+from .plan import ResponsePlan, require_cuda, stream_handle
 
 
 def _fft_side(inst) -> int:
@@ -58,6 +65,7 @@ class ProblemBatch:
         self.grad = [torch.empty_like(x) for x in self.x]
         self._graph = None
         self._streams: List[torch.cuda.Stream] = []
+        self._group = None
 
     # ------------------------------------------------------------ set-up
     def _make_plan(self, inst, path: Optional[str] = None) -> ResponsePlan:
@@ -135,7 +143,45 @@ class ProblemBatch:
             self._rebuild()
         return chosen
 
+    def group(self) -> bool:
+        """Switch the pass to grouped launches; False (and the per-problem pass
+        stays) when a problem does not run the per-unit fused kernels."""
+        self._drop_group()
+        lib = _lib.load()
+        n = len(self.plans)
+        handles = (C.c_void_p * n)(*[p._h.value for p in self.plans])
+        g = C.c_void_p()
+        if lib.jubik_group_create(handles, n, C.byref(g)) != _lib.OK:
+            return False
+        xs = (C.c_void_p * n)(*[x.data_ptr() for x in self.x])
+        gs = (C.c_void_p * n)(*[t.data_ptr() for t in self.grad])
+        st = lib.jubik_group_set_io(g, xs, gs, C.c_void_p(self.energy.data_ptr()))
+        if st != _lib.OK:
+            lib.jubik_group_destroy(g)
+            _lib.check(st, "jubik_group_set_io")
+        self._group = g
+        self._graph = None
+        return True
+
+    @property
+    def grouped(self) -> bool:
+        return self._group is not None
+
+    def launches_per_pass(self) -> int:
+        """Kernel launches of one pass (grouped, or five per problem)."""
+        if self._group is None:
+            return 5 * len(self.plans)
+        n = C.c_int32()
+        _lib.call("jubik_group_launches", self._group, C.byref(n))
+        return int(n.value)
+
+    def _drop_group(self):
+        if self._group is not None:
+            _lib.load().jubik_group_destroy(self._group)
+            self._group = None
+
     def _rebuild(self):
+        self._drop_group()
         for p in self.plans:
             p.close()
         self.plans = [self._make_plan(i) for i in self.instruments]
@@ -146,6 +192,9 @@ class ProblemBatch:
 
     # ------------------------------------------------------------ evaluation
     def _pass(self, streams: Optional[List[torch.cuda.Stream]]):
+        if self._group is not None:
+            _lib.call("jubik_group_energy_grad", self._group, stream_handle(self.device))
+            return
         if not streams:
             for k, plan in enumerate(self.plans):
                 plan.energy_and_grad(self.x[k], energy=self.energy[k], grad=self.grad[k])
@@ -171,7 +220,8 @@ class ProblemBatch:
         kernel's one-time set-up happens outside the capture."""
         self._pass(None)
         torch.cuda.synchronize(self.device)
-        self._streams = [torch.cuda.Stream(self.device) for _ in range(self.n_streams)]
+        self._streams = ([] if self._group is not None else
+                         [torch.cuda.Stream(self.device) for _ in range(self.n_streams)])
         graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(graph):
             self._pass(self._streams)
@@ -189,6 +239,7 @@ class ProblemBatch:
 
     def close(self):
         self._graph = None
+        self._drop_group()
         for p in self.plans:
             p.close()
         self.plans = []

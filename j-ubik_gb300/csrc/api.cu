@@ -1,5 +1,6 @@
 // C ABI of libjubik_gb300: plans, workspace, dispatch of the fused and the
 // unfused (plain) paths, readout index map, likelihood entry points.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -1040,6 +1041,220 @@ int jubik_convolve2d(const void* kernel, int64_t bk, const void* signal, int64_t
   fft1d_free(&fh);
   fft1d_free(&fw);
   return st;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- groups
+// Independent problems evaluated together: per FFT side one grouped launch of
+// each per-unit stage, one grouped likelihood pass and one grouped clearing
+// kernel, instead of a launch sequence per problem.
+struct GroupClass {
+  int P = 0;
+  std::vector<int> members;  // indices into the group's plans
+  int64_t blocks = 0;        // units of all members
+  void* fwd_list = nullptr;  // device Args per member: forward per-unit stage
+  void* adj_list = nullptr;  // device Args per member: adjoint per-unit stage
+  int* starts = nullptr;     // device: first block of each member, then the total
+};
+
+struct jubik_group {
+  std::vector<jubik_plan*> plans;
+  int dtype = JUBIK_F32;
+  std::vector<GroupClass> classes;
+  PoissonJob* pjobs = nullptr;
+  int* pstarts = nullptr;
+  int64_t pblocks = 0;
+  ZeroJob* zjobs = nullptr;
+  int* zstarts = nullptr;
+  int64_t zblocks = 0;
+  int nzero = 0;
+  bool io_set = false;
+  std::vector<void*> allocs;
+  int alloc(void** p, size_t n) {
+    JUBIK_TRY_CUDA(cudaMalloc(p, n));
+    allocs.push_back(*p);
+    return JUBIK_OK;
+  }
+  void free_io() {
+    for (void* p : allocs) cudaFree(p);
+    allocs.clear();
+    for (auto& c : classes) c.fwd_list = c.adj_list = c.starts = nullptr;
+    pjobs = nullptr;
+    zjobs = nullptr;
+    pstarts = zstarts = nullptr;
+    io_set = false;
+  }
+  ~jubik_group() { free_io(); }
+};
+
+namespace {
+template <typename V>
+int upload(jubik_group* g, const std::vector<V>& host, V** dev) {
+  JUBIK_TRY(g->alloc((void**)dev, sizeof(V) * std::max<size_t>(1, host.size())));
+  return cuda_status(cudaMemcpy(*dev, host.data(), sizeof(V) * host.size(),
+                                cudaMemcpyHostToDevice),
+                     "group upload");
+}
+}  // namespace
+
+extern "C" {
+
+int jubik_group_create(jubik_plan* const* plans, int32_t n, jubik_group** out) {
+  if (!plans || n < 1 || !out) {
+    set_error("group: need at least one plan");
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  auto* g = new (std::nothrow) jubik_group();
+  if (!g) {
+    set_error("group: out of host memory");
+    return JUBIK_ERR_ALLOC;
+  }
+  for (int i = 0; i < n; ++i) {
+    jubik_plan* p = plans[i];
+    int st = JUBIK_OK;
+    if (!p) {
+      set_error("group: plan %d is NULL", i);
+      st = JUBIK_ERR_INVALID_ARGUMENT;
+    } else if (p->path != JUBIK_PATH_FUSED || p->spec) {
+      set_error("group: plan %d does not run the per-unit fused kernels (one module, or path "
+                "fused_unit, with a fused FFT side)", i);
+      st = JUBIK_ERR_UNSUPPORTED;
+    } else if (i > 0 && p->dtype != plans[0]->dtype) {
+      set_error("group: plans of different dtypes");
+      st = JUBIK_ERR_INVALID_ARGUMENT;
+    } else if (!p->psf_set || !p->data_set) {
+      set_error("group: plan %d needs its PSF and data set", i);
+      st = JUBIK_ERR_STATE;
+    }
+    if (st) {
+      delete g;
+      return st;
+    }
+    g->plans.push_back(p);
+  }
+  g->dtype = plans[0]->dtype;
+  for (int i = 0; i < n; ++i) {
+    const int P = g->plans[i]->g.P;
+    auto it = std::find_if(g->classes.begin(), g->classes.end(),
+                           [&](const GroupClass& c) { return c.P == P; });
+    if (it == g->classes.end()) {
+      g->classes.emplace_back();
+      g->classes.back().P = P;
+      it = g->classes.end() - 1;
+    }
+    it->members.push_back(i);
+  }
+  *out = g;
+  return JUBIK_OK;
+}
+
+int jubik_group_set_io(jubik_group* g, const void* const* x, void* const* grad,
+                       double* energies) {
+  if (!g || !x || !grad || !energies) {
+    set_error("group: invalid arguments");
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  const int n = (int)g->plans.size();
+  for (int i = 0; i < n; ++i) {
+    if (!x[i] || !grad[i]) {
+      set_error("group: problem %d has no sky or gradient buffer", i);
+      return JUBIK_ERR_INVALID_ARGUMENT;
+    }
+  }
+  g->free_io();
+  const size_t asz = fused_args_size();
+  for (auto& c : g->classes) {
+    std::vector<unsigned char> fwd(asz * c.members.size()), adj(asz * c.members.size());
+    std::vector<int> starts;
+    int64_t b = 0;
+    for (size_t k = 0; k < c.members.size(); ++k) {
+      const int i = c.members[k];
+      jubik_plan* p = g->plans[i];
+      starts.push_back((int)b);
+      b += p->g.units();
+      FusedLaunch f{x[i], p->conv, p->hmain, p->hnyq, p->tw, p->wt, p->desc.pixel_area, nullptr};
+      fused_args_fill(p->g, p->dtype, f, FUSED_FWD_UNITS, fwd.data() + k * asz);
+      FusedLaunch r{p->resid, grad[i], p->hmain, p->hnyq, p->tw, p->wt, p->desc.pixel_area,
+                    nullptr};
+      fused_args_fill(p->g, p->dtype, r, FUSED_ADJ_UNITS, adj.data() + k * asz);
+    }
+    if (b > 0x7fffffffLL) {
+      set_error("group: too many patch units");
+      return JUBIK_ERR_UNSUPPORTED;
+    }
+    starts.push_back((int)b);
+    c.blocks = b;
+    JUBIK_TRY(upload(g, fwd, (unsigned char**)&c.fwd_list));
+    JUBIK_TRY(upload(g, adj, (unsigned char**)&c.adj_list));
+    JUBIK_TRY(upload(g, starts, &c.starts));
+  }
+  std::vector<PoissonJob> pj;
+  std::vector<ZeroJob> zj;
+  std::vector<int> ps, zs;
+  int64_t pb = 0, zb = 0;
+  for (int i = 0; i < n; ++i) {
+    jubik_plan* p = g->plans[i];
+    const int64_t img = image_elems(p);
+    pj.push_back(PoissonJob{p->conv, p->eps, p->dimg, img, p->lam, p->resid, p->partials,
+                            p->counter, energies + i});
+    ps.push_back((int)pb);
+    pb += poisson_group_blocks(img);
+    // each problem's overlap-add image and gradient start from zero
+    const int64_t bytes[2] = {img * (int64_t)p->esz, (int64_t)p->g.E * p->g.pixels() *
+                                                         (int64_t)p->esz};
+    void* ptrs[2] = {p->conv, grad[i]};
+    for (int t = 0; t < 2; ++t) {
+      zj.push_back(ZeroJob{ptrs[t], bytes[t]});
+      zs.push_back((int)zb);
+      zb += std::max<int64_t>(1, std::min<int64_t>(1024, bytes[t] / (256 * 16 * 8)));
+    }
+  }
+  ps.push_back((int)pb);
+  zs.push_back((int)zb);
+  g->pblocks = pb;
+  g->zblocks = zb;
+  g->nzero = (int)zj.size();
+  JUBIK_TRY(upload(g, pj, &g->pjobs));
+  JUBIK_TRY(upload(g, ps, &g->pstarts));
+  JUBIK_TRY(upload(g, zj, &g->zjobs));
+  JUBIK_TRY(upload(g, zs, &g->zstarts));
+  g->io_set = true;
+  return JUBIK_OK;
+}
+
+int jubik_group_energy_grad(jubik_group* g, void* stream) {
+  NvtxRange nvtx_("jubik_group_energy_grad");
+  if (!g || !g->io_set) {
+    set_error("group: set the sky, gradient and energy buffers first");
+    return JUBIK_ERR_STATE;
+  }
+  cudaStream_t s = S(stream);
+  const int n = (int)g->plans.size();
+  JUBIK_TRY(zero_group_run(g->zjobs, g->zstarts, g->nzero, g->zblocks, true, s));
+  for (auto& c : g->classes)
+    JUBIK_TRY(fused_group_run(c.P, g->dtype, c.fwd_list, c.starts, (int)c.members.size(),
+                              c.blocks, false, true, s));
+  JUBIK_TRY(poisson_group_run(g->dtype, g->pjobs, g->pstarts, n, g->pblocks, true, s));
+  for (auto& c : g->classes)
+    JUBIK_TRY(fused_group_run(c.P, g->dtype, c.adj_list, c.starts, (int)c.members.size(),
+                              c.blocks, true, true, s));
+  for (jubik_plan* p : g->plans) p->lam_valid = true;
+  return JUBIK_OK;
+}
+
+int jubik_group_launches(const jubik_group* g, int32_t* launches) {
+  if (!g || !launches) {
+    set_error("group: invalid arguments");
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  *launches = 2 + 2 * (int32_t)g->classes.size();
+  return JUBIK_OK;
+}
+
+int jubik_group_destroy(jubik_group* g) {
+  if (g) delete g;
+  return JUBIK_OK;
 }
 
 }  // extern "C"

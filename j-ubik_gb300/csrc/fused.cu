@@ -31,6 +31,7 @@
 // (classes kappa and 16-kappa form closed slot sets), the inverse combine
 // into the first inverse row phase.
 #include <cstdio>
+#include <cstring>
 
 #include "fft_codelets.cuh"
 #include "internal.h"
@@ -194,8 +195,10 @@ struct Unit {
   const cx<T>* twg;
   cx<T> wq[16];
 
-  // blockIdx -> (m, e, k); per_module == false decodes (e, k) only
-  __device__ __forceinline__ void init(const Args& a, unsigned char* smem, bool per_module) {
+  // unit block index ub (the CTA's blockIdx.x unless a grouped launch maps it)
+  // -> (m, e, k); per_module == false decodes (e, k) only
+  __device__ __forceinline__ void init(const Args& a, unsigned char* smem, bool per_module,
+                                       int ub = -1) {
     tile = reinterpret_cast<cx<T>*>(smem);
     stg = tile + R::TILE;
     tid = threadIdx.x;
@@ -203,7 +206,7 @@ struct Unit {
     lane = tid & 31;
     cls = warp;
     const int n2p = a.n * a.n;
-    int u = blockIdx.x;
+    int u = ub >= 0 ? ub : (int)blockIdx.x;
     m = 0;
     if (per_module) {
       m = u % a.M;
@@ -792,12 +795,10 @@ __device__ __forceinline__ void prefetch_unit(const void* h, unsigned hb, const 
 // ================================================================= kernels
 // One CTA per unit: the whole forward or adjoint of one patch.
 template <typename T, int P, bool ADJ>
-__global__ void __launch_bounds__(Tr<T, P>::NT) k_fused(Args a) {
+__device__ __forceinline__ void fused_unit_body(const Args& a, int ub, unsigned char* smem_raw) {
   using R = Tr<T, P>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   Unit<T, P> U;
-  pdl_trigger();
-  U.init(a, smem_raw, true);
+  U.init(a, smem_raw, true, ub);
   prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
   pdl_wait();
   stage_input<T, P, ADJ>(U, a);
@@ -812,6 +813,38 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fused(Args a) {
   stage_combine<T, P>(U, ADJ ? U.mg / 2 : 0, ADJ ? (U.mg + U.K + 1) / 2 : R::H);
   __syncthreads();
   stage_output<T, P, ADJ>(U, a);
+}
+
+template <typename T, int P, bool ADJ>
+__global__ void __launch_bounds__(Tr<T, P>::NT) k_fused(Args a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  pdl_trigger();
+  fused_unit_body<T, P, ADJ>(a, (int)blockIdx.x, smem_raw);
+}
+
+// Grouped launch over independent problems of one FFT side: problem p owns
+// blocks [starts[p], starts[p + 1]) and its own arguments list[p].
+template <typename T, int P, bool ADJ>
+__global__ void __launch_bounds__(Tr<T, P>::NT)
+    k_fused_group(const Args* __restrict__ list, const int* __restrict__ starts, int nprob) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_prob;
+  pdl_trigger();
+  if (threadIdx.x == 0) {  // the last problem whose first block is <= blockIdx.x
+    int lo = 0, hi = nprob - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (starts[mid] <= (int)blockIdx.x)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    s_prob = lo;
+  }
+  __syncthreads();
+  const int p = s_prob;
+  const Args a = list[p];
+  fused_unit_body<T, P, ADJ>(a, (int)blockIdx.x - starts[p], smem_raw);
 }
 
 // Forward, module-shared: the sky spectrum of each (energy, patch) once; the
@@ -904,8 +937,8 @@ int set_smem(KernelT kern, size_t smem) {
       "cudaFuncSetAttribute");
 }
 
-template <typename T, int P>
-int launch_one(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
+// Kernel arguments of one stage of one plan (sizes in bytes use esz).
+Args make_args(const Geom& g, const FusedLaunch& f, int which, size_t esz) {
   Args a;
   a.in = f.in;
   a.out = f.out;
@@ -925,11 +958,28 @@ int launch_one(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
   a.half = g.half;
   a.sr_max = g.sr_max;
   a.sc_max = g.sc_max;
-  using R = Tr<T, P>;
-  const size_t smem = R::SMEM;
-  // the shared-memory opt-in is a per-device function attribute: set it once
-  // per device before the first launch there (so never inside a stream capture
-  // that follows a warm-up call)
+  const int64_t units = g.units();
+  const int64_t patches = (int64_t)g.E * g.n * g.n;
+  const int64_t grid = which == FUSED_FWD_SKY ? patches : units;
+  const int64_t zbytes =
+      (which == FUSED_FWD_SKY ? (int64_t)g.M : 1) * g.E * g.pixels() * (int64_t)esz;
+  a.zchunk = grid > 0 ? ((zbytes + grid - 1) / grid + 15) & ~(int64_t)15 : 0;
+  a.aux = f.aux;
+  a.aux_bytes = f.aux ? f.aux_bytes : 0;
+  a.aux_chunk = grid > 0 ? ((a.aux_bytes + grid - 1) / grid + 15) & ~(int64_t)15 : 0;
+  a.zero_out = f.zero_out ? 1 : 0;
+  a.in_rs = f.in_rs > 0 ? f.in_rs : (int64_t)g.ny;
+  a.in_ps = f.in_ps > 0 ? f.in_ps : g.pixels();
+  a.in_exp = f.in_exp ? 1 : 0;
+  return a;
+}
+
+// The shared-memory opt-in is a per-device function attribute: set it once per
+// device before the first launch there (so never inside a stream capture that
+// follows a warm-up call).
+template <typename T, int P>
+int ensure_smem_attrs() {
+  const size_t smem = Tr<T, P>::SMEM;
   constexpr int kMaxDev = 64;
   static bool attr_set[kMaxDev] = {};
   int dev = 0;
@@ -941,27 +991,40 @@ int launch_one(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
   if (!attr_set[dev]) {
     JUBIK_TRY(set_smem(k_fused<T, P, false>, smem));
     JUBIK_TRY(set_smem(k_fused<T, P, true>, smem));
+    JUBIK_TRY(set_smem(k_fused_group<T, P, false>, smem));
+    JUBIK_TRY(set_smem(k_fused_group<T, P, true>, smem));
     JUBIK_TRY(set_smem(k_sky_spec<T, P>, smem));
     JUBIK_TRY(set_smem(k_fwd_from_spec<T, P>, smem));
     JUBIK_TRY(set_smem(k_adj_to_spec<T, P>, smem));
     JUBIK_TRY(set_smem(k_adj_from_spec<T, P>, smem));
     attr_set[dev] = true;
   }
+  return JUBIK_OK;
+}
+
+// Launch with programmatic stream serialisation when pdl: the kernel may be
+// scheduled while the previous kernel of the stream drains (see pdl_wait).
+template <typename T, int P, typename KernelT, typename... ArgsT>
+int launch_pdl(KernelT kern, int64_t grid, bool pdl, cudaStream_t s, ArgsT... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(Tr<T, P>::NT);
+  cfg.dynamicSmemBytes = Tr<T, P>::SMEM;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cuda_status(cudaLaunchKernelEx(&cfg, kern, args...), "fused kernel launch");
+}
+
+template <typename T, int P>
+int launch_one(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
+  JUBIK_TRY((ensure_smem_attrs<T, P>()));
+  const Args a = make_args(g, f, which, sizeof(T));
   const int64_t units = g.units();
   const int64_t patches = (int64_t)g.E * g.n * g.n;
-  {
-    const int64_t grid = which == FUSED_FWD_SKY ? patches : units;
-    const int64_t zbytes = (which == FUSED_FWD_SKY ? (int64_t)g.M : 1) * g.E * g.pixels() *
-                           (int64_t)sizeof(T);
-    a.zchunk = grid > 0 ? ((zbytes + grid - 1) / grid + 15) & ~(int64_t)15 : 0;
-    a.aux = f.aux;
-    a.aux_bytes = f.aux ? f.aux_bytes : 0;
-    a.aux_chunk = grid > 0 ? ((a.aux_bytes + grid - 1) / grid + 15) & ~(int64_t)15 : 0;
-    a.zero_out = f.zero_out ? 1 : 0;
-    a.in_rs = f.in_rs > 0 ? f.in_rs : (int64_t)g.ny;
-    a.in_ps = f.in_ps > 0 ? f.in_ps : g.pixels();
-    a.in_exp = f.in_exp ? 1 : 0;
-  }
   if (units <= 0) return JUBIK_OK;
   if (units > 0x7fffffffLL) {
     set_error("too many patch units for one launch");
@@ -971,32 +1034,49 @@ int launch_one(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
     set_error("module-shared kernels need the spectrum workspace");
     return JUBIK_ERR_STATE;
   }
-  // launched with programmatic stream serialisation: the kernel may be
-  // scheduled while the previous kernel of the stream drains (see pdl_wait)
-  auto launch = [&](auto kern, int64_t grid) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)grid);
-    cfg.blockDim = dim3(R::NT);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = f.pdl ? 1 : 0;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cuda_status(cudaLaunchKernelEx(&cfg, kern, a), "fused kernel launch");
-  };
   switch (which) {
-    case FUSED_FWD_UNITS: return launch(k_fused<T, P, false>, units);
-    case FUSED_ADJ_UNITS: return launch(k_fused<T, P, true>, units);
-    case FUSED_FWD_SKY: return launch(k_sky_spec<T, P>, patches);
-    case FUSED_FWD_FROM_SPEC: return launch(k_fwd_from_spec<T, P>, units);
-    case FUSED_ADJ_TO_SPEC: return launch(k_adj_to_spec<T, P>, units);
-    case FUSED_ADJ_FROM_SPEC: return launch(k_adj_from_spec<T, P>, patches);
+    case FUSED_FWD_UNITS: return launch_pdl<T, P>(k_fused<T, P, false>, units, f.pdl, s, a);
+    case FUSED_ADJ_UNITS: return launch_pdl<T, P>(k_fused<T, P, true>, units, f.pdl, s, a);
+    case FUSED_FWD_SKY: return launch_pdl<T, P>(k_sky_spec<T, P>, patches, f.pdl, s, a);
+    case FUSED_FWD_FROM_SPEC: return launch_pdl<T, P>(k_fwd_from_spec<T, P>, units, f.pdl, s, a);
+    case FUSED_ADJ_TO_SPEC: return launch_pdl<T, P>(k_adj_to_spec<T, P>, units, f.pdl, s, a);
+    case FUSED_ADJ_FROM_SPEC: return launch_pdl<T, P>(k_adj_from_spec<T, P>, patches, f.pdl, s, a);
     default:
       set_error("unknown fused stage %d", which);
       return JUBIK_ERR_INVALID_ARGUMENT;
   }
+}
+
+template <typename T, int P>
+int launch_group(const void* list, const int* starts, int nprob, int64_t blocks, bool adj,
+                 bool pdl, cudaStream_t s) {
+  JUBIK_TRY((ensure_smem_attrs<T, P>()));
+  if (blocks <= 0) return JUBIK_OK;
+  if (blocks > 0x7fffffffLL) {
+    set_error("too many patch units for one launch");
+    return JUBIK_ERR_UNSUPPORTED;
+  }
+  const Args* l = (const Args*)list;
+  return adj ? launch_pdl<T, P>(k_fused_group<T, P, true>, blocks, pdl, s, l, starts, nprob)
+             : launch_pdl<T, P>(k_fused_group<T, P, false>, blocks, pdl, s, l, starts, nprob);
+}
+
+template <typename T>
+int dispatch_group(int P, const void* list, const int* starts, int nprob, int64_t blocks,
+                   bool adj, bool pdl, cudaStream_t s) {
+  switch (P) {
+    case 32: return launch_group<T, 32>(list, starts, nprob, blocks, adj, pdl, s);
+    case 64: return launch_group<T, 64>(list, starts, nprob, blocks, adj, pdl, s);
+    case 96: return launch_group<T, 96>(list, starts, nprob, blocks, adj, pdl, s);
+    case 128: return launch_group<T, 128>(list, starts, nprob, blocks, adj, pdl, s);
+    case 192:
+      if constexpr (sizeof(T) == 4) return launch_group<T, 192>(list, starts, nprob, blocks, adj,
+                                                                pdl, s);
+      break;
+    default: break;
+  }
+  set_error("fused path does not cover P=%d for this dtype", P);
+  return JUBIK_ERR_UNSUPPORTED;
 }
 
 template <typename T>
@@ -1038,6 +1118,20 @@ size_t fused_smem_bytes(int P, int dtype) {
 
 int fused_run(const Geom& g, int dtype, const FusedLaunch& a, int which, cudaStream_t s) {
   return dtype == JUBIK_F32 ? dispatch<float>(g, a, which, s) : dispatch<double>(g, a, which, s);
+}
+
+size_t fused_args_size() { return sizeof(Args); }
+
+void fused_args_fill(const Geom& g, int dtype, const FusedLaunch& f, int which, void* dst) {
+  const Args a = make_args(g, f, which, dtype == JUBIK_F32 ? sizeof(float) : sizeof(double));
+  memcpy(dst, &a, sizeof(Args));
+}
+
+int fused_group_run(int P, int dtype, const void* list, const int* starts, int nprob,
+                    int64_t blocks, bool adj, bool pdl, cudaStream_t s) {
+  return dtype == JUBIK_F32
+             ? dispatch_group<float>(P, list, starts, nprob, blocks, adj, pdl, s)
+             : dispatch_group<double>(P, list, starts, nprob, blocks, adj, pdl, s);
 }
 
 }  // namespace jubik

@@ -95,6 +95,36 @@ struct FusedLaunch {
   bool in_exp = false;
 };
 size_t fused_spec_bytes(const Geom& g, int dtype);
+// Grouped per-unit launches over independent problems of one FFT side: the
+// kernel-argument block of one problem's stage (fused_args_size() bytes,
+// written by fused_args_fill), and one launch of FUSED_FWD_UNITS (adj false)
+// or FUSED_ADJ_UNITS (adj true) over nprob problems, problem p owning blocks
+// [starts[p], starts[p + 1]) of `blocks` (list and starts in device memory).
+// Grouped likelihood pass and grouped clearing over independent problems.
+struct PoissonJob {
+  const void* conv;
+  const void* eps;
+  const int32_t* dimg;
+  int64_t npix;
+  void* lam;
+  void* resid;
+  double* partials;
+  unsigned int* counter;
+  double* energy;
+};
+struct ZeroJob {
+  void* ptr;
+  int64_t bytes;
+};
+int poisson_group_blocks(int64_t npix);
+int poisson_group_run(int dtype, const PoissonJob* jobs, const int* starts, int njobs,
+                      int64_t blocks, bool pdl, cudaStream_t s);
+int zero_group_run(const ZeroJob* jobs, const int* starts, int njobs, int64_t blocks, bool pdl,
+                   cudaStream_t s);
+size_t fused_args_size();
+void fused_args_fill(const Geom& g, int dtype, const FusedLaunch& f, int which, void* dst);
+int fused_group_run(int P, int dtype, const void* list, const int* starts, int nprob,
+                    int64_t blocks, bool adj, bool pdl, cudaStream_t s);
 enum FusedStage {
   FUSED_FWD_UNITS = 0,     // one kernel per unit, forward
   FUSED_ADJ_UNITS = 1,     // one kernel per unit, adjoint

@@ -476,8 +476,11 @@ struct Kahan {
   __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
-__device__ __forceinline__ void block_reduce2(double a, double b, double* partials,
-                                              unsigned int* counter, double* energy) {
+// Block sums of (a, b) into partials[bid]; the last of nblocks blocks to finish
+// sums the partials in a fixed order (deterministic) and writes a - b.
+__device__ __forceinline__ void block_reduce2_of(double a, double b, double* partials,
+                                                 unsigned int* counter, double* energy,
+                                                 unsigned int bid, unsigned int nblocks) {
   __shared__ double sa[kBlock], sb[kBlock];
   __shared__ bool last;
   sa[threadIdx.x] = a;
@@ -491,18 +494,18 @@ __device__ __forceinline__ void block_reduce2(double a, double b, double* partia
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    partials[2 * blockIdx.x] = sa[0];
-    partials[2 * blockIdx.x + 1] = sb[0];
+    partials[2 * bid] = sa[0];
+    partials[2 * bid + 1] = sb[0];
     __threadfence();
     const unsigned int done = atomicAdd(counter, 1u);
-    last = (done == gridDim.x - 1);
+    last = (done == nblocks - 1);
   }
   __syncthreads();
   if (!last) return;
   // the last block sums the block partials in a fixed order (deterministic)
   __threadfence();
   double p1 = 0.0, p2 = 0.0;
-  for (unsigned int i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
+  for (unsigned int i = threadIdx.x; i < nblocks; i += blockDim.x) {
     p1 += __ldcg(partials + 2 * i);
     p2 += __ldcg(partials + 2 * i + 1);
   }
@@ -521,6 +524,11 @@ __device__ __forceinline__ void block_reduce2(double a, double b, double* partia
     if (energy) energy[0] = sa[0] - sb[0];
     *counter = 0u;
   }
+}
+
+__device__ __forceinline__ void block_reduce2(double a, double b, double* partials,
+                                              unsigned int* counter, double* energy) {
+  block_reduce2_of(a, b, partials, counter, energy, blockIdx.x, gridDim.x);
 }
 
 // One pass over the (M,E,nx,ny) images: lam = eps * conv where a pixel is read
@@ -542,18 +550,17 @@ __device__ __forceinline__ void poisson_px(T conv, T ep, int32_t d, T& lam_o, T&
   res_o = ep * ((T)1 - dd / lam);
 }
 
+// One problem's pass over its (M,E,nx,ny) images by block bid of nblocks.
 template <typename T>
-__global__ void __launch_bounds__(kBlock)
-    k_poisson_image(const T* __restrict__ conv, const T* __restrict__ eps,
-                    const int32_t* __restrict__ dimg, int64_t npix, T* __restrict__ lam_cache,
-                    T* __restrict__ resid, double* partials, unsigned int* counter,
-                    double* energy) {
-  // launched with programmatic stream serialisation after the forward kernels:
-  // let the adjoint be scheduled early, wait for the forward image
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  asm volatile("griddepcontrol.wait;" ::: "memory");
+__device__ __forceinline__ void poisson_image_body(const T* __restrict__ conv,
+                                                   const T* __restrict__ eps,
+                                                   const int32_t* __restrict__ dimg, int64_t npix,
+                                                   T* __restrict__ lam_cache, T* __restrict__ resid,
+                                                   double* partials, unsigned int* counter,
+                                                   double* energy, unsigned int bid,
+                                                   unsigned int nblocks) {
   Kahan<T> s_lam, s_dlog;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t stride = (int64_t)nblocks * blockDim.x;
   int64_t p0 = 0;
   if constexpr (sizeof(T) == 4) {
     // 4 pixels per thread with 16-byte accesses (all image bases are 16-byte aligned)
@@ -570,7 +577,7 @@ __global__ void __launch_bounds__(kBlock)
       if (resid) reinterpret_cast<float4*>(resid)[g] = r;
       if (lam_cache) __stcs(reinterpret_cast<float4*>(lam_cache) + g, l);
     };
-    int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t g = bid * (int64_t)blockDim.x + threadIdx.x;
     for (; g + stride < n4; g += 2 * stride) {
       const float4 ca = __ldcs(c4 + g), cb = __ldcs(c4 + g + stride);
       const float4 ea = eps ? __ldcs(e4 + g) : make_float4(1, 1, 1, 1);
@@ -582,13 +589,83 @@ __global__ void __launch_bounds__(kBlock)
     if (g < n4) px4(g, __ldcs(c4 + g), eps ? __ldcs(e4 + g) : make_float4(1, 1, 1, 1), __ldcs(d4 + g));
     p0 = n4 * 4;
   }
-  for (int64_t p = p0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npix; p += stride) {
+  for (int64_t p = p0 + bid * (int64_t)blockDim.x + threadIdx.x; p < npix; p += stride) {
     T l, r;
     poisson_px<T>(conv[p], eps ? eps[p] : (T)1, dimg[p], l, r, s_lam, s_dlog);
     if (resid) resid[p] = r;
     if (lam_cache) lam_cache[p] = l;
   }
-  block_reduce2(s_lam.value(), s_dlog.value(), partials, counter, energy);
+  block_reduce2_of(s_lam.value(), s_dlog.value(), partials, counter, energy, bid, nblocks);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock)
+    k_poisson_image(const T* __restrict__ conv, const T* __restrict__ eps,
+                    const int32_t* __restrict__ dimg, int64_t npix, T* __restrict__ lam_cache,
+                    T* __restrict__ resid, double* partials, unsigned int* counter,
+                    double* energy) {
+  // launched with programmatic stream serialisation after the forward kernels:
+  // let the adjoint be scheduled early, wait for the forward image
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  poisson_image_body<T>(conv, eps, dimg, npix, lam_cache, resid, partials, counter, energy,
+                        blockIdx.x, gridDim.x);
+}
+
+// Grouped launch: job j (one problem) owns blocks [starts[j], starts[j + 1]).
+template <typename T>
+__global__ void __launch_bounds__(kBlock)
+    k_poisson_group(const PoissonJob* __restrict__ jobs, const int* __restrict__ starts,
+                    int njobs) {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  __shared__ int s_job;
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (starts[mid] <= (int)blockIdx.x)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    s_job = lo;
+  }
+  __syncthreads();
+  const PoissonJob jb = jobs[s_job];
+  poisson_image_body<T>((const T*)jb.conv, (const T*)jb.eps, jb.dimg, jb.npix, (T*)jb.lam,
+                        (T*)jb.resid, jb.partials, jb.counter, jb.energy,
+                        blockIdx.x - starts[s_job], starts[s_job + 1] - starts[s_job]);
+}
+
+// Grouped clearing: job j owns blocks [starts[j], starts[j + 1]) and clears its
+// buffer in 16-byte stores (all plan and batch buffers are 256-byte aligned).
+__global__ void k_zero_group(const ZeroJob* __restrict__ jobs, const int* __restrict__ starts,
+                             int njobs) {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  __shared__ int s_job;
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (starts[mid] <= (int)blockIdx.x)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    s_job = lo;
+  }
+  __syncthreads();
+  const ZeroJob jb = jobs[s_job];
+  const int64_t nb = starts[s_job + 1] - starts[s_job], b = blockIdx.x - starts[s_job];
+  const int64_t n16 = jb.bytes >> 4;
+  float4* q = reinterpret_cast<float4*>(jb.ptr);
+  for (int64_t i = b * blockDim.x + threadIdx.x; i < n16; i += nb * blockDim.x)
+    q[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  unsigned char* c = static_cast<unsigned char*>(jb.ptr);
+  for (int64_t i = (n16 << 4) + b * blockDim.x + threadIdx.x; i < jb.bytes; i += nb * blockDim.x)
+    c[i] = 0;
 }
 
 // Count image: d[ridx[p]] where the pixel is read out, -1 elsewhere.
@@ -649,6 +726,46 @@ __global__ void k_elementwise(int op, const T* __restrict__ a, const T* __restri
 }  // namespace
 
 int energy_partials_count() { return kRedBlocks; }
+
+// blocks a grouped likelihood pass gives a problem of npix pixels
+int poisson_group_blocks(int64_t npix) {
+  const int64_t b = (npix + (int64_t)kBlock * 16 - 1) / ((int64_t)kBlock * 16);
+  return (int)(b < 1 ? 1 : (b > kRedBlocks ? kRedBlocks : b));
+}
+
+int poisson_group_run(int dtype, const PoissonJob* jobs, const int* starts, int njobs,
+                      int64_t blocks, bool pdl, cudaStream_t s) {
+  if (blocks <= 0) return JUBIK_OK;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)blocks);
+  cfg.blockDim = dim3(kBlock);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cuda_status(dtype == JUBIK_F32
+                         ? cudaLaunchKernelEx(&cfg, k_poisson_group<float>, jobs, starts, njobs)
+                         : cudaLaunchKernelEx(&cfg, k_poisson_group<double>, jobs, starts, njobs),
+                     "k_poisson_group");
+}
+
+int zero_group_run(const ZeroJob* jobs, const int* starts, int njobs, int64_t blocks, bool pdl,
+                   cudaStream_t s) {
+  if (blocks <= 0) return JUBIK_OK;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)blocks);
+  cfg.blockDim = dim3(kBlock);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cuda_status(cudaLaunchKernelEx(&cfg, k_zero_group, jobs, starts, njobs),
+                     "k_zero_group");
+}
 
 // --------------------------------------------------------------- host wrappers
 template <typename T>

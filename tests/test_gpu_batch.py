@@ -90,3 +90,50 @@ def test_batch_autotune_picks_a_covering_path(cuda, small_batch):
             assert abs(float(e[k]) - r["energy"]) / abs(r["energy"]) < 1e-6
     finally:
         b.close()
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32], ids=["f64", "f32"])
+def test_grouped_launches_match_per_problem(cuda, small_batch, dtype):
+    """One grouped launch per stage and FFT side gives the per-problem results,
+    eagerly and captured in a graph."""
+    insts, refs = small_batch
+    b = ju.ProblemBatch(insts, dtype=dtype, n_streams=2)
+    try:
+        b.set_data([r["data"] for r in refs])
+        e0, g0 = b.energy_and_grad()
+        torch.cuda.synchronize()
+        e0 = e0.clone()
+        g0 = [t.clone() for t in g0]
+        assert b.group()
+        sides = {2 * (i.shape[0] // i.n_patches) + 2 * i.margin for i in insts}
+        assert b.launches_per_pass() == 2 + 2 * len(sides) < 5 * len(insts)
+        etol = 1e-13 if dtype == torch.float64 else 1e-9
+        gtol = 1e-13 if dtype == torch.float64 else 2e-5
+        for run in ("eager", "graph", "graph again"):
+            if run == "graph":
+                b.capture()
+            for t in b.grad:
+                t.fill_(float("nan"))  # the grouped pass clears and fills every gradient
+            e, g = b.replay() if run.startswith("graph") else b.energy_and_grad()
+            torch.cuda.synchronize()
+            for k, r in enumerate(refs):
+                assert abs(float(e[k]) - float(e0[k])) <= etol * abs(float(e0[k])), (run, k)
+                assert rel(g[k], g0[k].double().cpu().numpy()) < gtol, (run, k)
+                assert abs(float(e[k]) - r["energy"]) / abs(r["energy"]) < (
+                    1e-12 if dtype == torch.float64 else 1e-6)
+    finally:
+        b.close()
+
+
+def test_group_refuses_module_shared_plans(cuda):
+    inst = synthetic.config2(nx=64, dx=16, margin=8, n_modules=2, n_energies=1)
+    b = ju.ProblemBatch([inst], dtype=torch.float32)
+    try:
+        lam = b.expected_counts()
+        b.set_data([synthetic.poisson_data(lam[0], 1)])
+        assert not b.group()      # two modules: the module-shared kernels
+        assert not b.grouped
+        e, _ = b.energy_and_grad()
+        assert np.isfinite(float(e[0]))
+    finally:
+        b.close()
