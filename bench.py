@@ -236,6 +236,51 @@ def uneven_batch_leg(dev, n_streams=8, passes=10):
 
 
 # ------------------------------------------------------------------ GPU leg
+def sky_model_leg(plan, dev, nx, E, mpix, reps=20):
+    """The diffuse sky model in front of the response: two correlated fields
+    (spatial, spectral index) on the padded grid good_fft_size(1.1075 nx)^2
+    (the demos' s_padding_ratio), the log-sky of E energy bins cropped to
+    nx^2, and the Poisson energy and gradient back to the excitations."""
+    import torch
+
+    from jubik_gb300 import sky as jsky
+    shape = (jsky.good_fft_size(int(nx * 1.1075)),) * 2
+    e_min = np.geomspace(0.2, 2.0, E)
+    coef = jsky.diffuse_coefficients(e_min, 2.0 * e_min, 1.0)
+    sky = jsky.CorrelatedFieldSky(shape, 1.0, n_fields=2, crop=(nx, nx), coefficients=coef,
+                                  dtype=torch.float32, device=dev)
+    rng = np.random.default_rng(12)
+    k = sky.mode_lengths / sky.mode_lengths[-1]
+    base = (1 + (k / 0.05) ** 2) ** -1.0 * 8 / np.sqrt(sky.pindex.size)
+    amp = torch.as_tensor(np.stack([0.4 * base, 0.05 * base]), dtype=torch.float32, device=dev)
+    xi = torch.as_tensor(rng.standard_normal((2,) + shape), dtype=torch.float32, device=dev)
+    off = torch.tensor([0.3, -0.2], dtype=torch.float32, device=dev)
+    ls = sky.logsky(amp, xi, off)
+    g = torch.randn_like(ls)
+    stream = torch.cuda.current_stream(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(reps):
+            fn()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / reps
+
+    out = {"padded_grid": list(shape), "fields": 2, "energies": E, "modes": sky.n_modes,
+           "logsky_ms": timed(lambda: sky.logsky(amp, xi, off, out=ls)),
+           "vjp_ms": timed(lambda: sky.vjp(amp, xi, g_logsky=g)),
+           "response_energy_grad_ms": timed(lambda: plan.energy_and_grad_logsky(ls)),
+           "chain_energy_grad_ms": timed(lambda: sky.energy_and_grad(plan, amp, xi, off))}
+    out["chain_mpix_s"] = mpix / (out["chain_energy_grad_ms"] / 1e3)
+    sky.close()
+    return out
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -480,6 +525,7 @@ def main():
             comp[name] = {"ms": t, "mpix_s": mpix / (t / 1e3)}
         line["operators"] = comp
         line["uneven_batch"] = uneven_batch_leg(dev)
+        line["sky_model"] = sky_model_leg(plan, dev, nx, E, mpix)
         line["rel_err_vs_fp64_gpu"] = err
         line["fp64_plain_ms_per_step"] = fp64_ms
         line["speedup_vs_fp64_plain"] = fp64_ms / ms

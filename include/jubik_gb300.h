@@ -240,6 +240,37 @@ JUBIK_API int jubik_group_energy_grad(jubik_group* group, void* stream);
 JUBIK_API int jubik_group_launches(const jubik_group* group, int32_t* launches);
 JUBIK_API int jubik_group_destroy(jubik_group* group);
 
+/* Correlated-field log-sky: the field-sized work of J-UBIK's diffuse sky
+ * model (jubik/sky_models.py:205-225 and :306-341; the fields come from
+ * NIFTy.re's CorrelatedFieldMaker, whose amplitude spectrum -- a 1-D function
+ * of a few scalars -- the caller computes).  On a padded s0 x s1 grid,
+ *     field_b = offsets[b] + hartley(amp[b][pindex] * xi[b]),
+ *     hartley(p) = Re(fftn(p)) + Im(fftn(p)),
+ * for n_fields <= 4 fields sharing one mode-length index pindex (s0 * s1
+ * int32 values in [0, n_modes), host memory, copied at creation).  The
+ * J-UBIK log-sky (spatial field plus spectral index times the log energy-bin
+ * centres, _apply_slope at sky_models.py:593-602, cropped as at :340) is
+ *     logsky[e][y][x] = sum_b ecoef[e * n_fields + b] * field_b[y][x],
+ *     y < nx, x < ny, E <= 32 (ecoef: host doubles).
+ * Device arrays in the cf's dtype: amp (n_fields, n_modes), xi and fields
+ * (n_fields, s0, s1), offsets (n_fields), logsky (E, nx, ny). */
+typedef struct jubik_cf jubik_cf;
+JUBIK_API int jubik_cf_create(int32_t n_fields, int32_t s0, int32_t s1, const int32_t* pindex,
+                              int32_t n_modes, int32_t dtype, jubik_cf** out);
+/* fields and/or logsky (either may be NULL, not both; logsky needs ecoef). */
+JUBIK_API int jubik_cf_apply(jubik_cf* cf, const void* amp, const void* xi, const void* offsets,
+                             void* fields, const double* ecoef, int32_t E, int32_t nx, int32_t ny,
+                             void* logsky, void* stream);
+/* Vector-Jacobian product for one cotangent: g_fields (n_fields, s0, s1), or
+ * g_logsky (E, nx, ny) with ecoef (pass NULL for the other).  Writes dxi
+ * (n_fields, s0, s1), damp (n_fields, n_modes) and doffsets (n_fields);
+ * deterministic (no atomics). */
+JUBIK_API int jubik_cf_vjp(jubik_cf* cf, const void* amp, const void* xi, const void* g_fields,
+                           const double* ecoef, int32_t E, int32_t nx, int32_t ny,
+                           const void* g_logsky, void* dxi, void* damp, void* doffsets,
+                           void* stream);
+JUBIK_API int jubik_cf_destroy(jubik_cf* cf);
+
 /* Sampling and global reductions for the callers of the response.
  * Random numbers: counter-based Philox4x32-10 (Salmon et al., SC'11) keyed by
  * `seed`; element i of a call uses its own counter, so results do not depend

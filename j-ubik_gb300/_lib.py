@@ -93,6 +93,11 @@ _SIGS = {
     "jubik_poisson_energy_grad_logsky": ([_vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp], C.c_int),
     "jubik_psf_interpolate": ([_vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32,
                                _dbl, _dbl, _i32, _i32, _i32, _vp, _vp], C.c_int),
+    "jubik_cf_create": ([_i32, _i32, _i32, _vp, _i32, _i32, _vp], C.c_int),
+    "jubik_cf_apply": ([_vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp], C.c_int),
+    "jubik_cf_vjp": ([_vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp],
+                     C.c_int),
+    "jubik_cf_destroy": ([_vp], C.c_int),
 }
 
 _lib = None

@@ -1,5 +1,5 @@
-// Register-resident small DFTs (sizes 1, 2, 3, 4, 5, 6, 8, 10, 12, 16, 20, 24,
-// 32) in natural order, fully unrolled at compile time.  Composite sizes use one level of
+// Register-resident small DFTs (sizes 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12,
+// 16, 20, 24, 32) in natural order, fully unrolled at compile time.  Composite sizes use one level of
 // Cooley-Tukey, N = N1 * N2 with n = N2*n1 + n2 and k = k1 + N1*k2:
 //   X[k1 + N1 k2] = sum_n2 w_N2^(n2 k2) w_N^(n2 k1) sum_n1 x[N2 n1 + n2] w_N1^(n1 k1)
 #pragma once
@@ -86,6 +86,90 @@ template <bool INV, typename T> struct Dft<5, INV, T> {
       v[3] = cadd<T>(a2, cmul_i<T>(b2));
     }
   }
+};
+
+// Odd N (7, 9, 11), direct: with t_q = x_q + x_{N-q}, u_q = x_q - x_{N-q},
+//   X_k, X_{N-k} = x_0 + sum_q cos(2 pi q k / N) t_q -/+ i sum_q sin(2 pi q k / N) u_q,
+// q, k = 1 .. (N - 1) / 2 (the inverse flips the i terms).  odd_cos / odd_sin
+// hold cos and sin of 2 pi m / N for m = 0 .. (N - 1) / 2 to 25 digits (m = 0
+// occurs for composite N: q k = 9 for N = 9).
+__host__ __device__ constexpr double odd_cos(int N, int m) {
+  if (m == 0) return 1.0;
+  switch (N * 16 + m) {
+    case 7 * 16 + 1: return 0.6234898018587335305250049;
+    case 7 * 16 + 2: return -0.2225209339563144042889026;
+    case 7 * 16 + 3: return -0.9009688679024191262361023;
+    case 9 * 16 + 1: return 0.7660444431189780352023926;
+    case 9 * 16 + 2: return 0.1736481776669303488517166;
+    case 9 * 16 + 3: return -0.5;
+    case 9 * 16 + 4: return -0.9396926207859083840541093;
+    case 11 * 16 + 1: return 0.8412535328311811688618117;
+    case 11 * 16 + 2: return 0.4154150130018864255292741;
+    case 11 * 16 + 3: return -0.1423148382732851404437927;
+    case 11 * 16 + 4: return -0.6548607339452850640569251;
+    case 11 * 16 + 5: return -0.9594929736144973898903681;
+    default: return 0.0;
+  }
+}
+__host__ __device__ constexpr double odd_sin(int N, int m) {
+  switch (N * 16 + m) {
+    case 7 * 16 + 1: return 0.7818314824680298087084445;
+    case 7 * 16 + 2: return 0.9749279121818236070181317;
+    case 7 * 16 + 3: return 0.4338837391175581204757683;
+    case 9 * 16 + 1: return 0.6427876096865393263226434;
+    case 9 * 16 + 2: return 0.9848077530122080593667430;
+    case 9 * 16 + 3: return 0.8660254037844386467637232;
+    case 9 * 16 + 4: return 0.3420201433256687330440996;
+    case 11 * 16 + 1: return 0.5406408174555975821076360;
+    case 11 * 16 + 2: return 0.9096319953545183714117154;
+    case 11 * 16 + 3: return 0.9898214418809327323760920;
+    case 11 * 16 + 4: return 0.7557495743542582837740358;
+    case 11 * 16 + 5: return 0.2817325568414296977114179;
+    default: return 0.0;
+  }
+}
+
+template <int N, bool INV, typename T>
+__device__ __forceinline__ void dft_odd(cx<T>* v) {
+  constexpr int H = (N - 1) / 2;
+  cx<T> t[H], u[H];
+  const cx<T> x0 = v[0];
+  cx<T> sum = x0;
+  sfor<H>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    t[q] = cadd<T>(v[q + 1], v[N - 1 - q]);
+    u[q] = csub<T>(v[q + 1], v[N - 1 - q]);
+    sum = cadd<T>(sum, t[q]);
+  });
+  sfor<H>([&](auto kc) {
+    constexpr int k = decltype(kc)::value + 1;
+    cx<T> a = x0, b = mkc<T>((T)0, (T)0);
+    sfor<H>([&](auto qc) {
+      constexpr int q = decltype(qc)::value + 1;
+      constexpr int m = (q * k) % N;
+      constexpr T c = (T)odd_cos(N, m <= H ? m : N - m);
+      constexpr T sn = (T)(m <= H ? odd_sin(N, m) : -odd_sin(N, N - m));
+      a = mkc<T>(a.x + c * t[q - 1].x, a.y + c * t[q - 1].y);
+      b = mkc<T>(b.x + sn * u[q - 1].x, b.y + sn * u[q - 1].y);
+    });
+    if (INV) {
+      v[k] = cadd<T>(a, cmul_i<T>(b));
+      v[N - k] = csub<T>(a, cmul_i<T>(b));
+    } else {
+      v[k] = csub<T>(a, cmul_i<T>(b));
+      v[N - k] = cadd<T>(a, cmul_i<T>(b));
+    }
+  });
+  v[0] = sum;
+}
+template <bool INV, typename T> struct Dft<7, INV, T> {
+  __device__ __forceinline__ static void run(cx<T>* v) { dft_odd<7, INV, T>(v); }
+};
+template <bool INV, typename T> struct Dft<9, INV, T> {
+  __device__ __forceinline__ static void run(cx<T>* v) { dft_odd<9, INV, T>(v); }
+};
+template <bool INV, typename T> struct Dft<11, INV, T> {
+  __device__ __forceinline__ static void run(cx<T>* v) { dft_odd<11, INV, T>(v); }
 };
 
 template <int N1, int N2, bool INV, typename T>

@@ -119,6 +119,11 @@ __global__ void __launch_bounds__(kThreads)
         case 2: bfly<2, T>(src, dst, j, Lr, Ns, tstep, tw, inv); break;
         case 3: bfly<3, T>(src, dst, j, Lr, Ns, tstep, tw, inv); break;
         case 4: bfly<4, T>(src, dst, j, Lr, Ns, tstep, tw, inv); break;
+        case 5: bfly<5, T>(src, dst, j, Lr, Ns, tstep, tw, inv); break;
+        case 7: bfly<7, T>(src, dst, j, Lr, Ns, tstep, tw, inv); break;
+        case 8: bfly<8, T>(src, dst, j, Lr, Ns, tstep, tw, inv); break;
+        case 9: bfly<9, T>(src, dst, j, Lr, Ns, tstep, tw, inv); break;
+        case 11: bfly<11, T>(src, dst, j, Lr, Ns, tstep, tw, inv); break;
         default: bfly_generic<T>(src, dst, j, L, r, Ns, tw, inv); break;
       }
     }
@@ -280,6 +285,11 @@ bool factorize(int L, FftStages* st) {
     st->r[st->n++] = r;
     return true;
   };
+  // larger register codelets first: fewer passes through shared memory
+  while (rem % 8 == 0) {
+    if (!push(8)) return false;
+    rem /= 8;
+  }
   while (rem % 4 == 0) {
     if (!push(4)) return false;
     rem /= 4;
@@ -287,6 +297,10 @@ bool factorize(int L, FftStages* st) {
   while (rem % 2 == 0) {
     if (!push(2)) return false;
     rem /= 2;
+  }
+  while (rem % 9 == 0) {
+    if (!push(9)) return false;
+    rem /= 9;
   }
   while (rem % 3 == 0) {
     if (!push(3)) return false;
