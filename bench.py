@@ -55,6 +55,9 @@ def parse():
                     help="skip the FP64 comparison and the CPU baseline")
     ap.add_argument("--profile-only", action="store_true",
                     help="one warm-up and two steps (for a launch list under a profiler)")
+    ap.add_argument("--leg", choices=["step", "sky", "batch"], default="step",
+                    help="with --profile-only: the response step, the correlated-field sky "
+                         "(log-sky and VJP), or the grouped uneven batch")
     return ap.parse_args()
 
 
@@ -281,6 +284,46 @@ def sky_model_leg(plan, dev, nx, E, mpix, reps=20):
     return out
 
 
+def profile_sky_leg(dev, nx, E, passes=3):
+    """Log-sky and VJP of the sky-model leg, ``passes`` times (for ncu)."""
+    import torch
+
+    from jubik_gb300 import sky as jsky
+    shape = (jsky.good_fft_size(int(nx * 1.1075)),) * 2
+    e_min = np.geomspace(0.2, 2.0, E)
+    sky = jsky.CorrelatedFieldSky(shape, 1.0, n_fields=2, crop=(nx, nx),
+                                  coefficients=jsky.diffuse_coefficients(e_min, 2 * e_min, 1.0),
+                                  dtype=torch.float32, device=dev)
+    amp = torch.rand(2, sky.n_modes, device=dev) * 1e-3
+    xi = torch.randn((2,) + shape, device=dev)
+    off = torch.zeros(2, device=dev)
+    ls = sky.logsky(amp, xi, off)
+    g = torch.randn_like(ls)
+    for _ in range(passes):
+        sky.logsky(amp, xi, off, out=ls)
+        sky.vjp(amp, xi, g_logsky=g)
+    torch.cuda.synchronize()
+    sky.close()
+
+
+def profile_batch_leg(dev, passes=3):
+    """The grouped pass over the config-5 uneven batch, ``passes`` times (for ncu)."""
+    import torch
+
+    import jubik_gb300 as ju
+    from jubik_gb300 import synthetic
+    insts = synthetic.config5()
+    b = ju.ProblemBatch(insts, dtype=torch.float32, device=dev,
+                        paths={32: "fused_unit", 64: "fused_unit", 128: "fused_unit"})
+    b.set_data([synthetic.poisson_data(l, 1) for l in b.expected_counts()])
+    if not b.group():
+        raise RuntimeError("the config-5 batch did not group")
+    for _ in range(passes):
+        b.energy_and_grad()
+    torch.cuda.synchronize()
+    b.close()
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -319,12 +362,17 @@ def main():
         plan.energy_and_grad(x, need_grad=True, energy=energy, grad=grad)
 
     if args.profile_only:
-        step()
-        step()
-        step()
+        if args.leg == "sky":
+            profile_sky_leg(dev, nx, E)
+        elif args.leg == "batch":
+            profile_batch_leg(dev)
+        else:
+            step()
+            step()
+            step()
         torch.cuda.synchronize()
         if rank == 0:
-            print(json.dumps({"profile_only": True, "path": plan.path}))
+            print(json.dumps({"profile_only": True, "leg": args.leg, "path": plan.path}))
         return
 
     index = os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[local if world > 1
