@@ -254,9 +254,10 @@ __device__ __forceinline__ void stage_input(Unit<T, P>& U, const Args& a) {
   const int jhi = ADJ ? H : (mg + K + 1) / 2;
   const int nchunks = (jhi - jlo + CH - 1) / CH;
   const int nzero = H - (jhi - jlo);
-  // second buffer: adjoint with 3 chunks -> the last chunk's tile pairs;
+  // second buffer: adjoint with 3 full chunks -> the last chunk's tile pairs
+  // [2 CH, 3 CH) (a short last chunk, as for P = 160, leaves too few);
   // forward with 2 chunks -> the zero pairs outside the window rows
-  const bool db = ADJ ? (nchunks == 3) : (nchunks == 2 && nzero >= CH);
+  const bool db = ADJ ? (nchunks == 3 && 3 * CH <= H) : (nchunks == 2 && nzero >= CH);
   auto alt_pair = [&](int jj) -> int {  // tile pair holding row-pair jj of the odd chunk
     if (ADJ) return 2 * CH + jj;
     return jj < jlo ? jj : jhi + (jj - jlo);
@@ -1069,6 +1070,10 @@ int dispatch_group(int P, const void* list, const int* starts, int nprob, int64_
     case 64: return launch_group<T, 64>(list, starts, nprob, blocks, adj, pdl, s);
     case 96: return launch_group<T, 96>(list, starts, nprob, blocks, adj, pdl, s);
     case 128: return launch_group<T, 128>(list, starts, nprob, blocks, adj, pdl, s);
+    case 160:
+      if constexpr (sizeof(T) == 4) return launch_group<T, 160>(list, starts, nprob, blocks, adj,
+                                                                pdl, s);
+      break;
     case 192:
       if constexpr (sizeof(T) == 4) return launch_group<T, 192>(list, starts, nprob, blocks, adj,
                                                                 pdl, s);
@@ -1086,6 +1091,9 @@ int dispatch(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
     case 64: return launch_one<T, 64>(g, f, which, s);
     case 96: return launch_one<T, 96>(g, f, which, s);
     case 128: return launch_one<T, 128>(g, f, which, s);
+    case 160:
+      if constexpr (sizeof(T) == 4) return launch_one<T, 160>(g, f, which, s);
+      break;
     case 192:
       if constexpr (sizeof(T) == 4) return launch_one<T, 192>(g, f, which, s);
       break;
@@ -1100,7 +1108,7 @@ int dispatch(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
 bool fused_supported(int P, int dtype) {
   switch (P) {
     case 32: case 64: case 96: case 128: return true;
-    case 192: return dtype == JUBIK_F32;
+    case 160: case 192: return dtype == JUBIK_F32;
     default: return false;
   }
 }

@@ -30,7 +30,8 @@ def rel(a, b):
 CASES = [(48, 4, 4, 1, 1), (64, 8, 8, 1, 1), (64, 16, 8, 2, 2), (64, 16, 16, 1, 2),
          (96, 32, 16, 2, 1), (128, 32, 32, 1, 1), (256, 64, 32, 2, 2),
          (64, 16, 24, 1, 1), (36, 2, 2, 1, 2), (60, 20, 5, 1, 1),
-         (32, 32, 8, 1, 1), (64, 32, 16, 2, 2)]  # one patch (P = 80), 2 x 2 patches
+         (32, 32, 8, 1, 1), (64, 32, 16, 2, 2),  # one patch (P = 80), 2 x 2 patches
+         (256, 64, 16, 2, 2), (160, 32, 48, 1, 1)]  # P = 160 (FP32 fused)
 
 
 @pytest.fixture(scope="module")
