@@ -31,6 +31,9 @@ def test_info_calls_need_no_gpu():
     assert lib.jubik_fused_supported(192, _lib.F32) == 1
     assert lib.jubik_fused_supported(192, _lib.F64) == 0
     assert lib.jubik_fused_supported(80, _lib.F32) == 0
+    assert lib.jubik_fused_supported(160, _lib.F32) == 1
+    assert lib.jubik_fused_supported(160, _lib.F64) == 0
+    assert lib.jubik_fft_length_supported(1134) == 1  # 2 . 9 . 9 . 7
     assert lib.jubik_fft_length_supported(96) == 1
     assert lib.jubik_fft_length_supported(131) == 0  # prime > 64
 
@@ -58,3 +61,33 @@ def test_invalid_plan_descriptions_fail_without_touching_the_gpu():
 def test_header_parser_finds_declarations():
     names = _lib.header_symbols()
     assert "jubik_poisson_energy_grad" in names and "jubik_plan_create" in names
+
+
+@pytest.mark.skipif(not _built(), reason="library not built")
+def test_group_and_cf_argument_errors_without_a_gpu():
+    """Argument checks of the grouped-launch and correlated-field entries run
+    before any CUDA call."""
+    lib = _lib.load()
+    g = ctypes.c_void_p()
+    assert lib.jubik_group_create(None, 0, ctypes.byref(g)) == _lib.ERR_INVALID_ARGUMENT
+    plans = (ctypes.c_void_p * 2)(None, None)
+    assert lib.jubik_group_create(plans, 2, ctypes.byref(g)) == _lib.ERR_INVALID_ARGUMENT
+    assert "NULL" in _lib.last_error()
+    cf = ctypes.c_void_p()
+    pidx = (ctypes.c_int32 * 16)(*([0] * 15 + [3]))
+    # pindex value outside [0, n_modes)
+    assert lib.jubik_cf_create(1, 4, 4, pidx, 3, _lib.F32, ctypes.byref(cf)) == \
+        _lib.ERR_INVALID_ARGUMENT
+    assert "pindex" in _lib.last_error()
+    # five fields (at most four), a bad dtype, a prime factor above the FFT radix limit
+    assert lib.jubik_cf_create(5, 4, 4, pidx, 4, _lib.F32, ctypes.byref(cf)) == \
+        _lib.ERR_INVALID_ARGUMENT
+    assert lib.jubik_cf_create(1, 4, 4, pidx, 4, 9, ctypes.byref(cf)) == \
+        _lib.ERR_INVALID_ARGUMENT
+    big = (ctypes.c_int32 * (4 * 67))()
+    assert lib.jubik_cf_create(1, 4, 67, big, 1, _lib.F32, ctypes.byref(cf)) == \
+        _lib.ERR_UNSUPPORTED
+    assert cf.value is None
+    assert lib.jubik_cf_apply(None, None, None, None, None, None, 0, 0, 0, None, None) == \
+        _lib.ERR_INVALID_ARGUMENT
+    assert lib.jubik_cf_destroy(None) == _lib.OK
