@@ -31,6 +31,7 @@
 // (classes kappa and 16-kappa form closed slot sets), the inverse combine
 // into the first inverse row phase.
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 
 #include "fft_codelets.cuh"
@@ -199,6 +200,14 @@ struct Unit {
   // -> (m, e, k); per_module == false decodes (e, k) only
   __device__ __forceinline__ void init(const Args& a, unsigned char* smem, bool per_module,
                                        int ub = -1) {
+    geom(a, smem, per_module, ub);
+    twg = (const cx<T>*)a.tw;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) wq[q] = ldg2(twg + cls * q);
+  }
+  // everything but the twiddles (a loop over units keeps those)
+  __device__ __forceinline__ void geom(const Args& a, unsigned char* smem, bool per_module,
+                                       int ub) {
     tile = reinterpret_cast<cx<T>*>(smem);
     stg = tile + R::TILE;
     tid = threadIdx.x;
@@ -226,9 +235,6 @@ struct Unit {
     hnyq = (const cx<T>*)a.hnyq + hu * (int64_t)P;
     spec = a.spec ? (cx<T>*)a.spec + ((int64_t)e * n2p + k) * (int64_t)(P * R::H) : nullptr;
     wt = (const T*)a.wt;
-    twg = (const cx<T>*)a.tw;
-#pragma unroll
-    for (int q = 0; q < 16; ++q) wq[q] = ldg2(twg + cls * q);
   }
 };
 
@@ -244,27 +250,114 @@ __device__ __forceinline__ void cp_async_wait() {
 // current chunk does not write is free: the next chunk's loads then overlap
 // the current chunk's transform.  Buffers are pair rows of pitch TP: chunk c
 // uses the staging area (c even) or a tile region (c odd).
+// Chunk layout of the input stage: pair rows [jlo, jhi) in chunks of CH.
 template <typename T, int P, bool ADJ>
-__device__ __forceinline__ void stage_input(Unit<T, P>& U, const Args& a) {
+struct InChunks {
+  using R = Tr<T, P>;
+  int jlo, jhi, nchunks, nzero;
+  bool db;
+  __device__ __forceinline__ InChunks(const Unit<T, P>& U) {
+    constexpr int H = R::H, CH = R::CH;
+    jlo = ADJ ? 0 : U.mg / 2;
+    jhi = ADJ ? H : (U.mg + U.K + 1) / 2;
+    nchunks = (jhi - jlo + CH - 1) / CH;
+    nzero = H - (jhi - jlo);
+    // second buffer: adjoint with 3 full chunks -> the last chunk's tile pairs
+    // [2 CH, 3 CH) (a short last chunk, as for P = 160, leaves too few);
+    // forward with 2 chunks -> the zero pairs outside the window rows
+    db = ADJ ? (nchunks == 3 && 3 * CH <= H) : (nchunks == 2 && nzero >= CH);
+  }
+  // tile pair holding row-pair jj of the odd chunk
+  __device__ __forceinline__ int alt_pair(int jj) const {
+    if (ADJ) return 2 * R::CH + jj;
+    return jj < jlo ? jj : jhi + (jj - jlo);
+  }
+  __device__ __forceinline__ cx<T>* buf(const Unit<T, P>& U, int c, int jj) const {
+    return (db && (c & 1)) ? U.tile + alt_pair(jj) * R::TP : U.stg + jj * R::TP;
+  }
+};
+
+// cp.async of input chunk c (one commit group).  Chunk 0 goes to the staging
+// area, so a loop over units may issue the next unit's chunk 0 while the
+// current unit's later stages (which leave the staging area alone) run.
+template <typename T, int P, bool ADJ>
+__device__ __forceinline__ void input_issue(const Unit<T, P>& U, const Args& a,
+                                            const InChunks<T, P, ADJ>& ch, int c) {
+  using R = Tr<T, P>;
+  constexpr int NT = R::NT, CH = R::CH;
+  const int mg = U.mg, K = U.K;
+  const int xoff = ADJ ? 0 : mg;
+  const int width = ADJ ? P : K;
+  // forward input: element (row, col) of energy e at e * in_ps + row * in_rs + col
+  const int64_t rs = ADJ ? (int64_t)a.ny : a.in_rs;
+  const T* __restrict__ src =
+      (const T*)a.in + (ADJ ? ((int64_t)U.m * a.E + U.e) * U.npix : (int64_t)U.e * a.in_ps);
+  // adjoint units whose P x P window lies inside the field need no bounds checks
+  const bool interior = ADJ && U.rb >= 0 && U.rb + P <= a.nx && U.cb >= 0 && U.cb + P <= a.ny;
+  const int j0 = ch.jlo + c * CH;
+  const int nch = min(CH, ch.jhi - j0);
+  if (ADJ && interior && NT % width == 0) {
+    const int xs = U.tid % width, jstep = NT / width;
+    const T* gcol = src + (int64_t)U.rb * rs + U.cb + xs;
+    for (int jj = U.tid / width; jj < nch; jj += jstep) {
+      const T* g0 = gcol + (int64_t)(2 * (j0 + jj)) * rs;
+      T* d = reinterpret_cast<T*>(ch.buf(U, c, jj) + xs);
+      cp_async_in<T>(d, g0);
+      cp_async_in<T>(d + 1, g0 + rs);
+    }
+  } else if (NT % width == 0) {
+    // each thread owns one staged column and every (NT / width)-th pair row
+    const int xs = U.tid % width, jstep = NT / width;
+    const int col = U.cb + xoff + xs;
+    const bool cok = col >= 0 && col < a.ny;
+    const T* gcol = src + (cok ? col : 0);
+    for (int jj = U.tid / width; jj < nch; jj += jstep) {
+      const int y0 = 2 * (j0 + jj);
+      const int row = U.rb + y0;
+      const bool ok0 = cok && row >= 0 && row < a.nx && (ADJ || (y0 - mg >= 0 && y0 - mg < K));
+      const bool ok1 = cok && row + 1 >= 0 && row + 1 < a.nx &&
+                       (ADJ || (y0 + 1 - mg >= 0 && y0 + 1 - mg < K));
+      T* d = reinterpret_cast<T*>(ch.buf(U, c, jj) + xs);
+      cp_async<T>(d, ok0 ? gcol + (int64_t)row * rs : src, ok0);
+      cp_async<T>(d + 1, ok1 ? gcol + (int64_t)(row + 1) * rs : src, ok1);
+    }
+  } else {
+    for (int i = U.tid; i < nch * width; i += NT) {
+      const int jj = i / width, xs = i - jj * width;
+      const int col = U.cb + xoff + xs;
+      const int y0 = 2 * (j0 + jj);
+      const int row = U.rb + y0;
+      const bool cok = col >= 0 && col < a.ny;
+      const bool ok0 =
+          cok && row >= 0 && row < a.nx && (ADJ || (y0 - mg >= 0 && y0 - mg < K));
+      const bool ok1 = cok && row + 1 >= 0 && row + 1 < a.nx &&
+                       (ADJ || (y0 + 1 - mg >= 0 && y0 + 1 - mg < K));
+      T* d = reinterpret_cast<T*>(ch.buf(U, c, jj) + xs);
+      cp_async<T>(d, ok0 ? src + (int64_t)row * rs + col : src, ok0);
+      cp_async<T>(d + 1, ok1 ? src + (int64_t)(row + 1) * rs + col : src, ok1);
+    }
+  }
+  cp_async_commit();
+}
+
+// ---- input rows -> staging (cp.async) -> row step A (variant B forward)
+// forward: weighted sky window rows; adjoint: cotangent window rows.
+// Chunks of CH pairs are double-buffered when a part of the tile that the
+// current chunk does not write is free: the next chunk's loads then overlap
+// the current chunk's transform.  Buffers are pair rows of pitch TP: chunk c
+// uses the staging area (c even) or a tile region (c odd).  chunk0_issued:
+// input_issue(c = 0) already ran for this unit (and nothing was committed since).
+template <typename T, int P, bool ADJ>
+__device__ __forceinline__ void stage_input(Unit<T, P>& U, const Args& a,
+                                            bool chunk0_issued = false) {
   using R = Tr<T, P>;
   constexpr int L1 = R::L1, H = R::H, NT = R::NT, TP = R::TP, CH = R::CH;
   cx<T>* tile = U.tile;
   const int mg = U.mg, K = U.K;
-  const int jlo = ADJ ? 0 : mg / 2;
-  const int jhi = ADJ ? H : (mg + K + 1) / 2;
-  const int nchunks = (jhi - jlo + CH - 1) / CH;
-  const int nzero = H - (jhi - jlo);
-  // second buffer: adjoint with 3 full chunks -> the last chunk's tile pairs
-  // [2 CH, 3 CH) (a short last chunk, as for P = 160, leaves too few);
-  // forward with 2 chunks -> the zero pairs outside the window rows
-  const bool db = ADJ ? (nchunks == 3 && 3 * CH <= H) : (nchunks == 2 && nzero >= CH);
-  auto alt_pair = [&](int jj) -> int {  // tile pair holding row-pair jj of the odd chunk
-    if (ADJ) return 2 * CH + jj;
-    return jj < jlo ? jj : jhi + (jj - jlo);
-  };
-  auto bufp = [&](int c, int jj) -> cx<T>* {
-    return (db && (c & 1)) ? tile + alt_pair(jj) * TP : U.stg + jj * TP;
-  };
+  const InChunks<T, P, ADJ> ch(U);
+  const int jlo = ch.jlo, jhi = ch.jhi, nchunks = ch.nchunks, nzero = ch.nzero;
+  const bool db = ch.db;
+  auto bufp = [&](int c, int jj) -> cx<T>* { return ch.buf(U, c, jj); };
   const int xoff = ADJ ? 0 : mg;
   const int width = ADJ ? P : K;
   // column weights, zero outside the window and outside the field (where the
@@ -276,58 +369,7 @@ __device__ __forceinline__ void stage_input(Unit<T, P>& U, const Args& a) {
     const int col = U.cb + U.cls + L1 * q;
     wc[q] = (!ADJ && xa >= 0 && xa < K && col >= 0 && col < a.ny) ? U.wt[xa] : (T)0;
   }
-  // forward input: element (row, col) of energy e at e * in_ps + row * in_rs + col
-  const int64_t rs = ADJ ? (int64_t)a.ny : a.in_rs;
-  const T* __restrict__ src =
-      (const T*)a.in + (ADJ ? ((int64_t)U.m * a.E + U.e) * U.npix : (int64_t)U.e * a.in_ps);
-  // adjoint units whose P x P window lies inside the field need no bounds checks
-  const bool interior = ADJ && U.rb >= 0 && U.rb + P <= a.nx && U.cb >= 0 && U.cb + P <= a.ny;
-  auto issue = [&](int c) {
-    const int j0 = jlo + c * CH;
-    const int nch = min(CH, jhi - j0);
-    if (ADJ && interior && NT % width == 0) {
-      const int xs = U.tid % width, jstep = NT / width;
-      const T* gcol = src + (int64_t)U.rb * rs + U.cb + xs;
-      for (int jj = U.tid / width; jj < nch; jj += jstep) {
-        const T* g0 = gcol + (int64_t)(2 * (j0 + jj)) * rs;
-        T* d = reinterpret_cast<T*>(bufp(c, jj) + xs);
-        cp_async_in<T>(d, g0);
-        cp_async_in<T>(d + 1, g0 + rs);
-      }
-    } else if (NT % width == 0) {
-      // each thread owns one staged column and every (NT / width)-th pair row
-      const int xs = U.tid % width, jstep = NT / width;
-      const int col = U.cb + xoff + xs;
-      const bool cok = col >= 0 && col < a.ny;
-      const T* gcol = src + (cok ? col : 0);
-      for (int jj = U.tid / width; jj < nch; jj += jstep) {
-        const int y0 = 2 * (j0 + jj);
-        const int row = U.rb + y0;
-        const bool ok0 = cok && row >= 0 && row < a.nx && (ADJ || (y0 - mg >= 0 && y0 - mg < K));
-        const bool ok1 = cok && row + 1 >= 0 && row + 1 < a.nx &&
-                         (ADJ || (y0 + 1 - mg >= 0 && y0 + 1 - mg < K));
-        T* d = reinterpret_cast<T*>(bufp(c, jj) + xs);
-        cp_async<T>(d, ok0 ? gcol + (int64_t)row * rs : src, ok0);
-        cp_async<T>(d + 1, ok1 ? gcol + (int64_t)(row + 1) * rs : src, ok1);
-      }
-    } else {
-      for (int i = U.tid; i < nch * width; i += NT) {
-        const int jj = i / width, xs = i - jj * width;
-        const int col = U.cb + xoff + xs;
-        const int y0 = 2 * (j0 + jj);
-        const int row = U.rb + y0;
-        const bool cok = col >= 0 && col < a.ny;
-        const bool ok0 =
-            cok && row >= 0 && row < a.nx && (ADJ || (y0 - mg >= 0 && y0 - mg < K));
-        const bool ok1 = cok && row + 1 >= 0 && row + 1 < a.nx &&
-                         (ADJ || (y0 + 1 - mg >= 0 && y0 + 1 - mg < K));
-        T* d = reinterpret_cast<T*>(bufp(c, jj) + xs);
-        cp_async<T>(d, ok0 ? src + (int64_t)row * rs + col : src, ok0);
-        cp_async<T>(d + 1, ok1 ? src + (int64_t)(row + 1) * rs + col : src, ok1);
-      }
-    }
-    cp_async_commit();
-  };
+  auto issue = [&](int c) { input_issue<T, P, ADJ>(U, a, ch, c); };
   if (!ADJ && !db) {  // zero pairs outside the window rows (before step A writes)
     for (int i = U.tid; i < nzero * P; i += NT) {
       const int jj = i / P, sl = i - jj * P;
@@ -335,7 +377,7 @@ __device__ __forceinline__ void stage_input(Unit<T, P>& U, const Args& a) {
       tile[j * TP + sl] = mkc<T>((T)0, (T)0);
     }
   }
-  issue(0);
+  if (!chunk0_issued) issue(0);
   if (db && nchunks > 1) issue(1);
   for (int c = 0; c < nchunks; ++c) {
     const int j0 = jlo + c * CH;
@@ -867,45 +909,87 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_sky_spec(Args a) {
   stage_mid<T, P, MID_TO_SPEC, false>(U);
 }
 
-// ... then, per unit, spectrum * PSF spectrum -> inverse -> overlap-add.
+// ... then, per unit, spectrum * PSF spectrum -> inverse -> overlap-add, as a
+// loop over units (CTA b takes units b, b + G, ...; G = gridDim.x, one CTA per
+// SM).  The next unit's PSF and shared spectra are prefetched into L2 when this
+// unit's output stage starts: its reductions leave the HBM reads free, and the
+// data is in L2 when the next unit's spectrum stage reads it.  (Prefetching a
+// whole unit ahead was slower: the prefetches then compete with the current
+// unit's spectrum loads.)
 template <typename T, int P>
-__global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_from_spec(Args a) {
+__global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_from_spec(Args a, int units) {
   using R = Tr<T, P>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Unit<T, P> U;
   pdl_trigger();
-  U.init(a, smem_raw, true);
+  int u = blockIdx.x;
+  U.init(a, smem_raw, true, u);
   prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
   pdl_wait();
   if (threadIdx.x == 32) prefetch_l2(U.spec, sizeof(cx<T>) * P * R::H);
-  stage_mid<T, P, MID_FROM_SPEC, false>(U);
-  __syncthreads();
-  stage_invB<T, P, 0>(U, U.tid, R::NT);
-  __syncthreads();
-  stage_combine<T, P>(U, 0, R::H);
-  __syncthreads();
-  stage_output<T, P, false>(U, a);
+  for (;;) {
+    const int un = u + (int)gridDim.x;
+    stage_mid<T, P, MID_FROM_SPEC, false>(U);
+    __syncthreads();
+    stage_invB<T, P, 0>(U, U.tid, R::NT);
+    __syncthreads();
+    stage_combine<T, P>(U, 0, R::H);
+    __syncthreads();
+    if (un < units) {  // the output stage's reductions leave HBM reads free
+      Unit<T, P> N;
+      N.geom(a, smem_raw, true, un);
+      prefetch_unit(N.hmain, sizeof(cx<T>) * P * R::H, N.hnyq, sizeof(cx<T>) * P);
+      if (threadIdx.x == 32) prefetch_l2(N.spec, sizeof(cx<T>) * P * R::H);
+    }
+    stage_output<T, P, false>(U, a);
+    if (un >= units) break;
+    __syncthreads();  // the output stage's last staging reads before the next mid writes
+    u = un;
+    U.geom(a, smem_raw, true, u);
+  }
 }
 
 // Adjoint, module-shared: per unit, cotangent spectrum * conj(PSF spectrum)
 // added into the patch's (zero) accumulator; the CTAs also clear the
-// (E,nx,ny) output that the next kernel adds into ...
+// (E,nx,ny) output that the next kernel adds into when called alone ...
+// A loop over units: CTA b takes units b, b + G, b + 2G, ... (G = gridDim.x,
+// one CTA per SM).  The next unit's first input chunk is issued into the
+// staging area before this unit's spectrum stage, which leaves the staging
+// area alone: those loads overlap the stage instead of opening the next unit.
+// The next unit's PSF spectrum is prefetched into L2 only once this unit is
+// done (earlier, it competes with this unit's spectrum loads).
 template <typename T, int P>
-__global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_to_spec(Args a) {
+__global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_to_spec(Args a, int units) {
   using R = Tr<T, P>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Unit<T, P> U;
   pdl_trigger();
-  U.init(a, smem_raw, true);
+  int u = blockIdx.x;
+  U.init(a, smem_raw, true, u);
   prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
   pdl_wait();
   if (a.zero_out) zero_slice(a.out, (int64_t)a.E * a.nx * a.ny * (int64_t)sizeof(T), a.zchunk);
-  stage_input<T, P, true>(U, a);
-  stage_split<T, P>(U);
-  __syncthreads();
-  stage_col1<T, P>(U, 0, P);
-  __syncthreads();
-  stage_mid<T, P, MID_TO_ACC, true>(U);
+  bool pre = false;
+  for (;;) {
+    stage_input<T, P, true>(U, a, pre);
+    stage_split<T, P>(U);
+    __syncthreads();
+    stage_col1<T, P>(U, 0, P);
+    __syncthreads();
+    const int un = u + (int)gridDim.x;
+    if (un < units) {
+      Unit<T, P> N;
+      N.geom(a, smem_raw, true, un);
+      input_issue<T, P, true>(N, a, InChunks<T, P, true>(N), 0);
+    }
+    stage_mid<T, P, MID_TO_ACC, true>(U);
+    if (un >= units) break;
+    __syncthreads();  // the tile's last reads before the next unit's input stage writes it
+    u = un;
+    U.geom(a, smem_raw, true, u);
+    prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
+    pre = true;
+  }
 }
 
 // ... then, per (energy, patch), one inverse transform -> window -> gradient;
@@ -936,6 +1020,18 @@ int set_smem(KernelT kern, size_t smem) {
   return cuda_status(
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
       "cudaFuncSetAttribute");
+}
+
+// Streaming multiprocessors of the current device (cached per device).
+int sm_count() {
+  constexpr int kMaxDev = 64;
+  static int n[kMaxDev] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return 1;
+  if (!n[dev] &&
+      cudaDeviceGetAttribute(&n[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    n[dev] = 1;
+  return n[dev] > 0 ? n[dev] : 1;
 }
 
 // Kernel arguments of one stage of one plan (sizes in bytes use esz).
@@ -995,9 +1091,9 @@ int ensure_smem_attrs() {
     JUBIK_TRY(set_smem(k_fused_group<T, P, false>, smem));
     JUBIK_TRY(set_smem(k_fused_group<T, P, true>, smem));
     JUBIK_TRY(set_smem(k_sky_spec<T, P>, smem));
-    JUBIK_TRY(set_smem(k_fwd_from_spec<T, P>, smem));
-    JUBIK_TRY(set_smem(k_adj_to_spec<T, P>, smem));
     JUBIK_TRY(set_smem(k_adj_from_spec<T, P>, smem));
+    JUBIK_TRY(set_smem(k_adj_to_spec<T, P>, smem));
+    JUBIK_TRY(set_smem(k_fwd_from_spec<T, P>, smem));
     attr_set[dev] = true;
   }
   return JUBIK_OK;
@@ -1039,8 +1135,17 @@ int launch_one(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
     case FUSED_FWD_UNITS: return launch_pdl<T, P>(k_fused<T, P, false>, units, f.pdl, s, a);
     case FUSED_ADJ_UNITS: return launch_pdl<T, P>(k_fused<T, P, true>, units, f.pdl, s, a);
     case FUSED_FWD_SKY: return launch_pdl<T, P>(k_sky_spec<T, P>, patches, f.pdl, s, a);
-    case FUSED_FWD_FROM_SPEC: return launch_pdl<T, P>(k_fwd_from_spec<T, P>, units, f.pdl, s, a);
-    case FUSED_ADJ_TO_SPEC: return launch_pdl<T, P>(k_adj_to_spec<T, P>, units, f.pdl, s, a);
+    case FUSED_FWD_FROM_SPEC:
+      return launch_pdl<T, P>(k_fwd_from_spec<T, P>, std::min<int64_t>(units, sm_count()),
+                              f.pdl, s, a, (int)units);
+    case FUSED_ADJ_TO_SPEC: {
+      // one CTA per SM, looping over the units
+      const int64_t grid = std::min<int64_t>(units, sm_count());
+      Args al = a;
+      const int64_t zbytes = (int64_t)g.E * g.pixels() * (int64_t)sizeof(T);
+      al.zchunk = ((zbytes + grid - 1) / grid + 15) & ~(int64_t)15;
+      return launch_pdl<T, P>(k_adj_to_spec<T, P>, grid, f.pdl, s, al, (int)units);
+    }
     case FUSED_ADJ_FROM_SPEC: return launch_pdl<T, P>(k_adj_from_spec<T, P>, patches, f.pdl, s, a);
     default:
       set_error("unknown fused stage %d", which);
