@@ -230,3 +230,30 @@ def test_cf_argument_errors(cuda):
         sky.close()
     with pytest.raises(ju.JubikUnsupported):
         jsky.CorrelatedFieldSky((16, 13 * 67), 1.0)  # prime factor above the FFT's radix limit
+
+
+def test_sky_of_the_reference_sky_model_test(cuda):
+    """The properties test/test_sky_model.py:80-97 checks of J-UBIK's sky for
+    its config (sdim 128, s_padding_ratio 1.1, 3 bins 0.2-1 / 1-2 / 2-4 keV,
+    e_ref 2, spatial + plaw fields): at positions 0.1 x standard normal the sky
+    exp(logsky) has the data shape, is finite, non-negative, not constant, and
+    a second evaluation repeats it exactly."""
+    shape = (jsky.good_fft_size(int(128 * 1.1)),) * 2
+    coef = jsky.diffuse_coefficients([0.2, 1.0, 2.0], [1.0, 2.0, 4.0], 2.0)
+    sky = jsky.CorrelatedFieldSky(shape, 1.0, n_fields=2, crop=(128, 128), coefficients=coef,
+                                  dtype=torch.float64)
+    try:
+        rng = np.random.default_rng(81)
+        k = sky.mode_lengths / sky.mode_lengths[-1]
+        amp = np.stack([(1 + (k / 0.05) ** 2) ** -1.0] * 2) / np.sqrt(sky.pindex.size)
+        xi = T(0.1 * rng.standard_normal((2,) + shape), torch.float64, cuda)
+        off = T(np.array([-14.0, -2.0]), torch.float64, cuda)
+        a = T(amp, torch.float64, cuda)
+        s1 = torch.exp(sky.logsky(a, xi, off))
+        s2 = torch.exp(sky.logsky(a, xi, off))
+        assert s1.shape == (3, 128, 128)
+        assert bool(torch.isfinite(s1).all()) and bool((s1 >= 0).all())
+        assert float(s1.var()) > 0
+        assert torch.equal(s1, s2)
+    finally:
+        sky.close()

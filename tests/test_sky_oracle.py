@@ -13,6 +13,8 @@ def test_good_fft_size_matches_the_reference_padding():
     # which is a 'good size' padded space" (demos/configs/eROSITA_demo.yaml:50)
     assert jsky.good_fft_size(int(1024 * 1.1075)) == 1134
     assert jsky.good_fft_size(int(512 * 1.1075)) == 567
+    # the reference's own sky-model test grid (test/test_sky_model.py:55-58)
+    assert jsky.good_fft_size(int(128 * 1.1)) == 140
     assert jsky.good_fft_size(1025) == 1029  # 3 * 7^3
     assert jsky.good_fft_size(13) == 14
     for n in range(1, 2500):
