@@ -1,6 +1,6 @@
 """CPU oracle for the callers around the response (TEST INFRASTRUCTURE).
 
-This module is the checker, never the product: only ``tests/`` may import it.
+This module is the oracle (test infrastructure), never the product: only ``tests/`` may import it.
 It restates in numpy:
 
 * the Philox4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw,

@@ -1,6 +1,6 @@
 """CPU oracle for the J-UBIK spatially-variant response (TEST INFRASTRUCTURE).
 
-This module is the checker, never the product: only ``tests/``,
+This module is the oracle (test infrastructure), never the product: only ``tests/``,
 ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg may import it.
 It restates, in float64 numpy / scipy.fft, the reference algorithm of
 

@@ -1,6 +1,6 @@
 """CPU oracle for the eROSITA PSF-patch interpolation (TEST INFRASTRUCTURE).
 
-This module is the checker, never the product: only ``tests/`` may import it.
+This module is the oracle (test infrastructure), never the product: only ``tests/`` may import it.
 It restates in float64 numpy the behaviour of
 ``jubik/instruments/erosita/erosita_psf_utils.py``:
 

@@ -1,6 +1,6 @@
 """CPU oracle for the correlated-field log-sky (TEST INFRASTRUCTURE).
 
-This module is the checker, never the product: only ``tests/`` may import it.
+This module is the oracle (test infrastructure), never the product: only ``tests/`` may import it.
 It restates in float64 numpy, independently of the product code:
 
 * the padded grid size of ``jubik/sky_models.py:306-307``
