@@ -1,8 +1,8 @@
 /*
  * Independent CPU restatement of jubik/convolve.py:66-145 (TEST INFRASTRUCTURE).
  *
- * Only tests/ and the smoke check call this; it is the checker, not the
- * product.  It recomputes linpatch_convolve by DIRECT circular convolution
+ * Only tests/ and the smoke check call this; it is part of the oracle, not
+ * the product.  It recomputes linpatch_convolve by DIRECT circular convolution
  * (no FFT) so that it shares no code path with the numpy oracle:
  *
  *   for patch k (row start (k % n)*dx, column start (k // n)*dx, clamped as
