@@ -220,14 +220,15 @@ JUBIK_API int jubik_psf_interpolate(const double* psfs, const double* rs,
                                     int32_t dtype, void* out, void* stream);
 
 /* Independent problems evaluated together (no counterpart in the reference,
- * which evaluates one likelihood per call): plans of one dtype that run the
- * per-unit fused kernels (one module, or path JUBIK_PATH_FUSED_UNIT, with a
- * fused FFT side), grouped by FFT side.  One energy+gradient call of the group
- * is one grouped clearing kernel, one forward and one adjoint launch per FFT
- * side over all of that side's problems, and one grouped likelihood pass --
- * the work of jubik_poisson_energy_grad on every plan.  The plans must outlive
- * the group, and none of them may run another call while a group call is in
- * flight.
+ * which evaluates one likelihood per call): plans of one dtype on a fused FFT
+ * side, grouped by FFT side and kind (per-unit kernels, or module-shared patch
+ * spectra for plans with several modules).  One energy+gradient call of the
+ * group is one grouped clearing kernel; per side, one forward and one adjoint
+ * launch over all of that side's per-unit problems, or two of each (patch
+ * spectra, then units) for its module-shared problems; and one grouped
+ * likelihood pass -- the work of jubik_poisson_energy_grad on every plan.  The
+ * plans must outlive the group, and none of them may run another call while a
+ * group call is in flight.
  * set_io: the device sky and gradient buffer of each problem (x[i], grad[i],
  * shaped (E,nx,ny) of plan i) and a device double[n] for the energies; they
  * are read at every later call. */

@@ -15,11 +15,13 @@ timing the candidates (module-shared fused, per-unit fused, unfused) on the
 largest problem of that side.  Problems with one module take the same kernels
 on both fused paths.
 
-When every problem runs the per-unit fused kernels, :meth:`ProblemBatch.group`
+When every problem runs on a fused FFT side, :meth:`ProblemBatch.group`
 switches the pass to grouped launches (``jubik_group_*``): one clearing
-kernel, one forward and one adjoint launch per FFT side over all of that
-side's problems, and one likelihood pass over all problems -- a handful of
-launches in place of five per problem.  The grouped pass can be captured too.
+kernel; per FFT side, one forward and one adjoint launch over all of that
+side's one-module problems and two of each over its several-module problems
+(patch spectra shared by the modules, then the units); and one likelihood
+pass over all problems -- a handful of launches in place of five per problem.
+The grouped pass can be captured too.
 """
 from __future__ import annotations
 
@@ -145,7 +147,7 @@ class ProblemBatch:
 
     def group(self) -> bool:
         """Switch the pass to grouped launches; False (and the per-problem pass
-        stays) when a problem does not run the per-unit fused kernels."""
+        stays) when a problem takes the unfused path."""
         self._drop_group()
         lib = _lib.load()
         n = len(self.plans)

@@ -1051,11 +1051,14 @@ int jubik_convolve2d(const void* kernel, int64_t bk, const void* signal, int64_t
 // kernel, instead of a launch sequence per problem.
 struct GroupClass {
   int P = 0;
+  bool shared = false;       // module-shared plans: 4 launches per pass, else 2
   std::vector<int> members;  // indices into the group's plans
   int64_t blocks = 0;        // units of all members
-  void* fwd_list = nullptr;  // device Args per member: forward per-unit stage
-  void* adj_list = nullptr;  // device Args per member: adjoint per-unit stage
-  int* starts = nullptr;     // device: first block of each member, then the total
+  int64_t items = 0;         // (energy, patch) items of all members (shared)
+  void* fwd_list = nullptr;  // device Args per member: forward stages
+  void* adj_list = nullptr;  // device Args per member: adjoint stages
+  int* starts = nullptr;     // device: first unit of each member, then the total
+  int* item_starts = nullptr;  // device: first item of each member, then the total
 };
 
 struct jubik_group {
@@ -1079,7 +1082,10 @@ struct jubik_group {
   void free_io() {
     for (void* p : allocs) cudaFree(p);
     allocs.clear();
-    for (auto& c : classes) c.fwd_list = c.adj_list = c.starts = nullptr;
+    for (auto& c : classes) {
+      c.fwd_list = c.adj_list = nullptr;
+      c.starts = c.item_starts = nullptr;
+    }
     pjobs = nullptr;
     zjobs = nullptr;
     pstarts = zstarts = nullptr;
@@ -1116,9 +1122,9 @@ int jubik_group_create(jubik_plan* const* plans, int32_t n, jubik_group** out) {
     if (!p) {
       set_error("group: plan %d is NULL", i);
       st = JUBIK_ERR_INVALID_ARGUMENT;
-    } else if (p->path != JUBIK_PATH_FUSED || p->spec) {
-      set_error("group: plan %d does not run the per-unit fused kernels (one module, or path "
-                "fused_unit, with a fused FFT side)", i);
+    } else if (p->path != JUBIK_PATH_FUSED) {
+      set_error("group: plan %d does not run the fused kernels (its FFT side or dtype takes the "
+                "unfused path)", i);
       st = JUBIK_ERR_UNSUPPORTED;
     } else if (i > 0 && p->dtype != plans[0]->dtype) {
       set_error("group: plans of different dtypes");
@@ -1136,11 +1142,14 @@ int jubik_group_create(jubik_plan* const* plans, int32_t n, jubik_group** out) {
   g->dtype = plans[0]->dtype;
   for (int i = 0; i < n; ++i) {
     const int P = g->plans[i]->g.P;
-    auto it = std::find_if(g->classes.begin(), g->classes.end(),
-                           [&](const GroupClass& c) { return c.P == P; });
+    const bool shared = g->plans[i]->spec != nullptr;
+    auto it = std::find_if(g->classes.begin(), g->classes.end(), [&](const GroupClass& c) {
+      return c.P == P && c.shared == shared;
+    });
     if (it == g->classes.end()) {
       g->classes.emplace_back();
       g->classes.back().P = P;
+      g->classes.back().shared = shared;
       it = g->classes.end() - 1;
     }
     it->members.push_back(i);
@@ -1166,28 +1175,41 @@ int jubik_group_set_io(jubik_group* g, const void* const* x, void* const* grad,
   const size_t asz = fused_args_size();
   for (auto& c : g->classes) {
     std::vector<unsigned char> fwd(asz * c.members.size()), adj(asz * c.members.size());
-    std::vector<int> starts;
-    int64_t b = 0;
+    std::vector<int> starts, item_starts;
+    int64_t b = 0, items = 0;
     for (size_t k = 0; k < c.members.size(); ++k) {
       const int i = c.members[k];
       jubik_plan* p = g->plans[i];
       starts.push_back((int)b);
+      item_starts.push_back((int)items);
       b += p->g.units();
-      FusedLaunch f{x[i], p->conv, p->hmain, p->hnyq, p->tw, p->wt, p->desc.pixel_area, nullptr};
-      fused_args_fill(p->g, p->dtype, f, FUSED_FWD_UNITS, fwd.data() + k * asz);
+      items += (int64_t)p->g.E * p->g.n * p->g.n;
+      // module-shared plans: the forward stages share p->spec, the adjoint stages sum
+      // into p->acc; nothing is cleared inside them (the clearing kernel runs first)
+      FusedLaunch f{x[i], p->conv, p->hmain, p->hnyq, p->tw, p->wt, p->desc.pixel_area,
+                    c.shared ? p->spec : nullptr};
+      f.clear = false;
+      fused_args_fill(p->g, p->dtype, f, c.shared ? FUSED_FWD_SKY : FUSED_FWD_UNITS,
+                      fwd.data() + k * asz);
       FusedLaunch r{p->resid, grad[i], p->hmain, p->hnyq, p->tw, p->wt, p->desc.pixel_area,
-                    nullptr};
-      fused_args_fill(p->g, p->dtype, r, FUSED_ADJ_UNITS, adj.data() + k * asz);
+                    c.shared ? p->acc : nullptr};
+      r.zero_out = false;
+      r.clear = false;
+      fused_args_fill(p->g, p->dtype, r, c.shared ? FUSED_ADJ_TO_SPEC : FUSED_ADJ_UNITS,
+                      adj.data() + k * asz);
     }
     if (b > 0x7fffffffLL) {
       set_error("group: too many patch units");
       return JUBIK_ERR_UNSUPPORTED;
     }
     starts.push_back((int)b);
+    item_starts.push_back((int)items);
     c.blocks = b;
+    c.items = items;
     JUBIK_TRY(upload(g, fwd, (unsigned char**)&c.fwd_list));
     JUBIK_TRY(upload(g, adj, (unsigned char**)&c.adj_list));
     JUBIK_TRY(upload(g, starts, &c.starts));
+    if (c.shared) JUBIK_TRY(upload(g, item_starts, &c.item_starts));
   }
   std::vector<PoissonJob> pj;
   std::vector<ZeroJob> zj;
@@ -1232,13 +1254,31 @@ int jubik_group_energy_grad(jubik_group* g, void* stream) {
   cudaStream_t s = S(stream);
   const int n = (int)g->plans.size();
   JUBIK_TRY(zero_group_run(g->zjobs, g->zstarts, g->nzero, g->zblocks, true, s));
-  for (auto& c : g->classes)
-    JUBIK_TRY(fused_group_run(c.P, g->dtype, c.fwd_list, c.starts, (int)c.members.size(),
-                              c.blocks, false, true, s));
+  for (auto& c : g->classes) {
+    const int m = (int)c.members.size();
+    if (c.shared) {
+      JUBIK_TRY(fused_group_shared_run(c.P, g->dtype, c.fwd_list, c.item_starts, m, c.items,
+                                       FUSED_FWD_SKY, true, s));
+      JUBIK_TRY(fused_group_shared_run(c.P, g->dtype, c.fwd_list, c.starts, m, c.blocks,
+                                       FUSED_FWD_FROM_SPEC, true, s));
+    } else {
+      JUBIK_TRY(fused_group_run(c.P, g->dtype, c.fwd_list, c.starts, m, c.blocks, false, true,
+                                s));
+    }
+  }
   JUBIK_TRY(poisson_group_run(g->dtype, g->pjobs, g->pstarts, n, g->pblocks, true, s));
-  for (auto& c : g->classes)
-    JUBIK_TRY(fused_group_run(c.P, g->dtype, c.adj_list, c.starts, (int)c.members.size(),
-                              c.blocks, true, true, s));
+  for (auto& c : g->classes) {
+    const int m = (int)c.members.size();
+    if (c.shared) {
+      JUBIK_TRY(fused_group_shared_run(c.P, g->dtype, c.adj_list, c.starts, m, c.blocks,
+                                       FUSED_ADJ_TO_SPEC, true, s));
+      JUBIK_TRY(fused_group_shared_run(c.P, g->dtype, c.adj_list, c.item_starts, m, c.items,
+                                       FUSED_ADJ_FROM_SPEC, true, s));
+    } else {
+      JUBIK_TRY(fused_group_run(c.P, g->dtype, c.adj_list, c.starts, m, c.blocks, true, true,
+                                s));
+    }
+  }
   for (jubik_plan* p : g->plans) p->lam_valid = true;
   return JUBIK_OK;
 }
@@ -1248,7 +1288,9 @@ int jubik_group_launches(const jubik_group* g, int32_t* launches) {
     set_error("group: invalid arguments");
     return JUBIK_ERR_INVALID_ARGUMENT;
   }
-  *launches = 2 + 2 * (int32_t)g->classes.size();
+  int32_t k = 2;
+  for (const auto& c : g->classes) k += c.shared ? 4 : 2;
+  *launches = k;
   return JUBIK_OK;
 }
 

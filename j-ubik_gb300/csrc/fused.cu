@@ -835,6 +835,34 @@ __device__ __forceinline__ void prefetch_unit(const void* h, unsigned hb, const 
   }
 }
 
+// Where a kernel's block (or loop) index g finds its arguments: one problem
+// (the kernel parameter itself), or a list of independent problems, problem p
+// owning indices [starts[p], starts[p + 1]) (grouped launches).
+struct OneProblem {
+  Args a;
+  __device__ __forceinline__ const Args& at(int g, int& local) const {
+    local = g;
+    return a;
+  }
+};
+struct ProblemList {
+  const Args* list;
+  const int* starts;
+  int n;
+  __device__ __forceinline__ const Args& at(int g, int& local) const {
+    int lo = 0, hi = n - 1;  // the last problem whose first index is <= g
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(starts + mid) <= g)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    local = g - __ldg(starts + lo);
+    return list[lo];
+  }
+};
+
 // ================================================================= kernels
 // One CTA per unit: the whole forward or adjoint of one patch.
 template <typename T, int P, bool ADJ>
@@ -892,12 +920,14 @@ __global__ void __launch_bounds__(Tr<T, P>::NT)
 
 // Forward, module-shared: the sky spectrum of each (energy, patch) once; the
 // CTAs also clear the (M,E,nx,ny) output that the next kernel adds into ...
-template <typename T, int P>
-__global__ void __launch_bounds__(Tr<T, P>::NT) k_sky_spec(Args a) {
+template <typename T, int P, typename Src>
+__global__ void __launch_bounds__(Tr<T, P>::NT) k_sky_spec(Src src) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Unit<T, P> U;
   pdl_trigger();
-  U.init(a, smem_raw, false);
+  int item;
+  const Args& a = src.at((int)blockIdx.x, item);
+  U.init(a, smem_raw, false, item);
   pdl_wait();
   zero_slice(a.out, (int64_t)a.M * a.E * a.nx * a.ny * (int64_t)sizeof(T), a.zchunk);
   if (a.aux) zero_slice(a.aux, a.aux_bytes, a.aux_chunk);
@@ -916,36 +946,44 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_sky_spec(Args a) {
 // data is in L2 when the next unit's spectrum stage reads it.  (Prefetching a
 // whole unit ahead was slower: the prefetches then compete with the current
 // unit's spectrum loads.)
-template <typename T, int P>
-__global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_from_spec(Args a, int units) {
+template <typename T, int P, typename Src>
+__global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_from_spec(Src src, int units) {
   using R = Tr<T, P>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Unit<T, P> U;
   pdl_trigger();
-  int u = blockIdx.x;
-  U.init(a, smem_raw, true, u);
+  int g = blockIdx.x;
+  {
+    int lu;
+    U.init(src.at(g, lu), smem_raw, true, lu);
+  }
   prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
   pdl_wait();
   if (threadIdx.x == 32) prefetch_l2(U.spec, sizeof(cx<T>) * P * R::H);
   for (;;) {
-    const int un = u + (int)gridDim.x;
+    const int gn = g + (int)gridDim.x;
     stage_mid<T, P, MID_FROM_SPEC, false>(U);
     __syncthreads();
     stage_invB<T, P, 0>(U, U.tid, R::NT);
     __syncthreads();
     stage_combine<T, P>(U, 0, R::H);
     __syncthreads();
-    if (un < units) {  // the output stage's reductions leave HBM reads free
+    if (gn < units) {  // the output stage's reductions leave HBM reads free
+      int lun;
       Unit<T, P> N;
-      N.geom(a, smem_raw, true, un);
+      N.geom(src.at(gn, lun), smem_raw, true, lun);
       prefetch_unit(N.hmain, sizeof(cx<T>) * P * R::H, N.hnyq, sizeof(cx<T>) * P);
       if (threadIdx.x == 32) prefetch_l2(N.spec, sizeof(cx<T>) * P * R::H);
     }
-    stage_output<T, P, false>(U, a);
-    if (un >= units) break;
+    {
+      int lu;
+      stage_output<T, P, false>(U, src.at(g, lu));
+    }
+    if (gn >= units) break;
     __syncthreads();  // the output stage's last staging reads before the next mid writes
-    u = un;
-    U.geom(a, smem_raw, true, u);
+    g = gn;
+    int lu;
+    U.geom(src.at(g, lu), smem_raw, true, lu);
   }
 }
 
@@ -958,35 +996,49 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_from_spec(Args a, int unit
 // area alone: those loads overlap the stage instead of opening the next unit.
 // The next unit's PSF spectrum is prefetched into L2 only once this unit is
 // done (earlier, it competes with this unit's spectrum loads).
-template <typename T, int P>
-__global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_to_spec(Args a, int units) {
+template <typename T, int P, typename Src>
+__global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_to_spec(Src src, int units) {
   using R = Tr<T, P>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Unit<T, P> U;
   pdl_trigger();
-  int u = blockIdx.x;
-  U.init(a, smem_raw, true, u);
+  int g = blockIdx.x;
+  {
+    int lu;
+    U.init(src.at(g, lu), smem_raw, true, lu);
+  }
   prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
   pdl_wait();
-  if (a.zero_out) zero_slice(a.out, (int64_t)a.E * a.nx * a.ny * (int64_t)sizeof(T), a.zchunk);
+  {
+    int lu;
+    const Args& a = src.at(g, lu);
+    if (a.zero_out)
+      zero_slice(a.out, (int64_t)a.E * a.nx * a.ny * (int64_t)sizeof(T), a.zchunk);
+  }
   bool pre = false;
   for (;;) {
-    stage_input<T, P, true>(U, a, pre);
+    {
+      int lu;
+      stage_input<T, P, true>(U, src.at(g, lu), pre);
+    }
     stage_split<T, P>(U);
     __syncthreads();
     stage_col1<T, P>(U, 0, P);
     __syncthreads();
-    const int un = u + (int)gridDim.x;
-    if (un < units) {
+    const int gn = g + (int)gridDim.x;
+    if (gn < units) {
+      int lun;
+      const Args& an = src.at(gn, lun);
       Unit<T, P> N;
-      N.geom(a, smem_raw, true, un);
-      input_issue<T, P, true>(N, a, InChunks<T, P, true>(N), 0);
+      N.geom(an, smem_raw, true, lun);
+      input_issue<T, P, true>(N, an, InChunks<T, P, true>(N), 0);
     }
     stage_mid<T, P, MID_TO_ACC, true>(U);
-    if (un >= units) break;
+    if (gn >= units) break;
     __syncthreads();  // the tile's last reads before the next unit's input stage writes it
-    u = un;
-    U.geom(a, smem_raw, true, u);
+    g = gn;
+    int lu;
+    U.geom(src.at(g, lu), smem_raw, true, lu);
     prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
     pre = true;
   }
@@ -994,13 +1046,15 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_to_spec(Args a, int units)
 
 // ... then, per (energy, patch), one inverse transform -> window -> gradient;
 // the accumulator is cleared as it is read.
-template <typename T, int P>
-__global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_from_spec(Args a) {
+template <typename T, int P, typename Src>
+__global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_from_spec(Src src) {
   using R = Tr<T, P>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Unit<T, P> U;
   pdl_trigger();
-  U.init(a, smem_raw, false);
+  int item;
+  const Args& a = src.at((int)blockIdx.x, item);
+  U.init(a, smem_raw, false, item);
   pdl_wait();
   stage_mid<T, P, MID_FROM_ACC, true>(U);
   __syncthreads();
@@ -1065,6 +1119,13 @@ Args make_args(const Geom& g, const FusedLaunch& f, int which, size_t esz) {
   a.aux_bytes = f.aux ? f.aux_bytes : 0;
   a.aux_chunk = grid > 0 ? ((a.aux_bytes + grid - 1) / grid + 15) & ~(int64_t)15 : 0;
   a.zero_out = f.zero_out ? 1 : 0;
+  if (!f.clear) {  // grouped launches clear every problem's buffers in one kernel
+    a.zchunk = 0;
+    a.aux = nullptr;
+    a.aux_bytes = 0;
+    a.aux_chunk = 0;
+    a.zero_out = 0;
+  }
   a.in_rs = f.in_rs > 0 ? f.in_rs : (int64_t)g.ny;
   a.in_ps = f.in_ps > 0 ? f.in_ps : g.pixels();
   a.in_exp = f.in_exp ? 1 : 0;
@@ -1090,10 +1151,14 @@ int ensure_smem_attrs() {
     JUBIK_TRY(set_smem(k_fused<T, P, true>, smem));
     JUBIK_TRY(set_smem(k_fused_group<T, P, false>, smem));
     JUBIK_TRY(set_smem(k_fused_group<T, P, true>, smem));
-    JUBIK_TRY(set_smem(k_sky_spec<T, P>, smem));
-    JUBIK_TRY(set_smem(k_adj_from_spec<T, P>, smem));
-    JUBIK_TRY(set_smem(k_adj_to_spec<T, P>, smem));
-    JUBIK_TRY(set_smem(k_fwd_from_spec<T, P>, smem));
+    JUBIK_TRY(set_smem(k_sky_spec<T, P, OneProblem>, smem));
+    JUBIK_TRY(set_smem(k_adj_from_spec<T, P, OneProblem>, smem));
+    JUBIK_TRY(set_smem(k_adj_to_spec<T, P, OneProblem>, smem));
+    JUBIK_TRY(set_smem(k_fwd_from_spec<T, P, OneProblem>, smem));
+    JUBIK_TRY(set_smem(k_sky_spec<T, P, ProblemList>, smem));
+    JUBIK_TRY(set_smem(k_adj_from_spec<T, P, ProblemList>, smem));
+    JUBIK_TRY(set_smem(k_adj_to_spec<T, P, ProblemList>, smem));
+    JUBIK_TRY(set_smem(k_fwd_from_spec<T, P, ProblemList>, smem));
     attr_set[dev] = true;
   }
   return JUBIK_OK;
@@ -1134,19 +1199,24 @@ int launch_one(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
   switch (which) {
     case FUSED_FWD_UNITS: return launch_pdl<T, P>(k_fused<T, P, false>, units, f.pdl, s, a);
     case FUSED_ADJ_UNITS: return launch_pdl<T, P>(k_fused<T, P, true>, units, f.pdl, s, a);
-    case FUSED_FWD_SKY: return launch_pdl<T, P>(k_sky_spec<T, P>, patches, f.pdl, s, a);
+    case FUSED_FWD_SKY:
+      return launch_pdl<T, P>(k_sky_spec<T, P, OneProblem>, patches, f.pdl, s, OneProblem{a});
     case FUSED_FWD_FROM_SPEC:
-      return launch_pdl<T, P>(k_fwd_from_spec<T, P>, std::min<int64_t>(units, sm_count()),
-                              f.pdl, s, a, (int)units);
+      return launch_pdl<T, P>(k_fwd_from_spec<T, P, OneProblem>,
+                              std::min<int64_t>(units, sm_count()), f.pdl, s, OneProblem{a},
+                              (int)units);
     case FUSED_ADJ_TO_SPEC: {
       // one CTA per SM, looping over the units
       const int64_t grid = std::min<int64_t>(units, sm_count());
       Args al = a;
       const int64_t zbytes = (int64_t)g.E * g.pixels() * (int64_t)sizeof(T);
       al.zchunk = ((zbytes + grid - 1) / grid + 15) & ~(int64_t)15;
-      return launch_pdl<T, P>(k_adj_to_spec<T, P>, grid, f.pdl, s, al, (int)units);
+      return launch_pdl<T, P>(k_adj_to_spec<T, P, OneProblem>, grid, f.pdl, s, OneProblem{al},
+                              (int)units);
     }
-    case FUSED_ADJ_FROM_SPEC: return launch_pdl<T, P>(k_adj_from_spec<T, P>, patches, f.pdl, s, a);
+    case FUSED_ADJ_FROM_SPEC:
+      return launch_pdl<T, P>(k_adj_from_spec<T, P, OneProblem>, patches, f.pdl, s,
+                              OneProblem{a});
     default:
       set_error("unknown fused stage %d", which);
       return JUBIK_ERR_INVALID_ARGUMENT;
@@ -1165,6 +1235,58 @@ int launch_group(const void* list, const int* starts, int nprob, int64_t blocks,
   const Args* l = (const Args*)list;
   return adj ? launch_pdl<T, P>(k_fused_group<T, P, true>, blocks, pdl, s, l, starts, nprob)
              : launch_pdl<T, P>(k_fused_group<T, P, false>, blocks, pdl, s, l, starts, nprob);
+}
+
+// One module-shared stage over a list of problems of one FFT side: starts
+// (device) index the (energy, patch) items for FUSED_FWD_SKY / FUSED_ADJ_FROM_SPEC
+// and the units for FUSED_FWD_FROM_SPEC / FUSED_ADJ_TO_SPEC; count is the total.
+template <typename T, int P>
+int launch_group_shared(const void* list, const int* starts, int nprob, int64_t count,
+                        int which, bool pdl, cudaStream_t s) {
+  JUBIK_TRY((ensure_smem_attrs<T, P>()));
+  if (count <= 0) return JUBIK_OK;
+  if (count > 0x7fffffffLL) {
+    set_error("too many patch units for one launch");
+    return JUBIK_ERR_UNSUPPORTED;
+  }
+  const ProblemList src{(const Args*)list, starts, nprob};
+  const int64_t loop_grid = std::min<int64_t>(count, sm_count());
+  switch (which) {
+    case FUSED_FWD_SKY: return launch_pdl<T, P>(k_sky_spec<T, P, ProblemList>, count, pdl, s, src);
+    case FUSED_FWD_FROM_SPEC:
+      return launch_pdl<T, P>(k_fwd_from_spec<T, P, ProblemList>, loop_grid, pdl, s, src,
+                              (int)count);
+    case FUSED_ADJ_TO_SPEC:
+      return launch_pdl<T, P>(k_adj_to_spec<T, P, ProblemList>, loop_grid, pdl, s, src,
+                              (int)count);
+    case FUSED_ADJ_FROM_SPEC:
+      return launch_pdl<T, P>(k_adj_from_spec<T, P, ProblemList>, count, pdl, s, src);
+    default:
+      set_error("unknown module-shared stage %d", which);
+      return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+}
+
+template <typename T>
+int dispatch_group_shared(int P, const void* list, const int* starts, int nprob, int64_t count,
+                          int which, bool pdl, cudaStream_t s) {
+  switch (P) {
+    case 32: return launch_group_shared<T, 32>(list, starts, nprob, count, which, pdl, s);
+    case 64: return launch_group_shared<T, 64>(list, starts, nprob, count, which, pdl, s);
+    case 96: return launch_group_shared<T, 96>(list, starts, nprob, count, which, pdl, s);
+    case 128: return launch_group_shared<T, 128>(list, starts, nprob, count, which, pdl, s);
+    case 160:
+      if constexpr (sizeof(T) == 4)
+        return launch_group_shared<T, 160>(list, starts, nprob, count, which, pdl, s);
+      break;
+    case 192:
+      if constexpr (sizeof(T) == 4)
+        return launch_group_shared<T, 192>(list, starts, nprob, count, which, pdl, s);
+      break;
+    default: break;
+  }
+  set_error("fused path does not cover P=%d for this dtype", P);
+  return JUBIK_ERR_UNSUPPORTED;
 }
 
 template <typename T>
@@ -1238,6 +1360,13 @@ size_t fused_args_size() { return sizeof(Args); }
 void fused_args_fill(const Geom& g, int dtype, const FusedLaunch& f, int which, void* dst) {
   const Args a = make_args(g, f, which, dtype == JUBIK_F32 ? sizeof(float) : sizeof(double));
   memcpy(dst, &a, sizeof(Args));
+}
+
+int fused_group_shared_run(int P, int dtype, const void* list, const int* starts, int nprob,
+                           int64_t count, int which, bool pdl, cudaStream_t s) {
+  return dtype == JUBIK_F32
+             ? dispatch_group_shared<float>(P, list, starts, nprob, count, which, pdl, s)
+             : dispatch_group_shared<double>(P, list, starts, nprob, count, which, pdl, s);
 }
 
 int fused_group_run(int P, int dtype, const void* list, const int* starts, int nprob,

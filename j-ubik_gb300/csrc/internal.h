@@ -93,6 +93,7 @@ struct FusedLaunch {
   // strides (0 = the field's own), and whether it holds log-sky values
   int64_t in_rs = 0, in_ps = 0;
   bool in_exp = false;
+  bool clear = true;    // false: the kernels clear nothing (grouped launches clear first)
 };
 size_t fused_spec_bytes(const Geom& g, int dtype);
 // Grouped per-unit launches over independent problems of one FFT side: the
@@ -123,6 +124,12 @@ int zero_group_run(const ZeroJob* jobs, const int* starts, int njobs, int64_t bl
                    cudaStream_t s);
 size_t fused_args_size();
 void fused_args_fill(const Geom& g, int dtype, const FusedLaunch& f, int which, void* dst);
+// One module-shared stage (FUSED_FWD_SKY, FUSED_FWD_FROM_SPEC, FUSED_ADJ_TO_SPEC,
+// FUSED_ADJ_FROM_SPEC) over nprob problems of FFT side P: starts (device, nprob + 1)
+// index the (energy, patch) items of the per-patch stages or the units of the
+// per-unit stages, count of them in all.
+int fused_group_shared_run(int P, int dtype, const void* list, const int* starts, int nprob,
+                           int64_t count, int which, bool pdl, cudaStream_t s);
 int fused_group_run(int P, int dtype, const void* list, const int* starts, int nprob,
                     int64_t blocks, bool adj, bool pdl, cudaStream_t s);
 enum FusedStage {
