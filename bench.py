@@ -186,17 +186,23 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def uneven_batch_leg(dev, n_streams=8, passes=10):
-    """64 independent problems of uneven size (sides 144..896, FFT sides
-    32/64/128, 1..3 energies): energy + gradient of all of them, problem after
-    problem on one stream against one CUDA-graph launch of the same pass with
-    the problems spread over ``n_streams`` branches."""
+def uneven_batch_leg(dev, n_streams=8, passes=10, modules=1, count=64):
+    """Independent problems of uneven size (the config-5 geometry: sides
+    144..896, FFT sides 32/64/128, 1..3 energies; ``count`` of them, each with
+    ``modules`` telescope modules): energy + gradient of all of them, problem
+    after problem on one stream, as one CUDA-graph launch of the same pass with
+    the problems spread over ``n_streams`` branches, and as grouped launches."""
     import torch
 
     import jubik_gb300 as ju
     from jubik_gb300 import synthetic
 
-    insts = synthetic.config5()
+    if modules == 1:
+        insts = synthetic.config5(count=count)
+    else:
+        insts = [synthetic.config2(nx=g["nx"], dx=g["dx"], margin=g["margin"],
+                                   n_modules=modules, n_energies=g["E"], seed=g["seed"])
+                 for g in synthetic.config5_geometry(count=count)]
     b = ju.ProblemBatch(insts, dtype=torch.float32, n_streams=n_streams, device=dev)
     try:
         lam = b.expected_counts()
@@ -220,7 +226,8 @@ def uneven_batch_leg(dev, n_streams=8, passes=10):
         loop_ms = timed(b.energy_and_grad)
         b.capture()
         graph_ms = timed(b.replay)
-        out = {"problems": len(insts), "mpix_per_pass": b.mpix, "streams": n_streams,
+        out = {"problems": len(insts), "modules": modules, "mpix_per_pass": b.mpix,
+               "streams": n_streams,
                "paths": {str(k): v for k, v in chosen.items()},
                "loop_ms": loop_ms, "graph_ms": graph_ms, "loop_launches": 5 * len(insts),
                "loop_mpix_s": b.mpix / (loop_ms / 1e3), "graph_mpix_s": b.mpix / (graph_ms / 1e3),
@@ -573,6 +580,8 @@ def main():
             comp[name] = {"ms": t, "mpix_s": mpix / (t / 1e3)}
         line["operators"] = comp
         line["uneven_batch"] = uneven_batch_leg(dev)
+        # the same geometry with the 7 modules of an eROSITA field, 16 fields
+        line["uneven_batch_7_modules"] = uneven_batch_leg(dev, modules=7, count=16)
         line["sky_model"] = sky_model_leg(plan, dev, nx, E, mpix)
         line["rel_err_vs_fp64_gpu"] = err
         line["fp64_plain_ms_per_step"] = fp64_ms
