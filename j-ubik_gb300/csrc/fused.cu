@@ -33,6 +33,8 @@
 #include <cstdio>
 #include <algorithm>
 #include <cstring>
+#include <mutex>
+#include <vector>
 
 #include "fft_codelets.cuh"
 #include "internal.h"
@@ -845,11 +847,14 @@ struct OneProblem {
     return a;
   }
 };
+// ProblemList::at returns a copy: the kernels then read the fields from
+// registers or local memory, not through a pointer into global memory that
+// their own stores could alias (which would keep every field access a load).
 struct ProblemList {
   const Args* list;
   const int* starts;
   int n;
-  __device__ __forceinline__ const Args& at(int g, int& local) const {
+  __device__ __forceinline__ Args at(int g, int& local) const {
     int lo = 0, hi = n - 1;  // the last problem whose first index is <= g
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
@@ -940,8 +945,8 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_sky_spec(Src src) {
 }
 
 // ... then, per unit, spectrum * PSF spectrum -> inverse -> overlap-add, as a
-// loop over units (CTA b takes units b, b + G, ...; G = gridDim.x, one CTA per
-// SM).  The next unit's PSF and shared spectra are prefetched into L2 when this
+// loop over units (CTA b takes units b, b + G, ...; G = gridDim.x, as many
+// CTAs as fit on the GPU at once; one per SM at P = 192).  The next unit's PSF and shared spectra are prefetched into L2 when this
 // unit's output stage starts: its reductions leave the HBM reads free, and the
 // data is in L2 when the next unit's spectrum stage reads it.  (Prefetching a
 // whole unit ahead was slower: the prefetches then compete with the current
@@ -991,7 +996,7 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_from_spec(Src src, int uni
 // added into the patch's (zero) accumulator; the CTAs also clear the
 // (E,nx,ny) output that the next kernel adds into when called alone ...
 // A loop over units: CTA b takes units b, b + G, b + 2G, ... (G = gridDim.x,
-// one CTA per SM).  The next unit's first input chunk is issued into the
+// as many CTAs as fit on the GPU at once; one per SM at P = 192).  The next unit's first input chunk is issued into the
 // staging area before this unit's spectrum stage, which leaves the staging
 // area alone: those loads overlap the stage instead of opening the next unit.
 // The next unit's PSF spectrum is prefetched into L2 only once this unit is
@@ -1086,6 +1091,40 @@ int sm_count() {
       cudaDeviceGetAttribute(&n[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     n[dev] = 1;
   return n[dev] > 0 ? n[dev] : 1;
+}
+
+// Grid of a loop kernel over `count` items: as many CTAs as fit on the
+// current device at once (the kernel's occupancy per SM from its shared
+// memory, registers and block size -- one at P = 192, several at small P), at
+// most one per item.  Cached per kernel and device.
+struct OccEntry {
+  const void* kern;
+  int dev, per_sm;
+};
+std::mutex g_occ_mu;
+std::vector<OccEntry> g_occ;
+
+template <typename T, int P, typename KernelT>
+int64_t loop_grid(KernelT kern, int64_t count) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+  int per_sm = 0;
+  {
+    std::lock_guard<std::mutex> lock(g_occ_mu);
+    for (const OccEntry& e : g_occ)
+      if (e.kern == (const void*)kern && e.dev == dev) per_sm = e.per_sm;
+  }
+  if (!per_sm) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, Tr<T, P>::NT,
+                                                      Tr<T, P>::SMEM) != cudaSuccess ||
+        per_sm < 1) {
+      cudaGetLastError();
+      per_sm = 1;
+    }
+    std::lock_guard<std::mutex> lock(g_occ_mu);
+    g_occ.push_back(OccEntry{(const void*)kern, dev, per_sm});
+  }
+  return std::max<int64_t>(1, std::min<int64_t>(count, (int64_t)sm_count() * per_sm));
 }
 
 // Kernel arguments of one stage of one plan (sizes in bytes use esz).
@@ -1203,11 +1242,11 @@ int launch_one(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
       return launch_pdl<T, P>(k_sky_spec<T, P, OneProblem>, patches, f.pdl, s, OneProblem{a});
     case FUSED_FWD_FROM_SPEC:
       return launch_pdl<T, P>(k_fwd_from_spec<T, P, OneProblem>,
-                              std::min<int64_t>(units, sm_count()), f.pdl, s, OneProblem{a},
-                              (int)units);
+                              loop_grid<T, P>(k_fwd_from_spec<T, P, OneProblem>, units), f.pdl,
+                              s, OneProblem{a}, (int)units);
     case FUSED_ADJ_TO_SPEC: {
-      // one CTA per SM, looping over the units
-      const int64_t grid = std::min<int64_t>(units, sm_count());
+      // as many CTAs as fit at once, looping over the units
+      const int64_t grid = loop_grid<T, P>(k_adj_to_spec<T, P, OneProblem>, units);
       Args al = a;
       const int64_t zbytes = (int64_t)g.E * g.pixels() * (int64_t)sizeof(T);
       al.zchunk = ((zbytes + grid - 1) / grid + 15) & ~(int64_t)15;
@@ -1250,15 +1289,16 @@ int launch_group_shared(const void* list, const int* starts, int nprob, int64_t 
     return JUBIK_ERR_UNSUPPORTED;
   }
   const ProblemList src{(const Args*)list, starts, nprob};
-  const int64_t loop_grid = std::min<int64_t>(count, sm_count());
   switch (which) {
     case FUSED_FWD_SKY: return launch_pdl<T, P>(k_sky_spec<T, P, ProblemList>, count, pdl, s, src);
     case FUSED_FWD_FROM_SPEC:
-      return launch_pdl<T, P>(k_fwd_from_spec<T, P, ProblemList>, loop_grid, pdl, s, src,
-                              (int)count);
+      return launch_pdl<T, P>(k_fwd_from_spec<T, P, ProblemList>,
+                              loop_grid<T, P>(k_fwd_from_spec<T, P, ProblemList>, count), pdl, s,
+                              src, (int)count);
     case FUSED_ADJ_TO_SPEC:
-      return launch_pdl<T, P>(k_adj_to_spec<T, P, ProblemList>, loop_grid, pdl, s, src,
-                              (int)count);
+      return launch_pdl<T, P>(k_adj_to_spec<T, P, ProblemList>,
+                              loop_grid<T, P>(k_adj_to_spec<T, P, ProblemList>, count), pdl, s,
+                              src, (int)count);
     case FUSED_ADJ_FROM_SPEC:
       return launch_pdl<T, P>(k_adj_from_spec<T, P, ProblemList>, count, pdl, s, src);
     default:
