@@ -95,3 +95,19 @@ def test_diffuse_coefficients():
     np.testing.assert_allclose(c[:, 0], 1.0)
     np.testing.assert_allclose(c[:, 1], 0.5 * np.log([0.2, 2.0, 9.0]) - np.log(2.0), rtol=1e-15)
     assert jsky.diffuse_coefficients([1.0], [2.0], 1.0, plaw=False).shape == (1, 1)
+
+
+def test_pair_packed_hartley_identity():
+    """The identity the correlated-field kernels use to take two real fields
+    through one complex transform: with Z = fftn(x0 + i x1) and Zm(k) = Z(-k),
+    H x0 = (Re Z + Re Zm + Im Z - Im Zm) / 2 and
+    H x1 = (Im Z + Im Zm + Re Zm - Re Z) / 2."""
+    rng = np.random.default_rng(5)
+    for shape in [(6, 10), (9, 7), (1, 12), (1134, 3)]:
+        x0, x1 = rng.standard_normal(shape), rng.standard_normal(shape)
+        Z = np.fft.fftn(x0 + 1j * x1)
+        Zm = np.roll(np.flip(Z), 1, axis=(0, 1))  # Z at (-k0, -k1) mod the grid
+        h0 = 0.5 * ((Z.real + Zm.real) + (Z.imag - Zm.imag))
+        h1 = 0.5 * ((Z.imag + Zm.imag) + (Zm.real - Z.real))
+        np.testing.assert_allclose(h0, SO.hartley(x0), rtol=0, atol=1e-10 * np.abs(Z).max())
+        np.testing.assert_allclose(h1, SO.hartley(x1), rtol=0, atol=1e-10 * np.abs(Z).max())
