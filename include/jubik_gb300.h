@@ -228,7 +228,9 @@ JUBIK_API int jubik_psf_interpolate(const double* psfs, const double* rs,
  * spectra, then units) for its module-shared problems; and one grouped
  * likelihood pass -- the work of jubik_poisson_energy_grad on every plan.  The
  * plans must outlive the group, and none of them may run another call while a
- * group call is in flight.
+ * group call is in flight.  set_io copies the plans' buffer addresses; after a
+ * plan's jubik_plan_set_exposure (or its first jubik_plan_set_data) the group's
+ * calls return JUBIK_ERR_STATE until set_io runs again.
  * set_io: the device sky and gradient buffer of each problem (x[i], grad[i],
  * shaped (E,nx,ny) of plan i) and a device double[n] for the energies; they
  * are read at every later call. */
@@ -304,7 +306,9 @@ JUBIK_API int jubik_dot(const void* a, const void* b, int64_t n, int32_t dtype, 
  * JUBIK_NOALLOC_SCRATCH_BYTES per GPU, held until the process exits; inputs needing
  * more scratch are rejected with JUBIK_ERR_INVALID_ARGUMENT.  The first call on a
  * device looks up the array's address (set-up work: make it before any stream
- * capture).  Every call shares the array: calls that overlap on the GPU race. */
+ * capture); the address is cached for the device's context, so a process that
+ * destroys that context (cudaDeviceReset) must not call this entry point again.
+ * Every call shares the array: calls that overlap on the GPU race. */
 #define JUBIK_NOALLOC_SCRATCH_BYTES (16 * 1024 * 1024)
 JUBIK_API int jubik_convolve2d_noalloc(const void* kernel, int64_t bk, const void* signal,
                                        int64_t bs, int32_t h, int32_t w, double dvol,

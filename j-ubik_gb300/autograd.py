@@ -4,6 +4,11 @@ The response is linear in the sky, so its JVP is the forward kernel on the
 tangent and its VJP is the hand-written adjoint kernel (correlation with the
 PSF, transposed overlap-add, transposed exposure and readout).  The Poisson
 energy returns its gradient from the same fused forward+adjoint pass.
+
+A plan holds one set of PSF spectra at a time, and callers may give it other
+kernels between a forward pass and its backward pass (two kernels on one
+geometry in one graph).  Every node therefore keeps a snapshot of the PSF its
+forward used and restores it before it runs the adjoint.
 """
 from __future__ import annotations
 
@@ -15,12 +20,18 @@ class PsfOpFn(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, x, plan):
-        ctx.plan = plan
+        ctx.plan, ctx.psf = plan, plan.psf_snapshot()
         return plan.psf_forward(x)
 
     @staticmethod
     def backward(ctx, g):
+        ctx.plan.restore_psf(ctx.psf)
         return ctx.plan.psf_adjoint(g.contiguous()), None
+
+    @staticmethod
+    def jvp(ctx, t, _):
+        ctx.plan.restore_psf(ctx.psf)
+        return ctx.plan.psf_forward(t)
 
 
 class ResponseFn(torch.autograd.Function):
@@ -28,15 +39,17 @@ class ResponseFn(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, x, plan):
-        ctx.plan = plan
+        ctx.plan, ctx.psf = plan, plan.psf_snapshot()
         return plan.response(x)
 
     @staticmethod
     def backward(ctx, g):
+        ctx.plan.restore_psf(ctx.psf)
         return ctx.plan.response_vjp(g.contiguous()), None
 
     @staticmethod
     def jvp(ctx, t, _):
+        ctx.plan.restore_psf(ctx.psf)
         return ctx.plan.response(t)
 
 

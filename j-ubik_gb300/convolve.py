@@ -84,7 +84,11 @@ def slice_patches_adjoint(patches, shape, n_patches_per_axis, additional_margin)
 
 # ---------------------------------------------------------------- linpatch
 class _PlanCache:
-    """Plans keyed by geometry, PSF spectra keyed by the kernel tensor."""
+    """Plans keyed by geometry (the PSF spectra a plan holds carry their own key).
+
+    An evicted plan is only dropped from the cache, never closed: an autograd
+    graph that still holds it runs its backward pass on it, and the plan frees
+    its device memory when the last reference goes."""
 
     def __init__(self, capacity: int = 8):
         self.capacity = capacity
@@ -93,16 +97,13 @@ class _PlanCache:
     def get(self, key, make):
         ent = self.plans.pop(key, None)
         if ent is None:
-            ent = {"plan": make(), "psf_key": None}
+            ent = {"plan": make()}
             while len(self.plans) >= self.capacity:
-                old = self.plans.pop(next(iter(self.plans)))
-                old["plan"].close()
+                self.plans.pop(next(iter(self.plans)))
         self.plans[key] = ent
         return ent
 
     def clear(self):
-        for ent in self.plans.values():
-            ent["plan"].close()
         self.plans.clear()
 
 
@@ -139,29 +140,39 @@ def linpatch_plan(x_shape, kernel_shape, n_patches_per_axis, margin, dtype, n_mo
 
 def _prepare_kernel(ent, src, kernel: torch.Tensor, E: int, field):
     """Kernels shaped like the field are full-field kernels (the reference's
-    input, cut by convolve.py:107-111); any other window is taken as pre-cut."""
+    input, cut by convolve.py:107-111); any other window is taken as pre-cut.
+    The plan's spectra are recomputed only when the kernel changed."""
     plan: ResponsePlan = ent["plan"]
     key, keep = _kernel_key(src)
-    if ent["psf_key"] == key:
+    if plan.psf_key == key:
         return
     n2 = plan.n_patches ** 2
-    if kernel.dim() == 3:  # (n^2, k, k): one kernel for every energy
-        k = kernel.unsqueeze(0)
-    else:
-        k = kernel.reshape(1, n2, E, kernel.shape[-2], kernel.shape[-1])
-    plan.set_psf(k, "full" if tuple(kernel.shape[-2:]) == tuple(field) else "precut")
-    ent["psf_key"], ent["psf_src"] = key, keep
+    layout = "full" if tuple(kernel.shape[-2:]) == tuple(field) else "precut"
+    kshape = tuple(kernel.shape)
+
+    def shaped(k):
+        if len(kshape) == 3:  # (n^2, k, k): one kernel for every energy
+            return k.unsqueeze(0)
+        return k.reshape(1, n2, E, kshape[-2], kshape[-1])
+
+    def again():  # the kernel as the caller passed it, on the device again
+        return shaped(as_device(keep, plan.dtype, plan.device))
+
+    plan.set_psf(shaped(kernel), layout, key=key, source=again,
+                 watch=keep if isinstance(keep, torch.Tensor) else None)
 
 
 class _LinpatchFn(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x, plan):
-        ctx.plan = plan
+        # the plan may hold another kernel when the backward pass runs
+        ctx.plan, ctx.psf = plan, plan.psf_snapshot()
         return plan.psf_forward(x)[0] if plan.n_modules == 1 else plan.psf_forward(x)
 
     @staticmethod
     def backward(ctx, g):
         plan = ctx.plan
+        plan.restore_psf(ctx.psf)
         gg = g.unsqueeze(0) if plan.n_modules == 1 else g
         return plan.psf_adjoint(gg.contiguous()), None
 

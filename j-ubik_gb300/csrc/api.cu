@@ -253,6 +253,9 @@ struct jubik_plan {
   int zu_modules = 0;
   // state
   bool psf_set = false, exposure_set = false, data_set = false, lam_valid = false;
+  // bumped whenever a buffer address or the readout map that a group copied in
+  // jubik_group_set_io changes (exposure set or dropped, data buffers allocated)
+  uint64_t layout_gen = 0;
   std::vector<int64_t> readout_sizes;
   int64_t readout_total = 0;
   std::vector<void*> allocs;
@@ -763,6 +766,7 @@ int jubik_plan_set_exposure(jubik_plan* p, const void* exposure, const uint8_t* 
   p->exposure_set = true;
   p->data_set = false;
   p->lam_valid = false;
+  ++p->layout_gen;
   return JUBIK_OK;
 }
 
@@ -787,6 +791,7 @@ int jubik_plan_set_data(jubik_plan* p, const int32_t* counts, void* stream) {
     set_error("counts is NULL");
     return JUBIK_ERR_INVALID_ARGUMENT;
   }
+  if (!p->data || !p->dimg) ++p->layout_gen;
   if (!p->data) JUBIK_TRY(p->alloc((void**)&p->data, image_elems(p) * sizeof(int32_t)));
   if (!p->dimg) JUBIK_TRY(p->alloc((void**)&p->dimg, image_elems(p) * sizeof(int32_t)));
   JUBIK_TRY_CUDA(cudaMemcpyAsync(p->data, counts, p->readout_total * sizeof(int32_t),
@@ -1018,6 +1023,10 @@ int jubik_convolve2d(const void* kernel, int64_t bk, const void* signal, int64_t
     set_error("convolve2d: invalid shapes (kernel batch must divide the signal batch)");
     return JUBIK_ERR_INVALID_ARGUMENT;
   }
+  if (dtype != JUBIK_F32 && dtype != JUBIK_F64) {
+    set_error("convolve2d: dtype must be JUBIK_F32 or JUBIK_F64");
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
   cudaStream_t s = S(stream);
   Fft1D fh, fw;
   JUBIK_TRY(fft1d_init(&fh, h));
@@ -1063,6 +1072,7 @@ struct GroupClass {
 
 struct jubik_group {
   std::vector<jubik_plan*> plans;
+  std::vector<uint64_t> gens;  // each plan's layout_gen when set_io copied its buffers
   int dtype = JUBIK_F32;
   std::vector<GroupClass> classes;
   PoissonJob* pjobs = nullptr;
@@ -1241,6 +1251,8 @@ int jubik_group_set_io(jubik_group* g, const void* const* x, void* const* grad,
   JUBIK_TRY(upload(g, ps, &g->pstarts));
   JUBIK_TRY(upload(g, zj, &g->zjobs));
   JUBIK_TRY(upload(g, zs, &g->zstarts));
+  g->gens.clear();
+  for (jubik_plan* p : g->plans) g->gens.push_back(p->layout_gen);
   g->io_set = true;
   return JUBIK_OK;
 }
@@ -1253,6 +1265,14 @@ int jubik_group_energy_grad(jubik_group* g, void* stream) {
   }
   cudaStream_t s = S(stream);
   const int n = (int)g->plans.size();
+  for (int i = 0; i < n; ++i) {
+    const jubik_plan* p = g->plans[i];
+    if (p->layout_gen != g->gens[i] || !p->data_set) {
+      set_error("group: plan %d changed its exposure, readout or data buffers since "
+                "jubik_group_set_io (or has no data); call jubik_group_set_io again", i);
+      return JUBIK_ERR_STATE;
+    }
+  }
   JUBIK_TRY(zero_group_run(g->zjobs, g->zstarts, g->nzero, g->zblocks, true, s));
   for (auto& c : g->classes) {
     const int m = (int)c.members.size();

@@ -20,7 +20,9 @@
 // stand-in, not a device address): the first call on each device, with that
 // device current, looks the address up with cudaGetSymbolAddress and caches
 // it.  That first call therefore performs set-up work and should come before
-// any stream capture.
+// any stream capture.  The cached address belongs to the device's current
+// context: a caller that destroys it (cudaDeviceReset) must not call this entry
+// point again in the same process.
 #include <cstdio>
 #include <mutex>
 
@@ -77,7 +79,15 @@ int jubik_convolve2d_noalloc(const void* kernel, int64_t bk, const void* signal,
   }
   // scratch layout: twiddles (h, then w: float2 then double2), kernel spectra, signal spectra
   const size_t csz = dtype == JUBIK_F32 ? sizeof(float2) : sizeof(double2);
-  const size_t hw = (size_t)h * (size_t)w;
+  const size_t hw = (size_t)h * (size_t)w;  // h, w <= 4096: no overflow
+  // bound the plane counts before multiplying, so that no product wraps
+  const size_t max_planes = (size_t)JUBIK_NOALLOC_SCRATCH_BYTES / (csz * hw);
+  if ((uint64_t)bk > max_planes || (uint64_t)bs > max_planes) {
+    set_error("convolve2d_noalloc: %lld kernel and %lld signal planes of %d x %d exceed the "
+              "static scratch of %d bytes (use jubik_convolve2d)",
+              (long long)bk, (long long)bs, h, w, JUBIK_NOALLOC_SCRATCH_BYTES);
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
   const size_t tw_h32 = 0;
   const size_t tw_h64 = tw_h32 + align256(sizeof(float2) * h);
   const size_t tw_w32 = tw_h64 + align256(sizeof(double2) * h);

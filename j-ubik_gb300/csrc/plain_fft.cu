@@ -9,6 +9,7 @@
 // by the stand-alone convolve.  Stage s with radix r and running length Ns:
 //   v_q = in[j + q L/r] * w^(q k),  k = j mod Ns,  w = exp(-2 pi i / (Ns r))
 //   out[(j / Ns) Ns r + k + q Ns] = DFT_r(v)_q
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -317,13 +318,20 @@ bool factorize(int L, FftStages* st) {
 
 constexpr int kMaxL = 4096;
 
+// Opt-in shared memory per block of the current device (cached per device).
 int max_smem_optin() {
-  static int v = -1;
-  if (v < 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+  constexpr int kMaxDev = 64;
+  static std::atomic<int> cache[kMaxDev];  // 0 = not looked up yet
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return 48 * 1024;
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (v <= 0) {
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+        v <= 0) {
+      cudaGetLastError();
       v = 48 * 1024;
+    }
+    cache[dev].store(v, std::memory_order_relaxed);
   }
   return v;
 }
@@ -352,10 +360,17 @@ int fft1d_init(Fft1D* f, int L) {
     t64[t] = make_double2((double)c, (double)s);
     t32[t] = make_float2((float)c, (float)s);
   }
-  JUBIK_TRY_CUDA(cudaMalloc(&f->tw32, sizeof(float2) * L));
-  JUBIK_TRY_CUDA(cudaMalloc(&f->tw64, sizeof(double2) * L));
-  JUBIK_TRY_CUDA(cudaMemcpy(f->tw32, t32.data(), sizeof(float2) * L, cudaMemcpyHostToDevice));
-  JUBIK_TRY_CUDA(cudaMemcpy(f->tw64, t64.data(), sizeof(double2) * L, cudaMemcpyHostToDevice));
+  f->tw32 = f->tw64 = nullptr;
+  cudaError_t e = cudaMalloc(&f->tw32, sizeof(float2) * L);
+  if (e == cudaSuccess) e = cudaMalloc(&f->tw64, sizeof(double2) * L);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(f->tw32, t32.data(), sizeof(float2) * L, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(f->tw64, t64.data(), sizeof(double2) * L, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {  // release whatever was allocated before the failure
+    fft1d_free(f);
+    return cuda_status(e, "fft1d_init");
+  }
   return JUBIK_OK;
 }
 

@@ -43,12 +43,17 @@ def build_psf_op(domain, npatch: int, margin: int, dtype: torch.dtype = torch.fl
         if plan is None or plan.n_modules != M:
             plan = ResponsePlan(M, E, shape[-2:], npatch, margin, dtype=dtype, path=path,
                                 device=dev)
-            state["plan"], state["key"] = plan, None
+            state["plan"] = plan
         key, keep = _kernel_key(kernel)
-        if state["key"] != key:
-            kk = k if k.dim() == 4 else k.reshape(M, npatch ** 2, E, k.shape[-2], k.shape[-1])
-            plan.set_psf(kk)
-            state["key"], state["keep"] = key, keep
+        if plan.psf_key != key:
+            kshape = tuple(k.shape)
+
+            def shaped(t):
+                return t if len(kshape) == 4 else t.reshape(M, npatch ** 2, E, kshape[-2],
+                                                             kshape[-1])
+
+            plan.set_psf(shaped(k), key=key, source=lambda: shaped(as_device(keep, dtype, dev)),
+                         watch=keep if isinstance(keep, torch.Tensor) else None)
         xt = x if isinstance(x, torch.Tensor) else torch.as_tensor(np.asarray(x))
         xt = xt.to(device=dev, dtype=dtype).reshape((E,) + shape[-2:])
         out = PsfOpFn.apply(xt, plan)
@@ -84,9 +89,7 @@ class Response:
         self.pixel_area = float(pixel_area)
         self.plan = ResponsePlan(self.M, self.E, shape[-2:], n_patch, margin, dtype=dtype,
                                  path=path, pixel_area=self.pixel_area, device=dev)
-        self.plan.set_psf(k if k.dim() == 4 else
-                          k.reshape(self.M, n_patch ** 2, self.E, k.shape[-2], k.shape[-1]))
-        self._kernel_key, self._kernel_keep = _kernel_key(kernel)
+        self._use_kernel(kernel, k)
         self.kernel = k
         full = (self.M, self.E) + shape[-2:]
         exp = None
@@ -112,6 +115,23 @@ class Response:
             raise ValueError("length of keys should match the number of flag maps.")
         self.plan.set_exposure(exp, readmask)
 
+    def _use_kernel(self, src, kt=None) -> None:
+        """Give the plan the kernels ``src`` unless it holds them already."""
+        key, keep = _kernel_key(src)
+        if self.plan.psf_key == key:
+            return
+        plan, M, E = self.plan, self.M, self.E
+
+        def shaped(t):
+            return t if t.dim() == 4 else t.reshape(M, plan.n_patches ** 2, E, t.shape[-2],
+                                                    t.shape[-1])
+
+        if kt is None:
+            kt = as_device(src, plan.dtype, plan.device)
+        plan.set_psf(shaped(kt), key=key,
+                     source=lambda: shaped(as_device(keep, plan.dtype, plan.device)),
+                     watch=keep if isinstance(keep, torch.Tensor) else None)
+
     def _sky(self, x):
         dev = self.plan.device
         xt = x if isinstance(x, torch.Tensor) else torch.as_tensor(np.asarray(x))
@@ -123,12 +143,7 @@ class Response:
 
     def __call__(self, x, k=None) -> Vector:
         if k is not None:
-            key, keep = _kernel_key(k)
-            if key != self._kernel_key:
-                kt = as_device(k, self.plan.dtype, self.plan.device)
-                self.plan.set_psf(kt if kt.dim() == 4 else kt.reshape(
-                    self.M, self.plan.n_patches ** 2, self.E, kt.shape[-2], kt.shape[-1]))
-                self._kernel_key, self._kernel_keep = key, keep
+            self._use_kernel(k)
         parts = torch.split(self.flat(x), self.plan.readout_sizes)
         return Vector(dict(zip(self.keys, parts)))
 
@@ -140,6 +155,8 @@ class Response:
 
     def psf(self, x, k=None):
         """(M, E, N, N) PSF images without pixel area (the vmapped linpatch)."""
+        if k is not None:
+            self._use_kernel(k)
         out = PsfOpFn.apply(self._sky(x), self.plan)
         return out.reshape((self.M,) + self.shape)
 

@@ -56,6 +56,29 @@ def ptr(t: Optional[torch.Tensor]) -> C.c_void_p:
     return C.c_void_p(0 if t is None else t.data_ptr())
 
 
+class PsfSnapshot:
+    """The PSF a plan held when an operator ran: its key and a way to set it
+    again.  Autograd nodes keep one, so that a backward pass that runs after the
+    plan was given another kernel first restores the kernel of its forward."""
+
+    __slots__ = ("key", "source", "layout", "watch", "version")
+
+    def __init__(self, key, source, layout, watch=None):
+        self.key, self.source, self.layout = key, source, layout
+        # in-place edits of a tensor kernel after the forward are an error, as
+        # for any tensor that autograd saved
+        if watch is None and isinstance(source, torch.Tensor):
+            watch = source
+        self.watch = watch if isinstance(watch, torch.Tensor) else None
+        self.version = self.watch._version if self.watch is not None else None
+
+    def kernel(self):
+        if self.watch is not None and self.watch._version != self.version:
+            raise RuntimeError("the PSF kernel of this response was modified in place after the "
+                               "forward pass; its gradient cannot be computed")
+        return self.source() if callable(self.source) else self.source
+
+
 class ResponsePlan:
     """Plan for ``R(x) = mask(exposure(psf(x * pixel_area)))`` on one GPU.
 
@@ -99,6 +122,8 @@ class ResponsePlan:
         self.shared_spectra = self.path == "fused" and path != "fused_unit" and self.n_modules >= 2
         self._refresh_readout()
         self._keep = []  # tensors the plan reads asynchronously
+        self.psf_key = None  # identifies the PSF spectra the plan holds
+        self._psf = None     # PsfSnapshot of them
 
     # -------------------------------------------------------------- state
     def close(self):
@@ -147,10 +172,35 @@ class ResponsePlan:
         self.readout_sizes = [int(v) for v in sizes]
         self.readout_total = int(tot.value)
 
-    def set_psf(self, psf, layout: str = "auto") -> "ResponsePlan":
+    def set_psf(self, psf, layout: str = "auto", key=None, source=None,
+                watch=None) -> "ResponsePlan":
         """PSF kernels: (M, n^2, E, K, K) pre-cut windows or (M, n^2, E, nx, ny)
         full-field kernels; an array without the E axis is broadcast over
-        energies (``convolve.py:167-171``)."""
+        energies (``convolve.py:167-171``).
+
+        ``key`` names these kernels (a fresh token when None) and becomes
+        ``psf_key``; ``source`` (default: ``psf`` itself) is what
+        :meth:`restore_psf` sets again -- a tensor, or a callable returning the
+        kernels, so that a snapshot need not hold a device copy; ``watch`` is
+        the caller's tensor whose in-place edits invalidate the snapshot."""
+        self._set_psf(psf, layout)
+        self.psf_key = key if key is not None else object()
+        self._psf = PsfSnapshot(self.psf_key, psf if source is None else source, layout,
+                                watch=watch)
+        return self
+
+    def psf_snapshot(self) -> Optional[PsfSnapshot]:
+        """The PSF the plan holds now (for :meth:`restore_psf`)."""
+        return self._psf
+
+    def restore_psf(self, snap: Optional[PsfSnapshot]) -> None:
+        """Set the PSF of ``snap`` again if the plan holds another one."""
+        if snap is None or (self.psf_key is snap.key or self.psf_key == snap.key):
+            return
+        self._set_psf(snap.kernel(), snap.layout)
+        self.psf_key, self._psf = snap.key, snap
+
+    def _set_psf(self, psf, layout: str) -> None:
         t = as_device(psf, self.dtype, self.device)
         n2 = self.n_patches ** 2
         if t.dim() == 4:
@@ -175,7 +225,6 @@ class ResponsePlan:
         code = _lib.PSF_PRECUT if layout == "precut" else _lib.PSF_FULL
         _lib.call("jubik_plan_set_psf", self._h, ptr(t), code, bcast, self._s())
         torch.cuda.current_stream(self.device).synchronize()
-        return self
 
     def set_exposure(self, exposure=None, readmask=None) -> "ResponsePlan":
         """exposure (M,E,nx,ny) (None = ones); readmask (M,E,nx,ny) bool, True

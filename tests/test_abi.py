@@ -91,3 +91,19 @@ def test_group_and_cf_argument_errors_without_a_gpu():
     assert lib.jubik_cf_apply(None, None, None, None, None, None, 0, 0, 0, None, None) == \
         _lib.ERR_INVALID_ARGUMENT
     assert lib.jubik_cf_destroy(None) == _lib.OK
+
+
+@pytest.mark.skipif(not _built(), reason="library not built")
+def test_convolve2d_argument_errors_without_a_gpu():
+    """Both convolution entries reject an unknown dtype, and the allocation-free
+    one rejects plane counts whose scratch would overflow, before any CUDA call."""
+    lib = _lib.load()
+    dummy = ctypes.c_void_p(16)  # never dereferenced: the checks run first
+    for name in ("jubik_convolve2d", "jubik_convolve2d_noalloc"):
+        fn = getattr(lib, name)
+        assert fn(dummy, 1, dummy, 1, 8, 8, 1.0, 5, dummy, None) == _lib.ERR_INVALID_ARGUMENT
+        assert "dtype" in _lib.last_error() or "invalid" in _lib.last_error()
+    huge = 1 << 62  # bk * h * w * 16 would wrap around 2^64
+    assert lib.jubik_convolve2d_noalloc(dummy, huge, dummy, huge, 64, 64, 1.0, _lib.F64, dummy,
+                                        None) == _lib.ERR_INVALID_ARGUMENT
+    assert "exceed" in _lib.last_error()

@@ -190,3 +190,27 @@ def test_group_refuses_unfused_problems(cuda):
         assert np.isfinite(float(e[0]))
     finally:
         b.close()
+
+
+def test_group_refuses_plans_changed_after_set_io(cuda, small_batch):
+    """A group copies its plans' buffer addresses and readout maps at set_io: a
+    plan that gets a new exposure afterwards makes the group's calls fail with
+    a state error (instead of reading freed or stale buffers) until set_io."""
+    insts, refs = small_batch
+    b = ju.ProblemBatch(insts, dtype=torch.float32, n_streams=2)
+    try:
+        b.set_data([r["data"] for r in refs])
+        assert b.group()
+        b.energy_and_grad()
+        b.plans[0].set_exposure(None, insts[0].readmask)  # drops the exposure buffer
+        with pytest.raises(ju.JubikError, match="set_io"):
+            b.energy_and_grad()
+        b.plans[0].set_exposure(insts[0].exposure, insts[0].readmask)
+        b.plans[0].set_data(refs[0]["data"])
+        assert b.group()  # set_io again
+        e, _ = b.energy_and_grad()
+        torch.cuda.synchronize()
+        for k, r in enumerate(refs):
+            assert abs(float(e[k]) - r["energy"]) / abs(r["energy"]) < 1e-6
+    finally:
+        b.close()

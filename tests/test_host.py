@@ -108,3 +108,40 @@ def test_kernel_cache_keys_distinguish_new_arrays():
     kt, _ = _kernel_key(t)
     t.mul_(2.0)                                         # in-place edit bumps the version
     assert _kernel_key(t)[0] != kt
+
+
+def test_psf_snapshot_restore_logic():
+    """Host logic of the PSF snapshots that autograd nodes keep (no GPU): a
+    plan given another kernel re-applies the snapshot's kernel, and only then."""
+    import torch
+    from jubik_gb300.plan import PsfSnapshot, ResponsePlan
+
+    plan = ResponsePlan.__new__(ResponsePlan)  # no device plan: record the uploads
+    applied = []
+    plan._set_psf = lambda psf, layout: applied.append((psf, layout))
+    plan.psf_key, plan._psf = None, None
+    ka, kb = torch.ones(3), torch.zeros(3)
+    ResponsePlan.set_psf(plan, ka, "precut", key=("a",))
+    snap_a = plan.psf_snapshot()
+    ResponsePlan.set_psf(plan, kb, "precut", key=("b",))
+    assert plan.psf_key == ("b",) and len(applied) == 2
+    plan.restore_psf(snap_a)
+    assert plan.psf_key == ("a",) and applied[-1][0] is ka and len(applied) == 3
+    plan.restore_psf(snap_a)  # already held: nothing is uploaded
+    assert len(applied) == 3
+    # a callable source is evaluated when the snapshot is restored
+    ResponsePlan.set_psf(plan, kb, "full", source=lambda: "again")
+    snap_c = plan.psf_snapshot()
+    ResponsePlan.set_psf(plan, ka, "precut")
+    plan.restore_psf(snap_c)
+    assert applied[-1] == ("again", "full")
+    # an in-place edit of the watched tensor invalidates the snapshot
+    w = torch.ones(2)
+    s = PsfSnapshot(("w",), lambda: w, "precut", watch=w)
+    w.add_(1.0)
+    try:
+        s.kernel()
+    except RuntimeError as e:
+        assert "modified in place" in str(e)
+    else:
+        raise AssertionError("expected RuntimeError")
