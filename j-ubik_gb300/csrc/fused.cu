@@ -32,6 +32,7 @@
 // into the first inverse row phase.
 #include <cstdio>
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -1081,18 +1082,6 @@ int set_smem(KernelT kern, size_t smem) {
       "cudaFuncSetAttribute");
 }
 
-// Streaming multiprocessors of the current device (cached per device).
-int sm_count() {
-  constexpr int kMaxDev = 64;
-  static int n[kMaxDev] = {};
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return 1;
-  if (!n[dev] &&
-      cudaDeviceGetAttribute(&n[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-    n[dev] = 1;
-  return n[dev] > 0 ? n[dev] : 1;
-}
-
 // Grid of a loop kernel over `count` items: as many CTAs as fit on the
 // current device at once (the kernel's occupancy per SM from its shared
 // memory, registers and block size -- one at P = 192, several at small P), at
@@ -1371,6 +1360,23 @@ int dispatch(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
 }
 
 }  // namespace
+
+// Streaming multiprocessors of the current device (cached per device).
+int sm_count() {
+  constexpr int kMaxDev = 64;
+  static std::atomic<int> n[kMaxDev];  // 0 = not looked up yet
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return 1;
+  int v = n[dev].load(std::memory_order_relaxed);
+  if (v <= 0) {
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v < 1) {
+      cudaGetLastError();
+      v = 1;
+    }
+    n[dev].store(v, std::memory_order_relaxed);
+  }
+  return v;
+}
 
 bool fused_supported(int P, int dtype) {
   switch (P) {

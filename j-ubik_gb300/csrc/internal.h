@@ -24,6 +24,9 @@ int cuda_status(cudaError_t err, const char* what);
     if (_s != JUBIK_OK) return _s;   \
   } while (0)
 
+// Streaming multiprocessors of the current device (cached per device).
+int sm_count();
+
 // ------------------------------------------------------------------ geometry
 // Patch geometry of jubik/convolve.py:43-63 / :102-143 (square patches).
 struct Geom {

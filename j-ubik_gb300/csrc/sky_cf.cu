@@ -48,7 +48,7 @@ struct ECoef {
 
 unsigned blocks_for(int64_t n) {
   const int64_t b = (n + kThreads - 1) / kThreads;
-  return (unsigned)std::min<int64_t>(std::max<int64_t>(b, 1), 152 * 16);
+  return (unsigned)std::min<int64_t>(std::max<int64_t>(b, 1), (int64_t)sm_count() * 16);
 }
 
 // The per-pixel kernels run a 2-D grid: blockIdx.y is the row y of the padded

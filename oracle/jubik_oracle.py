@@ -22,15 +22,20 @@ It restates, in float64 numpy / scipy.fft, the reference algorithm of
   values is unpinned: no reference test fixes them (the only test swaps in
   a fake, ``test/instruments/chandra/test_chandra_response_wrappers.py:80-88``).
 
-Parity pins: the known answers of the reference's own tests
-(``test/test_convolve.py``, ``test/test_slice_patches.py``,
-``test/test_build_exposure_function.py``,
-``test/test_build_exposure_readout_function.py``, ``test/test_utils.py:66-68``)
-are re-asserted against this module in ``tests/test_oracle_pins.py``; an
-independent direct (non-FFT) C restatement in ``oracle/direct_linpatch.c``
-cross-checks ``linpatch_convolve`` end to end.  The reference itself (JAX)
-cannot be imported where this oracle runs, so end-to-end
-``linpatch_convolve`` parity is pinned only through those two routes.
+Parity pins:
+* outputs of the reference's own ``convolve.py`` / ``response.py`` /
+  ``utils.py``, run unmodified through a numpy stand-in of the JAX calls they
+  make (``tests/golden/make_ref_fixtures.py``, which first runs the reference's
+  tests for those files through the stand-in): ``tests/test_ref_fixtures.py``
+  checks this module against them (slicing, readout and patch centres
+  bit-exact, ``linpatch_convolve`` and its VJP to 1e-13 / 1e-12);
+* the known answers of the reference's own tests
+  (``test/test_convolve.py``, ``test/test_slice_patches.py``,
+  ``test/test_build_exposure_function.py``,
+  ``test/test_build_exposure_readout_function.py``, ``test/test_utils.py:66-68``),
+  re-asserted against this module in ``tests/test_oracle_pins.py``;
+* an independent direct (non-FFT) C restatement in ``oracle/direct_linpatch.c``
+  that cross-checks ``linpatch_convolve`` end to end.
 """
 from __future__ import annotations
 

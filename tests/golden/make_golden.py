@@ -1,9 +1,12 @@
-"""Generate the small golden fixtures of tests/golden/*.npz from the oracle.
+"""Generate the small golden fixtures of tests/golden/{slice36,linpatch48,response32}.npz.
 
-The reference (JAX + NIFTy.re) cannot be imported where these were made, so
-the fixtures freeze the float64 oracle's outputs on seeded inputs; the
-oracle itself is pinned by the reference's known-answer tests
-(tests/test_oracle_pins.py).  Run: ``python tests/golden/make_golden.py``.
+These freeze the float64 oracle's outputs on seeded inputs, including the
+composed response and Poisson energy that the reference's patch files do not
+compute on their own.  The oracle itself is pinned to the reference's code by
+the fixtures of ``make_ref_fixtures.py`` (outputs of the reference's own
+``convolve.py`` / ``response.py`` / ``utils.py``) and by the reference's
+known-answer tests (tests/test_oracle_pins.py).
+Run: ``python tests/golden/make_golden.py``.
 """
 import os
 import sys
