@@ -153,6 +153,132 @@ __device__ __forceinline__ void red_add_cx(double2* p, double2 v) {
   atomicAdd(&p->y, v.y);
 }
 
+// ---- exact, order-independent accumulation in two words
+// Atomic reductions add in whatever order the patches arrive, and floating
+// point addition rounds differently in different orders.  Each term v of an
+// overlap-add is therefore split into two words whose sums are exact:
+//   hi = v rounded to a multiple of Q1,   lo = (v - hi) rounded to a multiple of Q2,
+// with Q1 = 2^(e - (D - 2)) for a bound 2^e > B on every term and partial sum
+// (D = significand bits of T) and Q2 = Q1 * 2^(L + 1 - D) for at most 2^L terms
+// per element.  Multiples of Q below 2^D * Q in magnitude add exactly in T, so the
+// hi words and the lo words each reach the same bits in any order; the result
+// hi + lo (one rounding) is within 2^L * Q2 / 2 of the exact sum of the terms,
+// about B * 2^(2L + 2 - 2D) -- far below the rounding of the FFT that made them.
+// Rounding to a grid is one add and one subtract of 1.5 * 2^(D-1) * Q.
+template <typename T>
+struct Split2 {
+  T m1, m2;
+  __device__ __forceinline__ void init(double bound, int L) {
+    constexpr int D = sizeof(T) == 4 ? 24 : 53;
+    constexpr int EMIN = sizeof(T) == 4 ? -75 : -900, EMAX = sizeof(T) == 4 ? 120 : 1000;
+    if (!(bound <= 1.0e308)) {  // a NaN or infinite input: every result becomes NaN
+      m1 = m2 = (T)NAN;
+      return;
+    }
+    int e = 0;
+    frexp(bound, &e);  // bound < 2^e
+    e = e < EMIN ? EMIN : (e > EMAX ? EMAX : e);
+    const int q1 = e - (D - 2), q2 = q1 + L + 1 - D;
+    m1 = (T)ldexp(1.5, q1 + D - 1);
+    m2 = (T)ldexp(1.5, q2 + D - 1);
+  }
+  __device__ __forceinline__ void split(T v, T& hi, T& lo) const {
+    if constexpr (sizeof(T) == 4) {
+      hi = __fsub_rn(__fadd_rn(v, m1), m1);
+      lo = __fsub_rn(v, hi);
+      lo = __fsub_rn(__fadd_rn(lo, m2), m2);
+    } else {
+      hi = __dsub_rn(__dadd_rn(v, m1), m1);
+      lo = __dsub_rn(v, hi);
+      lo = __dsub_rn(__dadd_rn(lo, m2), m2);
+    }
+  }
+};
+
+// Magnitude maxima travel as the bits of a non-negative double: unsigned
+// comparison of those bits orders them, and a NaN sorts above every number.
+__device__ __forceinline__ unsigned long long mag_bits(double v) {
+  return (unsigned long long)__double_as_longlong(fabs(v));
+}
+__device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) {
+  return a > b ? a : b;
+}
+// CTA-wide maximum of one value per thread (every thread gets it); uses s_slot.
+__device__ __forceinline__ unsigned long long cta_max(unsigned long long v,
+                                                      unsigned long long* s_slot) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = umax64(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if (threadIdx.x == 0) *s_slot = 0ull;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) atomicMax(s_slot, v);
+  __syncthreads();
+  const unsigned long long r = *s_slot;
+  __syncthreads();
+  return r;
+}
+// Maximum of n stored maxima, by the whole CTA.
+__device__ __forceinline__ double reduce_bound(const unsigned long long* p, int n,
+                                               unsigned long long* s_slot) {
+  unsigned long long v = 0ull;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) v = umax64(v, __ldcg(p + i));
+  return __longlong_as_double((long long)cta_max(v, s_slot));
+}
+
+// ---- tensor memory (TMEM) as a per-SM accumulator
+// The adjoint keeps each patch's running sum over modules in tensor memory:
+// 128 lanes x 512 columns of 32 bits per SM, which this kernel's arithmetic
+// does not otherwise use.  Warp w reaches lanes 32 (w % 4) .. 32 (w % 4) + 31;
+// thread (w, lane) owns TMEM lane 32 (w % 4) + lane and the column range of its
+// warp.  Allocation, loads and stores are warp-collective (.sync.aligned).
+__device__ __forceinline__ void tmem_alloc(uint32_t* smem_slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(smem_slot)),
+               "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_fence_before_sync() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_fence_after_sync() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// 32 consecutive 32-bit columns of the thread's lane, from column taddr
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
+      "%28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
+      "%28, %29, %30, %31, %32};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
+      "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]),
+      "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]),
+      "r"(r[29]), "r"(r[30]), "r"(r[31])
+      : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() {
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
 // (a + conj(b)) / 2 and (a - conj(b)) / (2i)
 template <typename T>
 __device__ __forceinline__ cx<T> sp_a(cx<T> a, cx<T> b) {

@@ -10,9 +10,12 @@ import numpy as np
 import pytest
 import torch
 
+import importlib
+
 import jubik_oracle as O
 import jubik_gb300 as ju
-from jubik_gb300 import convolve as jc
+
+jc = importlib.import_module("jubik_gb300.convolve")  # the module (the package exports the function)
 
 pytestmark = pytest.mark.gpu
 
