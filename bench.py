@@ -586,6 +586,23 @@ def main():
         e64, g64 = plan64.energy_and_grad(x64)
         err["energy"] = abs(float(e32) - float(e64)) / abs(float(e64))
         err["grad"] = rel(g32, g64)
+        # the floor that lam's FP32 representation sets: the exact (FP64) lam
+        # rounded once to FP32, everything else in FP64
+        lam64 = plan64.response(x64)
+        lam_r = lam64.float().double()
+        dd = torch.as_tensor(data, device=dev, dtype=torch.float64)
+        err["grad_floor_fp32_lambda"] = rel(plan64.response_vjp(1.0 - dd / lam_r), g64)
+        vm = torch.as_tensor(rng.normal(size=x.shape), device=dev)
+        m64 = plan64.metric(x64, vm)
+        err["metric"] = rel(plan.metric(x, vm.float()), m64)
+        err["metric_floor_fp32_lambda"] = rel(plan64.response_vjp(plan64.response(vm) / lam_r),
+                                              m64)
+        # bitwise reproducibility of the FP32 step
+        e_a, g_a = plan.energy_and_grad(x)
+        e_a, g_a = float(e_a), g_a.clone()
+        e_b, g_b = plan.energy_and_grad(x)
+        torch.cuda.synchronize()
+        line["bitwise_repeatable"] = bool(e_a == float(e_b) and torch.equal(g_a, g_b))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(2):

@@ -154,8 +154,9 @@ JUBIK_API int jubik_metric_apply(jubik_plan* plan, const void* x, const void* v,
  * synchronises on the phase's end event).  Phases: 0 forward per-unit PSF
  * kernel, 1 adjoint per-unit PSF kernel, 2 likelihood / readout kernels,
  * 3 memsets, 4 forward per-patch sky-spectrum kernel, 5 adjoint per-patch
- * inverse kernel (4 and 5 run when modules share patch spectra). */
-#define JUBIK_PHASES 6
+ * inverse kernel (4 and 5 run when modules share patch spectra), 6 the pass
+ * that adds the low words of the gradient's exact two-word sum (fused path). */
+#define JUBIK_PHASES 7
 /* Programmatic dependent launch between the kernels of one plan call (default
  * on; no counterpart in the reference): each kernel may be scheduled onto the
  * SMs the previous kernel's last wave frees, and waits there for that kernel's

@@ -148,14 +148,21 @@ __global__ void k_exp_crop(const T* __restrict__ s, int E, int nx, int ny, int64
 
 // chain rule through sky = exp(s[:E, :nx, :ny]): grad_s = exp(s) * grad_x on the
 // crop, 0 on the rest of the (Ep, n0p, n1p) log-sky array
+// (gx_lo: the low words of a two-word gradient, or nullptr)
 template <typename T>
-__global__ void k_logsky_grad(const T* __restrict__ s, const T* __restrict__ gx, int E, int nx,
-                              int ny, int Ep, int n0p, int n1p, T* __restrict__ gs) {
+__global__ void k_logsky_grad(const T* __restrict__ s, const T* __restrict__ gx,
+                              const T* __restrict__ gx_lo, int E, int nx, int ny, int Ep, int n0p,
+                              int n1p, T* __restrict__ gs) {
   const int64_t n = (int64_t)Ep * n0p * n1p;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t e = i / ((int64_t)n0p * n1p), r = (i / n1p) % n0p, c = i % n1p;
-    gs[i] = (e < E && r < nx && c < ny) ? exp(s[i]) * gx[(e * nx + r) * ny + c] : (T)0;
+    if (e < E && r < nx && c < ny) {
+      const int64_t j = (e * nx + r) * ny + c;
+      gs[i] = exp(s[i]) * (gx_lo ? gx[j] + gx_lo[j] : gx[j]);
+    } else {
+      gs[i] = (T)0;
+    }
   }
 }
 
@@ -231,13 +238,25 @@ struct jubik_plan {
   void* hfull = nullptr;
   void* spec = nullptr;  // per-(energy, patch) spectra shared by the modules
   bool pdl = true;       // programmatic dependent launch between the kernels of a call
-  void* acc = nullptr;   // per-(energy, patch) adjoint sums over modules; all zero between
-                         // calls (zeroed when allocated, cleared by their reader)
+  void* acc = nullptr;   // per-(energy, patch) adjoint sums over modules (written whole by
+                         // the ordered adjoint; grouped launches clear it before they add)
+  // exact two-word accumulation (fused path): low-word planes of the images and
+  // the gradient, the input-magnitude maxima that bound their terms, the spill
+  // slots and grid of the ordered adjoint, and the largest sum of |kernel| over
+  // the units (the PSF's share of the bounds)
+  void* conv_lo = nullptr;
+  void* conv_v_lo = nullptr;
+  void* grad_lo = nullptr;
+  void* bnd_f = nullptr;
+  void* bnd_a = nullptr;
+  void* spill = nullptr;
+  int64_t adj_grid = 0;
+  double kmax = 1.0;
   // images (M,E,nx,ny)
   void* conv = nullptr;
   void* conv_v = nullptr;
   void* resid = nullptr;
-  void* lam = nullptr;
+  void* wts = nullptr;  // metric weights eps^2 / lam of the last lam (image space)
   void* eps = nullptr;
   void* xsky = nullptr;   // (E,nx,ny) sky from a log-sky input (unfused path)
   void* xgrad = nullptr;  // (E,nx,ny) sky gradient before the chain rule to a log-sky
@@ -336,8 +355,25 @@ struct SkyView {
   bool exp = false;
 };
 
-int do_forward(jubik_plan* p, const void* x, void* out, double scale, cudaStream_t s,
-               void* also_zero = nullptr, int64_t also_zero_bytes = 0,
+// log2 of the most terms the two-word sums add per element: the patches that
+// overlap a forward pixel (side P at stride dx, one more for clamped starts),
+// and, for the gradient, the windows (side 2 dx) over a pixel times the modules.
+int terms_log2(int64_t terms) {
+  int L = 0;
+  while ((int64_t(1) << L) < terms) ++L;
+  return L;
+}
+int fwd_terms_log2(const Geom& g) {
+  const int64_t per = (g.P + g.dx - 1) / g.dx + 1;
+  return terms_log2(per * per);
+}
+int adj_terms_log2(const Geom& g) {
+  const int64_t per = (g.K + g.dx - 1) / g.dx + 1;
+  return terms_log2(per * per * g.M);
+}
+
+int do_forward(jubik_plan* p, const void* x, void* out, void* out_lo, double scale,
+               cudaStream_t s, void* also_zero = nullptr, int64_t also_zero_bytes = 0,
                bool* zeroed = nullptr, SkyView view = SkyView()) {
   const Geom& g = p->g;
   if (zeroed) *zeroed = false;
@@ -358,6 +394,12 @@ int do_forward(jubik_plan* p, const void* x, void* out, double scale, cudaStream
     a.in_ps = view.ps;
     a.in_rs = view.rs;
     a.in_exp = view.exp;
+    // the overlap-add is exact in two words: every partial sum of a pixel is
+    // bounded by (terms) x (kernel gain) x |scale| x the largest weighted sky value
+    a.out_lo = out_lo;
+    const int L = fwd_terms_log2(g);
+    a.bnd_log2 = L;
+    a.bnd_scale = 2.0 * (double)(int64_t(1) << L) * p->kmax * std::fabs(scale);
     if (p->spec && also_zero) {
       a.aux = also_zero;
       a.aux_bytes = also_zero_bytes;
@@ -367,15 +409,30 @@ int do_forward(jubik_plan* p, const void* x, void* out, double scale, cudaStream
       {
         Phase ph(p, 3, s);
         JUBIK_TRY_CUDA(cudaMemsetAsync(out, 0, image_elems(p) * p->esz, s));
+        JUBIK_TRY_CUDA(cudaMemsetAsync(out_lo, 0, image_elems(p) * p->esz, s));
       }
       Phase ph(p, 0, s);
+      int nb = 0;
+      const int64_t ps = view.ps > 0 ? view.ps : g.pixels(), rs = view.rs > 0 ? view.rs : g.ny;
+      JUBIK_TRY(p->dtype == JUBIK_F32
+                    ? absmax_blocks<float>(x, g.E, g.nx, g.ny, ps, rs, view.exp, p->bnd_f, &nb,
+                                           p->pdl, s)
+                    : absmax_blocks<double>(x, g.E, g.nx, g.ny, ps, rs, view.exp, p->bnd_f, &nb,
+                                            p->pdl, s));
+      a.bnd_in = p->bnd_f;
+      a.bnd_n = nb;
       return fused_run(g, p->dtype, a, FUSED_FWD_UNITS, s);
     }
-    {  // the sky-spectrum kernel also clears `out` for the overlap-add
+    {  // the sky-spectrum kernel also clears `out` (both words) for the overlap-add
+      // and records each window's largest weighted sky value
       Phase ph(p, 4, s);
+      a.bnd_out = p->bnd_f;
       JUBIK_TRY(fused_run(g, p->dtype, a, FUSED_FWD_SKY, s));
     }
     Phase ph(p, 0, s);
+    a.bnd_out = nullptr;
+    a.bnd_in = p->bnd_f;
+    a.bnd_n = (int)((int64_t)g.E * g.n * g.n);
     return fused_run(g, p->dtype, a, FUSED_FWD_FROM_SPEC, s);
   }
   Phase ph(p, 0, s);
@@ -397,37 +454,59 @@ int do_forward(jubik_plan* p, const void* x, void* out, double scale, cudaStream
   return JUBIK_OK;
 }
 
-// transpose: out_x (E,nx,ny) = scale * sum_m psf_m^T cot[m]
-int do_adjoint(jubik_plan* p, const void* cot, void* out_x, double scale, cudaStream_t s,
-               bool out_zeroed = false) {
+// transpose: out_x (E,nx,ny) = scale * sum_m psf_m^T cot[m]; on the fused path
+// in two words (out_x, out_lo), the caller adding them (combine_words)
+int do_adjoint(jubik_plan* p, const void* cot, void* out_x, void* out_lo, double scale,
+               cudaStream_t s, bool out_zeroed = false) {
   const Geom& g = p->g;
   if (p->path == JUBIK_PATH_FUSED) {
+    const int L = adj_terms_log2(g);
+    // every partial sum of a gradient pixel is bounded by (windows x modules) x
+    // (kernel gain) x |scale| x the largest cotangent magnitude
+    const double bscale = 2.0 * (double)(int64_t(1) << L) * p->kmax * std::fabs(scale);
     if (!p->spec) {
       {
         Phase ph(p, 3, s);
         JUBIK_TRY_CUDA(cudaMemsetAsync(out_x, 0, (size_t)g.E * g.pixels() * p->esz, s));
+        JUBIK_TRY_CUDA(cudaMemsetAsync(out_lo, 0, (size_t)g.E * g.pixels() * p->esz, s));
       }
       FusedLaunch a{cot, out_x, p->hmain, p->hnyq, p->tw, p->wt, scale, nullptr};
       a.pdl = p->pdl;
+      a.out_lo = out_lo;
+      a.bnd_log2 = L;
+      a.bnd_scale = bscale;
       Phase ph(p, 1, s);
+      int nb = 0;
+      JUBIK_TRY(p->dtype == JUBIK_F32
+                    ? absmax_blocks<float>(cot, g.M * g.E, g.nx, g.ny, g.pixels(), g.ny, false,
+                                           p->bnd_a, &nb, p->pdl, s)
+                    : absmax_blocks<double>(cot, g.M * g.E, g.nx, g.ny, g.pixels(), g.ny, false,
+                                            p->bnd_a, &nb, p->pdl, s));
+      a.bnd_in = p->bnd_a;
+      a.bnd_n = nb;
       return fused_run(g, p->dtype, a, FUSED_ADJ_UNITS, s);
     }
-    // per-unit kernel: clears out_x and adds into the (zero) accumulator; per-patch
-    // kernel: reads and clears the accumulator, adds into out_x
+    // ordered per-unit kernel: clears out_x (unless zeroed) and out_lo, sums each
+    // patch over modules in module order; per-patch kernel: accumulator plus
+    // spill slots -> gradient in two words
     FusedLaunch a{cot, out_x, p->hmain, p->hnyq, p->tw, p->wt, scale, p->acc};
     a.zero_out = !out_zeroed;
     a.pdl = p->pdl;
-    int st;
+    a.out_lo = out_lo;
+    a.spill = p->spill;
+    a.loop_grid = p->adj_grid;
+    a.bnd_log2 = L;
+    a.bnd_scale = bscale;
     {
       Phase ph(p, 1, s);
-      st = fused_run(g, p->dtype, a, FUSED_ADJ_TO_SPEC, s);
+      a.bnd_out = p->bnd_a;
+      JUBIK_TRY(fused_run(g, p->dtype, a, FUSED_ADJ_TO_SPEC, s));
     }
-    if (!st) {
-      Phase ph(p, 5, s);
-      st = fused_run(g, p->dtype, a, FUSED_ADJ_FROM_SPEC, s);
-    }
-    if (st) cudaMemsetAsync(p->acc, 0, fused_spec_bytes(g, p->dtype), s);  // restore the zeros
-    return st;
+    Phase ph(p, 5, s);
+    a.bnd_out = nullptr;
+    a.bnd_in = p->bnd_a;
+    a.bnd_n = (int)p->adj_grid;
+    return fused_run(g, p->dtype, a, FUSED_ADJ_FROM_SPEC, s);
   }
   Phase ph(p, 1, s);
   const bool f32 = p->dtype == JUBIK_F32;
@@ -445,6 +524,13 @@ int do_adjoint(jubik_plan* p, const void* cot, void* out_x, double scale, cudaSt
                 : fft2_batched<double>(p->fft, p->fft, p->zs, plain_pairs(g), true, s));
   return f32 ? plain_grad_gather<float>(g, p->zs, p->wt, scale, out_x, s)
              : plain_grad_gather<double>(g, p->zs, p->wt, scale, out_x, s);
+}
+
+// hi += lo where the fused path left a two-word result
+int finish_words(jubik_plan* p, void* hi, const void* lo, int64_t n, cudaStream_t s) {
+  if (p->path != JUBIK_PATH_FUSED) return JUBIK_OK;
+  return p->dtype == JUBIK_F32 ? combine_words<float>(hi, lo, n, p->pdl, s)
+                               : combine_words<double>(hi, lo, n, p->pdl, s);
 }
 
 int need(bool ok, const char* what) {
@@ -577,6 +663,26 @@ int jubik_plan_create(const jubik_plan_desc* d, jubik_plan** out) {
     if (share && (st = cuda_status(cudaMemset(p->acc, 0, fused_spec_bytes(g, p->dtype)),
                                    "memset accumulator")))
       return fail(st);
+    const int64_t patches = (int64_t)g.E * g.n * g.n;
+    if (share) {
+      p->adj_grid = fused_adj_grid(g, p->dtype);
+      if (p->adj_grid <= 0) {
+        delete p;
+        set_error("no launch configuration for the ordered adjoint at P=%d", g.P);
+        return JUBIK_ERR_UNSUPPORTED;
+      }
+      if ((st = p->alloc(&p->spill, (size_t)p->adj_grid * g.P * (g.P / 2) * csz)))
+        return fail(st);
+    }
+    if ((st = p->alloc(&p->conv_lo, img * p->esz))) return fail(st);
+    if ((st = p->alloc(&p->conv_v_lo, img * p->esz))) return fail(st);
+    if ((st = p->alloc(&p->grad_lo, (size_t)g.E * g.pixels() * p->esz))) return fail(st);
+    if ((st = p->alloc(&p->bnd_f, sizeof(uint64_t) * std::max<int64_t>(patches,
+                                                                        kMaxBoundBlocks))))
+      return fail(st);
+    if ((st = p->alloc(&p->bnd_a, sizeof(uint64_t) * std::max<int64_t>(p->adj_grid,
+                                                                        kMaxBoundBlocks))))
+      return fail(st);
   } else {
     if ((st = p->alloc(&p->hfull, (size_t)units * g.P * (g.P / 2 + 1) * csz))) return fail(st);
     if ((st = p->alloc(&p->zs, (size_t)plain_pairs(g) * g.P * g.P * csz))) return fail(st);
@@ -588,7 +694,7 @@ int jubik_plan_create(const jubik_plan_desc* d, jubik_plan** out) {
   if ((st = p->alloc(&p->conv, img * p->esz))) return fail(st);
   if ((st = p->alloc(&p->conv_v, img * p->esz))) return fail(st);
   if ((st = p->alloc(&p->resid, img * p->esz))) return fail(st);
-  if ((st = p->alloc(&p->lam, img * p->esz))) return fail(st);
+  if ((st = p->alloc(&p->wts, img * p->esz))) return fail(st);
   if ((st = p->alloc(&p->xsky, (size_t)g.E * g.pixels() * p->esz))) return fail(st);
   if ((st = p->alloc(&p->xgrad, (size_t)g.E * g.pixels() * p->esz))) return fail(st);
   if ((st = p->alloc((void**)&p->ridx, img * sizeof(int32_t)))) return fail(st);
@@ -688,14 +794,26 @@ int jubik_plan_set_psf(jubik_plan* p, const void* psf, int32_t layout, int32_t e
   void* buf = nullptr;
   double* sums = nullptr;
   JUBIK_TRY_CUDA(cudaMallocAsync(&buf, per * chunk, s));
-  JUBIK_TRY_CUDA(cudaMallocAsync((void**)&sums, sizeof(double) * chunk, s));
+  JUBIK_TRY_CUDA(cudaMallocAsync((void**)&sums, 2 * sizeof(double) * chunk, s));
   int st = JUBIK_OK;
+  double kmax = 0.0;
+  std::vector<double> hs(2 * chunk);
   for (int64_t u0 = 0; u0 < units && st == JUBIK_OK; u0 += chunk) {
     const int64_t nu = std::min(chunk, units - u0);
     st = p->dtype == JUBIK_F32
              ? psf_to_cplx<float>(g, psf, layout, e_broadcast, u0, nu, sums, buf, s)
              : psf_to_cplx<double>(g, psf, layout, e_broadcast, u0, nu, sums, buf, s);
     if (st) break;
+    // sum |k| / |sum k| of each unit's window: the magnitude gain of its
+    // normalised kernel, which the output bounds of the two-word sums use
+    st = cuda_status(cudaMemcpyAsync(hs.data(), sums, 2 * sizeof(double) * nu,
+                                     cudaMemcpyDeviceToHost, s), "copy kernel sums");
+    if (!st) st = cuda_status(cudaStreamSynchronize(s), "copy kernel sums");
+    if (st) break;
+    for (int64_t i = 0; i < nu; ++i) {
+      const double r = std::fabs(hs[2 * i + 1] / hs[2 * i]);
+      kmax = (r > kmax || r != r) ? r : kmax;
+    }
     st = fft2_batched<double>(p->fft, p->fft, buf, nu, false, s);
     if (st) break;
     st = p->dtype == JUBIK_F32
@@ -705,6 +823,7 @@ int jubik_plan_set_psf(jubik_plan* p, const void* psf, int32_t layout, int32_t e
   cudaFreeAsync(buf, s);
   cudaFreeAsync(sums, s);
   JUBIK_TRY(st);
+  p->kmax = kmax;
   p->psf_set = true;
   p->lam_valid = false;
   return cuda_status(cudaGetLastError(), "set_psf");
@@ -805,14 +924,18 @@ int jubik_psf_forward(jubik_plan* p, const void* x, void* out, void* stream) {
   NvtxRange nvtx_("jubik_psf_forward");
   JUBIK_TRY(check_plan(p));
   JUBIK_TRY(need(p->psf_set, "PSF"));
-  return do_forward(p, x, out, 1.0, S(stream));
+  cudaStream_t s = S(stream);
+  JUBIK_TRY(do_forward(p, x, out, p->conv_lo, 1.0, s));
+  return finish_words(p, out, p->conv_lo, image_elems(p), s);
 }
 
 int jubik_psf_adjoint(jubik_plan* p, const void* cot, void* out_x, void* stream) {
   NvtxRange nvtx_("jubik_psf_adjoint");
   JUBIK_TRY(check_plan(p));
   JUBIK_TRY(need(p->psf_set, "PSF"));
-  return do_adjoint(p, cot, out_x, 1.0, S(stream));
+  cudaStream_t s = S(stream);
+  JUBIK_TRY(do_adjoint(p, cot, out_x, p->grad_lo, 1.0, s));
+  return finish_words(p, out_x, p->grad_lo, (int64_t)p->g.E * p->g.pixels(), s);
 }
 
 int jubik_response_forward(jubik_plan* p, const void* x, void* out_readout, void* stream) {
@@ -820,11 +943,14 @@ int jubik_response_forward(jubik_plan* p, const void* x, void* out_readout, void
   JUBIK_TRY(check_plan(p));
   JUBIK_TRY(need(p->psf_set, "PSF"));
   cudaStream_t s = S(stream);
-  JUBIK_TRY(do_forward(p, x, p->conv, p->desc.pixel_area, s));
+  JUBIK_TRY(do_forward(p, x, p->conv, p->conv_lo, p->desc.pixel_area, s));
+  const void* lo = p->path == JUBIK_PATH_FUSED ? p->conv_lo : nullptr;
   Phase ph(p, 2, s);
   return p->dtype == JUBIK_F32
-             ? readout_gather<float>(p->conv, p->eps, p->rlist, p->readout_total, out_readout, s)
-             : readout_gather<double>(p->conv, p->eps, p->rlist, p->readout_total, out_readout, s);
+             ? readout_gather<float>(p->conv, p->eps, p->rlist, p->readout_total, out_readout, s,
+                                     lo)
+             : readout_gather<double>(p->conv, p->eps, p->rlist, p->readout_total, out_readout,
+                                      s, lo);
 }
 
 int jubik_response_jvp(jubik_plan* p, const void* t, void* out_readout, void* stream) {
@@ -846,7 +972,8 @@ int jubik_response_vjp(jubik_plan* p, const void* cot_readout, void* out_x, void
                   : readout_scatter<double>(cot_readout, p->eps, p->rlist, p->readout_total,
                                             p->resid, s));
   }
-  return do_adjoint(p, p->resid, out_x, p->desc.pixel_area, s);
+  JUBIK_TRY(do_adjoint(p, p->resid, out_x, p->grad_lo, p->desc.pixel_area, s));
+  return finish_words(p, out_x, p->grad_lo, (int64_t)p->g.E * p->g.pixels(), s);
 }
 
 int jubik_poisson_energy_grad(jubik_plan* p, const void* x, double* energy, void* grad_x,
@@ -857,22 +984,25 @@ int jubik_poisson_energy_grad(jubik_plan* p, const void* x, double* energy, void
   JUBIK_TRY(need(p->data_set, "data"));
   cudaStream_t s = S(stream);
   bool grad_zeroed = false;
-  JUBIK_TRY(do_forward(p, x, p->conv, p->desc.pixel_area, s, grad_x,
+  JUBIK_TRY(do_forward(p, x, p->conv, p->conv_lo, p->desc.pixel_area, s, grad_x,
                        (int64_t)p->g.E * p->g.pixels() * (int64_t)p->esz, &grad_zeroed));
   const int64_t img = image_elems(p);
+  const void* lo = p->path == JUBIK_PATH_FUSED ? p->conv_lo : nullptr;
   {
   Phase ph(p, 2, s);
   JUBIK_TRY(p->dtype == JUBIK_F32
-                ? poisson_image<float>(p->conv, p->eps, p->dimg, img, p->lam,
+                ? poisson_image<float>(p->conv, lo, p->eps, p->dimg, img, p->wts,
                                        grad_x ? p->resid : nullptr, p->partials, p->counter,
                                        energy, p->pdl, s)
-                : poisson_image<double>(p->conv, p->eps, p->dimg, img, p->lam,
+                : poisson_image<double>(p->conv, lo, p->eps, p->dimg, img, p->wts,
                                         grad_x ? p->resid : nullptr, p->partials, p->counter,
                                         energy, p->pdl, s));
   }
   p->lam_valid = true;
   if (!grad_x) return JUBIK_OK;
-  return do_adjoint(p, p->resid, grad_x, p->desc.pixel_area, s, grad_zeroed);
+  JUBIK_TRY(do_adjoint(p, p->resid, grad_x, p->grad_lo, p->desc.pixel_area, s, grad_zeroed));
+  Phase ph(p, 6, s);
+  return finish_words(p, grad_x, p->grad_lo, (int64_t)p->g.E * p->g.pixels(), s);
 }
 
 int jubik_poisson_energy_grad_logsky(jubik_plan* p, const void* s_log, int32_t e_pad,
@@ -894,32 +1024,36 @@ int jubik_poisson_energy_grad_logsky(jubik_plan* p, const void* s_log, int32_t e
   view.ps = (int64_t)nx_pad * ny_pad;
   view.exp = true;
   bool grad_zeroed = false;
-  JUBIK_TRY(do_forward(p, s_log, p->conv, p->desc.pixel_area, s, grad_s ? p->xgrad : nullptr,
-                       (int64_t)g.E * g.pixels() * (int64_t)p->esz, &grad_zeroed, view));
+  JUBIK_TRY(do_forward(p, s_log, p->conv, p->conv_lo, p->desc.pixel_area, s,
+                       grad_s ? p->xgrad : nullptr, (int64_t)g.E * g.pixels() * (int64_t)p->esz,
+                       &grad_zeroed, view));
   const int64_t img = image_elems(p);
+  const void* lo = p->path == JUBIK_PATH_FUSED ? p->conv_lo : nullptr;
   {
     Phase ph(p, 2, s);
     JUBIK_TRY(p->dtype == JUBIK_F32
-                  ? poisson_image<float>(p->conv, p->eps, p->dimg, img, p->lam,
+                  ? poisson_image<float>(p->conv, lo, p->eps, p->dimg, img, p->wts,
                                          grad_s ? p->resid : nullptr, p->partials, p->counter,
                                          energy, p->pdl, s)
-                  : poisson_image<double>(p->conv, p->eps, p->dimg, img, p->lam,
+                  : poisson_image<double>(p->conv, lo, p->eps, p->dimg, img, p->wts,
                                           grad_s ? p->resid : nullptr, p->partials,
                                           p->counter, energy, p->pdl, s));
   }
   p->lam_valid = true;
   if (!grad_s) return JUBIK_OK;
-  JUBIK_TRY(do_adjoint(p, p->resid, p->xgrad, p->desc.pixel_area, s, grad_zeroed));
+  JUBIK_TRY(do_adjoint(p, p->resid, p->xgrad, p->grad_lo, p->desc.pixel_area, s, grad_zeroed));
+  const void* glo = p->path == JUBIK_PATH_FUSED ? p->grad_lo : nullptr;
   const int64_t n = (int64_t)e_pad * nx_pad * ny_pad;
   if (p->dtype == JUBIK_F32)
     k_logsky_grad<float><<<blocks_for(n), 256, 0, s>>>((const float*)s_log,
-                                                        (const float*)p->xgrad, g.E, g.nx, g.ny,
-                                                        e_pad, nx_pad, ny_pad, (float*)grad_s);
+                                                        (const float*)p->xgrad, (const float*)glo,
+                                                        g.E, g.nx, g.ny, e_pad, nx_pad, ny_pad,
+                                                        (float*)grad_s);
   else
     k_logsky_grad<double><<<blocks_for(n), 256, 0, s>>>((const double*)s_log,
-                                                         (const double*)p->xgrad, g.E, g.nx,
-                                                         g.ny, e_pad, nx_pad, ny_pad,
-                                                         (double*)grad_s);
+                                                         (const double*)p->xgrad,
+                                                         (const double*)glo, g.E, g.nx, g.ny,
+                                                         e_pad, nx_pad, ny_pad, (double*)grad_s);
   return cuda_status(cudaGetLastError(), "k_logsky_grad");
 }
 
@@ -929,31 +1063,32 @@ int jubik_metric_apply(jubik_plan* p, const void* x, const void* v, void* out, v
   JUBIK_TRY(need(p->psf_set, "PSF"));
   cudaStream_t s = S(stream);
   const int64_t img = image_elems(p);
-  if (x) {
-    JUBIK_TRY(do_forward(p, x, p->conv, p->desc.pixel_area, s));
-    // lam = eps * conv (read-out pixels are the only ones the weights use)
-    if (p->eps) {
-      JUBIK_TRY(p->dtype == JUBIK_F32
-                    ? elementwise_op<float>(3, p->conv, p->eps, nullptr, img, p->lam, s)
-                    : elementwise_op<double>(3, p->conv, p->eps, nullptr, img, p->lam, s));
-    } else {
-      JUBIK_TRY_CUDA(
-          cudaMemcpyAsync(p->lam, p->conv, img * p->esz, cudaMemcpyDeviceToDevice, s));
-    }
+  const bool two = p->path == JUBIK_PATH_FUSED;
+  if (x) {  // weights eps^2 / lam of a new lam = R(x), as the likelihood pass leaves them
+    JUBIK_TRY(do_forward(p, x, p->conv, p->conv_lo, p->desc.pixel_area, s));
+    JUBIK_TRY(p->dtype == JUBIK_F32
+                  ? metric_weights<float>(p->conv, two ? p->conv_lo : nullptr, p->eps, p->ridx,
+                                          img, p->wts, s)
+                  : metric_weights<double>(p->conv, two ? p->conv_lo : nullptr, p->eps, p->ridx,
+                                           img, p->wts, s));
     p->lam_valid = true;
   }
   JUBIK_TRY(need(p->lam_valid, "lambda (call with x or after poisson_energy_grad)"));
+  // R v, weighted in the pass that adds its two words, then the adjoint
   bool out_zeroed = false;
-  JUBIK_TRY(do_forward(p, v, p->conv_v, p->desc.pixel_area, s, out,
+  JUBIK_TRY(do_forward(p, v, p->conv_v, p->conv_v_lo, p->desc.pixel_area, s, out,
                        (int64_t)p->g.E * p->g.pixels() * (int64_t)p->esz, &out_zeroed));
   {
     Phase ph(p, 2, s);
     JUBIK_TRY(p->dtype == JUBIK_F32
-                  ? metric_weights<float>(p->conv_v, p->eps, p->ridx, p->lam, img, p->resid, s)
-                  : metric_weights<double>(p->conv_v, p->eps, p->ridx, p->lam, img, p->resid,
-                                           s));
+                  ? apply_weights<float>(p->conv_v, two ? p->conv_v_lo : nullptr, p->wts, img,
+                                         p->resid, p->pdl, s)
+                  : apply_weights<double>(p->conv_v, two ? p->conv_v_lo : nullptr, p->wts, img,
+                                          p->resid, p->pdl, s));
   }
-  return do_adjoint(p, p->resid, out, p->desc.pixel_area, s, out_zeroed);
+  JUBIK_TRY(do_adjoint(p, p->resid, out, p->grad_lo, p->desc.pixel_area, s, out_zeroed));
+  Phase ph(p, 6, s);
+  return finish_words(p, out, p->grad_lo, (int64_t)p->g.E * p->g.pixels(), s);
 }
 
 int jubik_poisson_energy(const void* lam, const int32_t* data, int64_t n, int32_t dtype,
@@ -1228,15 +1363,19 @@ int jubik_group_set_io(jubik_group* g, const void* const* x, void* const* grad,
   for (int i = 0; i < n; ++i) {
     jubik_plan* p = g->plans[i];
     const int64_t img = image_elems(p);
-    pj.push_back(PoissonJob{p->conv, p->eps, p->dimg, img, p->lam, p->resid, p->partials,
+    pj.push_back(PoissonJob{p->conv, p->eps, p->dimg, img, p->wts, p->resid, p->partials,
                             p->counter, energies + i});
     ps.push_back((int)pb);
     pb += poisson_group_blocks(img);
-    // each problem's overlap-add image and gradient start from zero
-    const int64_t bytes[2] = {img * (int64_t)p->esz, (int64_t)p->g.E * p->g.pixels() *
-                                                         (int64_t)p->esz};
-    void* ptrs[2] = {p->conv, grad[i]};
-    for (int t = 0; t < 2; ++t) {
+    // each problem's overlap-add image and gradient start from zero, and so does
+    // the module-shared accumulator that the grouped adjoint adds into (a
+    // one-problem call leaves its last sums there)
+    const int64_t bytes[3] = {img * (int64_t)p->esz,
+                              (int64_t)p->g.E * p->g.pixels() * (int64_t)p->esz,
+                              p->acc ? (int64_t)fused_spec_bytes(p->g, p->dtype) : 0};
+    void* ptrs[3] = {p->conv, grad[i], p->acc};
+    for (int t = 0; t < 3; ++t) {
+      if (!ptrs[t]) continue;
       zj.push_back(ZeroJob{ptrs[t], bytes[t]});
       zs.push_back((int)zb);
       zb += std::max<int64_t>(1, std::min<int64_t>(1024, bytes[t] / (256 * 16 * 8)));

@@ -35,6 +35,7 @@
 #include <atomic>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "fft_codelets.cuh"
@@ -73,6 +74,19 @@ struct Args {
   int64_t in_rs, in_ps;  // forward input: row and plane strides (a crop of a larger array)
   int in_exp;            // forward input holds log-sky values: the sky is their exp
   int M, E, nx, ny, n, dx, margin, half, sr_max, sc_max;
+  // exact two-word accumulation of the output (see Split2): the low words, and
+  // the bound on its terms = bnd_scale * max(bnd_in[0 .. bnd_n)), at most
+  // 2^bnd_log2 terms per element.  out_lo == nullptr: single-word reductions.
+  void* out_lo;
+  const unsigned long long* bnd_in;
+  int bnd_n, bnd_log2;
+  double bnd_scale;
+  // input magnitude maxima this kernel records (per item or per CTA), or nullptr
+  unsigned long long* bnd_out;
+  // module-shared adjoint in unit order (one problem): partial module sums of
+  // the patch a CTA continues (one slot per CTA of the loop grid `loop_grid`)
+  void* spill;
+  int loop_grid;
 };
 
 __device__ __forceinline__ float2 ldg2(const float2* p) { return __ldg(p); }
@@ -203,6 +217,14 @@ __device__ __forceinline__ unsigned long long mag_bits(double v) {
 __device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) {
   return a > b ? a : b;
 }
+__device__ __forceinline__ unsigned umax32(unsigned a, unsigned b) { return a > b ? a : b; }
+// U.mx of either width as the bits of a double magnitude
+__device__ __forceinline__ unsigned long long mag_as_double_bits(unsigned v) {
+  return mag_bits((double)__uint_as_float(v));
+}
+__device__ __forceinline__ unsigned long long mag_as_double_bits(unsigned long long v) {
+  return v;
+}
 // CTA-wide maximum of one value per thread (every thread gets it); uses s_slot.
 __device__ __forceinline__ unsigned long long cta_max(unsigned long long v,
                                                       unsigned long long* s_slot) {
@@ -324,12 +346,21 @@ struct Unit {
   const T* wt;
   const cx<T>* twg;
   cx<T> wq[16];
+  // largest input magnitude staged so far (bits of |v|; a NaN sorts last)
+  typename std::conditional<sizeof(T) == 4, unsigned, unsigned long long>::type mx;
+  // module-shared adjoint in unit order: partial sums of this patch held by
+  // the CTAs that continued it (nsp slots from sp0)
+  const cx<T>* sp0;
+  int nsp;
 
   // unit block index ub (the CTA's blockIdx.x unless a grouped launch maps it)
   // -> (m, e, k); per_module == false decodes (e, k) only
   __device__ __forceinline__ void init(const Args& a, unsigned char* smem, bool per_module,
                                        int ub = -1) {
     geom(a, smem, per_module, ub);
+    mx = 0;
+    sp0 = nullptr;
+    nsp = 0;
     twg = (const cx<T>*)a.tw;
 #pragma unroll
     for (int q = 0; q < 16; ++q) wq[q] = ldg2(twg + cls * q);
@@ -476,7 +507,8 @@ __device__ __forceinline__ void input_issue(const Unit<T, P>& U, const Args& a,
 // the current chunk's transform.  Buffers are pair rows of pitch TP: chunk c
 // uses the staging area (c even) or a tile region (c odd).  chunk0_issued:
 // input_issue(c = 0) already ran for this unit (and nothing was committed since).
-template <typename T, int P, bool ADJ>
+// TRACK: also record the largest magnitude of the staged (weighted) values in U.mx.
+template <typename T, int P, bool ADJ, bool TRACK = false>
 __device__ __forceinline__ void stage_input(Unit<T, P>& U, const Args& a,
                                             bool chunk0_issued = false) {
   using R = Tr<T, P>;
@@ -536,6 +568,15 @@ __device__ __forceinline__ void stage_input(Unit<T, P>& U, const Args& a,
           v[q] = ADJ ? t : mkc<T>((wr0 * wc[q]) * t.x, (wr1 * wc[q]) * t.y);
         } else {
           v[q] = mkc<T>((T)0, (T)0);
+        }
+        if constexpr (TRACK) {
+          if constexpr (sizeof(T) == 4) {
+            const unsigned b = umax32(__float_as_uint(fabsf(v[q].x)),
+                                      __float_as_uint(fabsf(v[q].y)));
+            U.mx = b > U.mx ? b : U.mx;
+          } else {
+            U.mx = umax64(U.mx, umax64(mag_bits(v[q].x), mag_bits(v[q].y)));
+          }
         }
       }
       Dft<16, false, T>::run(v);
@@ -646,6 +687,14 @@ __device__ __forceinline__ void stage_mid(Unit<T, P>& U) {
     if (MODE == MID_FROM_SPEC || MODE == MID_FROM_ACC) {
 #pragma unroll
       for (int q = 0; q < 16; ++q) v[q] = U.spec[(16 * cls + q) * H + c];
+      if (MODE == MID_FROM_ACC) {
+        // partial sums of the CTAs that continued this patch, in CTA order
+        for (int j = 0; j < U.nsp; ++j) {
+          const cx<T>* sq = U.sp0 + (int64_t)j * (P * H);
+#pragma unroll
+          for (int q = 0; q < 16; ++q) v[q] = cadd<T>(v[q], sq[(16 * cls + q) * H + c]);
+        }
+      }
     } else {
 #pragma unroll
       for (int q = 0; q < 16; ++q) {
@@ -810,17 +859,49 @@ __device__ __forceinline__ void stage_combine(Unit<T, P>& U, int jc_lo, int jc_h
   }
 }
 
+// Accumulate into an output element (group): one reduction per word.  TWO:
+// the exact two-word form (Split2), hi into the output, lo into its low plane.
+template <bool TWO>
+__device__ __forceinline__ void acc4(float* hi, float* lo, const Split2<float>& sp, float a,
+                                     float b, float c, float d) {
+  if constexpr (TWO) {
+    float h0, h1, h2, h3, l0, l1, l2, l3;
+    sp.split(a, h0, l0);
+    sp.split(b, h1, l1);
+    sp.split(c, h2, l2);
+    sp.split(d, h3, l3);
+    red_add_v4(hi, h0, h1, h2, h3);
+    red_add_v4(lo, l0, l1, l2, l3);
+  } else {
+    red_add_v4(hi, a, b, c, d);
+  }
+}
+template <bool TWO, typename T>
+__device__ __forceinline__ void acc1(T* hi, T* lo, const Split2<T>& sp, T v) {
+  if constexpr (TWO) {
+    T h, l;
+    sp.split(v, h, l);
+    atomicAdd(hi, h);
+    atomicAdd(lo, l);
+  } else {
+    atomicAdd(hi, v);
+  }
+}
+
 // ---- inverse variant-A phase 2 -> natural-order staging -> global
 // forward: overlap-add of the whole P x P patch into out[m][e];
 // adjoint: crop to the window, bilinear weights, scatter into out[e].
-template <typename T, int P, bool ADJ>
-__device__ __forceinline__ void stage_output(Unit<T, P>& U, const Args& a) {
+// TWO: exact two-word accumulation into out / out_lo with the splitter sp.
+template <typename T, int P, bool ADJ, bool TWO = false>
+__device__ __forceinline__ void stage_output(Unit<T, P>& U, const Args& a,
+                                             const Split2<T>& sp = Split2<T>{}) {
   using R = Tr<T, P>;
   constexpr int L1 = R::L1, H = R::H, NT = R::NT, TP = R::TP, CH = R::CH;
   const int mg = U.mg, K = U.K, cb = U.cb, rb = U.rb;
   const T scale = (T)a.scale;
   const bool vec4 = ((cb + (ADJ ? mg : 0)) % 4 == 0) && (a.ny % 4 == 0) &&
-                    (((uintptr_t)a.out) % 16 == 0) && (ADJ ? K % 4 == 0 : true);
+                    (((uintptr_t)a.out) % 16 == 0) && (!TWO || ((uintptr_t)a.out_lo) % 16 == 0) &&
+                    (ADJ ? K % 4 == 0 : true);
   const int jo_lo = ADJ ? mg / 2 : 0;
   const int jo_hi = ADJ ? (mg + K + 1) / 2 : H;
   const T* wt = U.wt;
@@ -839,8 +920,10 @@ __device__ __forceinline__ void stage_output(Unit<T, P>& U, const Args& a) {
       for (int q = 0; q < 16; ++q) stg[jj * TP + U.cls + L1 * q] = v[q];
     }
     __syncthreads();
+    const int64_t plane = ADJ ? (int64_t)U.e * U.npix : ((int64_t)U.m * a.E + U.e) * U.npix;
+    T* __restrict__ dst = (T*)a.out + plane;
+    T* __restrict__ dlo = TWO ? (T*)a.out_lo + plane : nullptr;
     if (!ADJ) {
-      T* __restrict__ dst = (T*)a.out + ((int64_t)U.m * a.E + U.e) * U.npix;
       if (sizeof(T) == 4 && vec4) {
         // groups of 4 columns never straddle the field edge (cb, ny multiples of 4).
         // A warp takes 8 pair rows x 4 groups: with the pitch P + 1 = 1 (mod 16)
@@ -850,17 +933,19 @@ __device__ __forceinline__ void stage_output(Unit<T, P>& U, const Args& a) {
         const int ntile = ((nch + 7) / 8) * GT;
         if (rb >= 0 && rb + P <= a.nx && cb >= 0 && cb + P <= a.ny) {
           // the whole P x P patch lies inside the field: no bounds checks
-          T* base = dst + (int64_t)(rb + 2 * j0) * a.ny + cb;
+          const int64_t o0 = (int64_t)(rb + 2 * j0) * a.ny + cb;
           for (int w = U.warp; w < ntile; w += R::NW) {
             const int jj = 8 * (w / GT) + (U.lane >> 2);
             const int x = 16 * (w % GT) + 4 * (U.lane & 3);
             if (jj >= nch) continue;
-            const cx<T>* sp = stg + jj * TP + x;
-            const cx<T> z0 = sp[0], z1 = sp[1], z2 = sp[2], z3 = sp[3];
-            T* p = base + (int64_t)(2 * jj) * a.ny + x;
-            red_add_v4((float*)p, scale * z0.x, scale * z1.x, scale * z2.x, scale * z3.x);
-            red_add_v4((float*)(p + a.ny), scale * z0.y, scale * z1.y, scale * z2.y,
-                       scale * z3.y);
+            const cx<T>* sq = stg + jj * TP + x;
+            const cx<T> z0 = sq[0], z1 = sq[1], z2 = sq[2], z3 = sq[3];
+            const int64_t o = o0 + (int64_t)(2 * jj) * a.ny + x;
+            acc4<TWO>((float*)(dst + o), (float*)(dlo + o), (const Split2<float>&)sp,
+                      scale * z0.x, scale * z1.x, scale * z2.x, scale * z3.x);
+            acc4<TWO>((float*)(dst + o + a.ny), (float*)(dlo + o + a.ny),
+                      (const Split2<float>&)sp, scale * z0.y, scale * z1.y, scale * z2.y,
+                      scale * z3.y);
           }
         } else
         for (int w = U.warp; w < ntile; w += R::NW) {
@@ -872,12 +957,16 @@ __device__ __forceinline__ void stage_output(Unit<T, P>& U, const Args& a) {
           const cx<T> z0 = stg[jj * TP + x], z1 = stg[jj * TP + x + 1];
           const cx<T> z2 = stg[jj * TP + x + 2], z3 = stg[jj * TP + x + 3];
           const int row = rb + 2 * (j0 + jj);
-          if (row >= 0 && row < a.nx)
-            red_add_v4((float*)(dst + (int64_t)row * a.ny + col), scale * z0.x, scale * z1.x,
-                       scale * z2.x, scale * z3.x);
-          if (row + 1 >= 0 && row + 1 < a.nx)
-            red_add_v4((float*)(dst + (int64_t)(row + 1) * a.ny + col), scale * z0.y,
-                       scale * z1.y, scale * z2.y, scale * z3.y);
+          if (row >= 0 && row < a.nx) {
+            const int64_t o = (int64_t)row * a.ny + col;
+            acc4<TWO>((float*)(dst + o), (float*)(dlo + o), (const Split2<float>&)sp,
+                      scale * z0.x, scale * z1.x, scale * z2.x, scale * z3.x);
+          }
+          if (row + 1 >= 0 && row + 1 < a.nx) {
+            const int64_t o = (int64_t)(row + 1) * a.ny + col;
+            acc4<TWO>((float*)(dst + o), (float*)(dlo + o), (const Split2<float>&)sp,
+                      scale * z0.y, scale * z1.y, scale * z2.y, scale * z3.y);
+          }
         }
       } else {
         for (int i = U.tid; i < nch * P; i += NT) {
@@ -886,13 +975,17 @@ __device__ __forceinline__ void stage_output(Unit<T, P>& U, const Args& a) {
           if (col < 0 || col >= a.ny) continue;
           const cx<T> z = stg[jj * TP + x];
           const int row = rb + 2 * (j0 + jj);
-          if (row >= 0 && row < a.nx) atomicAdd(dst + (int64_t)row * a.ny + col, scale * z.x);
-          if (row + 1 >= 0 && row + 1 < a.nx)
-            atomicAdd(dst + (int64_t)(row + 1) * a.ny + col, scale * z.y);
+          if (row >= 0 && row < a.nx) {
+            const int64_t o = (int64_t)row * a.ny + col;
+            acc1<TWO, T>(dst + o, dlo + o, sp, scale * z.x);
+          }
+          if (row + 1 >= 0 && row + 1 < a.nx) {
+            const int64_t o = (int64_t)(row + 1) * a.ny + col;
+            acc1<TWO, T>(dst + o, dlo + o, sp, scale * z.y);
+          }
         }
       }
     } else {
-      T* __restrict__ dst = (T*)a.out + (int64_t)U.e * U.npix;
       if (sizeof(T) == 4 && vec4) {
         // warp tiles of 8 pair rows x 4 column groups, as in the forward branch
         const int G = K / 4, GT = (G + 3) / 4;
@@ -915,13 +1008,17 @@ __device__ __forceinline__ void stage_output(Unit<T, P>& U, const Args& a) {
           }
           if (ya >= 0 && ya < K && row >= 0 && row < a.nx) {
             const T wy = wt[ya];
-            red_add_v4((float*)(dst + (int64_t)row * a.ny + col), (wy * w4[0]) * z[0].x,
-                       (wy * w4[1]) * z[1].x, (wy * w4[2]) * z[2].x, (wy * w4[3]) * z[3].x);
+            const int64_t o = (int64_t)row * a.ny + col;
+            acc4<TWO>((float*)(dst + o), (float*)(dlo + o), (const Split2<float>&)sp,
+                      (wy * w4[0]) * z[0].x, (wy * w4[1]) * z[1].x, (wy * w4[2]) * z[2].x,
+                      (wy * w4[3]) * z[3].x);
           }
           if (ya + 1 >= 0 && ya + 1 < K && row + 1 >= 0 && row + 1 < a.nx) {
             const T wy = wt[ya + 1];
-            red_add_v4((float*)(dst + (int64_t)(row + 1) * a.ny + col), (wy * w4[0]) * z[0].y,
-                       (wy * w4[1]) * z[1].y, (wy * w4[2]) * z[2].y, (wy * w4[3]) * z[3].y);
+            const int64_t o = (int64_t)(row + 1) * a.ny + col;
+            acc4<TWO>((float*)(dst + o), (float*)(dlo + o), (const Split2<float>&)sp,
+                      (wy * w4[0]) * z[0].y, (wy * w4[1]) * z[1].y, (wy * w4[2]) * z[2].y,
+                      (wy * w4[3]) * z[3].y);
           }
         }
       } else {
@@ -933,13 +1030,157 @@ __device__ __forceinline__ void stage_output(Unit<T, P>& U, const Args& a) {
           const T wx = wt[xa] * scale;
           const int y0 = 2 * (j0 + jj);
           const int ya = y0 - mg, row = rb + y0;
-          if (ya >= 0 && ya < K && row >= 0 && row < a.nx)
-            atomicAdd(dst + (int64_t)row * a.ny + col, (wt[ya] * wx) * z.x);
-          if (ya + 1 >= 0 && ya + 1 < K && row + 1 >= 0 && row + 1 < a.nx)
-            atomicAdd(dst + (int64_t)(row + 1) * a.ny + col, (wt[ya + 1] * wx) * z.y);
+          if (ya >= 0 && ya < K && row >= 0 && row < a.nx) {
+            const int64_t o = (int64_t)row * a.ny + col;
+            acc1<TWO, T>(dst + o, dlo + o, sp, (wt[ya] * wx) * z.x);
+          }
+          if (ya + 1 >= 0 && ya + 1 < K && row + 1 >= 0 && row + 1 < a.nx) {
+            const int64_t o = (int64_t)(row + 1) * a.ny + col;
+            acc1<TWO, T>(dst + o, dlo + o, sp, (wt[ya + 1] * wx) * z.y);
+          }
         }
       }
     }
+  }
+}
+
+// ---- ordered module sum of the module-shared adjoint (one problem)
+// Thread (warp w, lane) holds, for its NCI column iterations, 16 complex
+// values of the patch's running sum in TMEM lane 32 (w % 4) + lane, columns
+// (w / 4) * PER_WARP + i * WC ... + WC.
+template <typename T, int P>
+struct TmemGeom {
+  static constexpr int H = P / 2, NW = P / 16;
+  static constexpr int NCI = (H + 31) / 32;                   // column iterations per thread
+  static constexpr int WC = 16 * (int)sizeof(cx<T>) / 4;      // 32-bit columns per iteration
+  static constexpr int PER_WARP = NCI * WC;
+  static constexpr int NEED = ((NW + 3) / 4) * PER_WARP;
+  static constexpr int NCOLS = NEED <= 32 ? 32 : NEED <= 64 ? 64 : NEED <= 128 ? 128
+                               : NEED <= 256 ? 256 : 512;
+  static_assert(NEED <= 512, "the running sum must fit the 512 TMEM columns of an SM");
+};
+
+// v[q] += the 16 complex values at TMEM address ta (this thread's lane)
+template <typename T>
+__device__ __forceinline__ void tmem_add16(uint32_t ta, cx<T> (&v)[16]) {
+  if constexpr (sizeof(T) == 4) {
+    uint32_t r[32];
+    tmem_ld32(ta, r);
+#pragma unroll
+    for (int q = 0; q < 16; ++q)
+      v[q] = mkc<T>(v[q].x + __uint_as_float(r[2 * q]), v[q].y + __uint_as_float(r[2 * q + 1]));
+  } else {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      uint32_t r[32];
+      tmem_ld32(ta + 32 * h, r);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int q = 8 * h + j;
+        v[q] = mkc<T>(v[q].x + __hiloint2double((int)r[4 * j + 1], (int)r[4 * j]),
+                      v[q].y + __hiloint2double((int)r[4 * j + 3], (int)r[4 * j + 2]));
+      }
+    }
+  }
+}
+template <typename T>
+__device__ __forceinline__ void tmem_put16(uint32_t ta, const cx<T> (&v)[16]) {
+  if constexpr (sizeof(T) == 4) {
+    uint32_t r[32];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      r[2 * q] = __float_as_uint(v[q].x);
+      r[2 * q + 1] = __float_as_uint(v[q].y);
+    }
+    tmem_st32(ta, r);
+  } else {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      uint32_t r[32];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int q = 8 * h + j;
+        r[4 * j] = (uint32_t)__double2loint(v[q].x);
+        r[4 * j + 1] = (uint32_t)__double2hiint(v[q].x);
+        r[4 * j + 2] = (uint32_t)__double2loint(v[q].y);
+        r[4 * j + 3] = (uint32_t)__double2hiint(v[q].y);
+      }
+      tmem_st32(ta + 32 * h, r);
+    }
+  }
+}
+
+// The cotangent spectrum of this unit times conj(PSF spectrum), added to the
+// patch's running sum over modules in TMEM.  The first unit of a patch in the
+// CTA's range starts the sum; the last writes it to `dest` (the patch's
+// accumulator, or this CTA's spill slot when an earlier CTA holds module 0).
+// Column 0 (the packed kx = 0 / P/2 columns) takes the scatter form, whose two
+// terms land on rows of different warps: they meet in shared memory (c0own,
+// c0mir) and column 0's sum stays there (c0acc).  Sums run in module order:
+// the result does not depend on timing.
+template <typename T, int P>
+__device__ __forceinline__ void stage_acc_tmem(Unit<T, P>& U, uint32_t tbase, bool first,
+                                               bool last, cx<T>* dest, cx<T>* c0own,
+                                               cx<T>* c0mir, cx<T>* c0acc) {
+  using TG = TmemGeom<T, P>;
+  constexpr int L1 = Tr<T, P>::L1, H = TG::H, NT = Tr<T, P>::NT;
+  const int cls = U.cls;
+  const uint32_t trow = tbase + ((uint32_t)(32 * (U.warp & 3)) << 16) +
+                        (uint32_t)((U.warp >> 2) * TG::PER_WARP);
+#pragma unroll 1
+  for (int i = 0; i < TG::NCI; ++i) {
+    const int c = U.lane + 32 * i;
+    const bool act = c < H;
+    cx<T> v[16];
+    if (act) {
+      cx<T> hv[16];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) hv[q] = ldg2(U.hmain + (16 * cls + q) * H + c);
+      const cx<T>* tb = U.tile + rf<P>(16 * cls, c);
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        const cx<T> t = tb[rfd<P>(q)];
+        v[q] = q ? cmul<T>(t, U.wq[q]) : t;
+      }
+      Dft<16, false, T>::run(v);
+      if (c == 0) {
+        // W(ky) adds conj(alpha(ky)) W(ky) to ky and conj(beta(-ky)) conj(W(ky)) to -ky
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          const int ky = cls + L1 * q, km = (P - ky) % P;
+          const int sm = 16 * (km % L1) + km / L1;
+          c0own[16 * cls + q] = cmulc<T>(v[q], hv[q]);
+          c0mir[sm] = cconj<T>(cmul<T>(v[q], ldg2(U.hnyq + sm)));
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) v[q] = cmulc<T>(v[q], hv[q]);
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < 16; ++q) v[q] = mkc<T>((T)0, (T)0);
+    }
+    // the running sum: warp-collective TMEM access, every lane takes part
+    const uint32_t ta = trow + (uint32_t)(i * TG::WC);
+    if (!first) tmem_add16<T>(ta, v);
+    if (last) {
+      if (act && c != 0) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) dest[(16 * cls + q) * H + c] = v[q];
+      }
+    } else {
+      tmem_put16<T>(ta, v);
+    }
+  }
+  if (!last) tmem_wait_st();
+  __syncthreads();  // column 0 terms of every warp are in shared memory
+  for (int sr = threadIdx.x; sr < P; sr += NT) {
+    cx<T> t = cadd<T>(c0own[sr], c0mir[sr]);
+    if (!first) t = cadd<T>(c0acc[sr], t);
+    if (last)
+      dest[sr * H] = t;
+    else
+      c0acc[sr] = t;
   }
 }
 
@@ -996,14 +1237,29 @@ struct ProblemList {
 };
 
 // ================================================================= kernels
-// One CTA per unit: the whole forward or adjoint of one patch.
-template <typename T, int P, bool ADJ>
-__device__ __forceinline__ void fused_unit_body(const Args& a, int ub, unsigned char* smem_raw) {
+// The output bound of a kernel that accumulates in two words: bnd_scale times
+// the largest stored input magnitude (read after the dependency wait).
+template <typename T>
+__device__ __forceinline__ Split2<T> output_splitter(const Args& a, unsigned long long* s_slot) {
+  Split2<T> sp;
+  const double m = reduce_bound(a.bnd_in, a.bnd_n, s_slot);
+  sp.init(a.bnd_scale * m, a.bnd_log2);
+  return sp;
+}
+
+// One CTA per unit: the whole forward or adjoint of one patch.  TWO: the
+// output accumulates in two words (one problem; its input bound was recorded
+// by a pass before this kernel).
+template <typename T, int P, bool ADJ, bool TWO>
+__device__ __forceinline__ void fused_unit_body(const Args& a, int ub, unsigned char* smem_raw,
+                                                unsigned long long* s_slot) {
   using R = Tr<T, P>;
   Unit<T, P> U;
   U.init(a, smem_raw, true, ub);
   prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
   pdl_wait();
+  Split2<T> sp{};
+  if constexpr (TWO) sp = output_splitter<T>(a, s_slot);
   stage_input<T, P, ADJ>(U, a);
   stage_split<T, P>(U);
   __syncthreads();
@@ -1015,14 +1271,15 @@ __device__ __forceinline__ void fused_unit_body(const Args& a, int ub, unsigned 
   __syncthreads();
   stage_combine<T, P>(U, ADJ ? U.mg / 2 : 0, ADJ ? (U.mg + U.K + 1) / 2 : R::H);
   __syncthreads();
-  stage_output<T, P, ADJ>(U, a);
+  stage_output<T, P, ADJ, TWO>(U, a, sp);
 }
 
 template <typename T, int P, bool ADJ>
 __global__ void __launch_bounds__(Tr<T, P>::NT) k_fused(Args a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ unsigned long long s_slot;
   pdl_trigger();
-  fused_unit_body<T, P, ADJ>(a, (int)blockIdx.x, smem_raw);
+  fused_unit_body<T, P, ADJ, true>(a, (int)blockIdx.x, smem_raw, &s_slot);
 }
 
 // Grouped launch over independent problems of one FFT side: problem p owns
@@ -1047,23 +1304,32 @@ __global__ void __launch_bounds__(Tr<T, P>::NT)
   __syncthreads();
   const int p = s_prob;
   const Args a = list[p];
-  fused_unit_body<T, P, ADJ>(a, (int)blockIdx.x - starts[p], smem_raw);
+  fused_unit_body<T, P, ADJ, false>(a, (int)blockIdx.x - starts[p], smem_raw, nullptr);
 }
 
 // Forward, module-shared: the sky spectrum of each (energy, patch) once; the
-// CTAs also clear the (M,E,nx,ny) output that the next kernel adds into ...
+// CTAs also clear the (M,E,nx,ny) output that the next kernel adds into, and
+// (one problem) record the largest weighted sky magnitude of their window ...
 template <typename T, int P, typename Src>
 __global__ void __launch_bounds__(Tr<T, P>::NT) k_sky_spec(Src src) {
+  constexpr bool ORD = std::is_same<Src, OneProblem>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ unsigned long long s_slot;
   Unit<T, P> U;
   pdl_trigger();
   int item;
   const Args& a = src.at((int)blockIdx.x, item);
   U.init(a, smem_raw, false, item);
   pdl_wait();
-  zero_slice(a.out, (int64_t)a.M * a.E * a.nx * a.ny * (int64_t)sizeof(T), a.zchunk);
+  const int64_t obytes = (int64_t)a.M * a.E * a.nx * a.ny * (int64_t)sizeof(T);
+  zero_slice(a.out, obytes, a.zchunk);
+  if (ORD && a.out_lo) zero_slice(a.out_lo, obytes, a.zchunk);
   if (a.aux) zero_slice(a.aux, a.aux_bytes, a.aux_chunk);
-  stage_input<T, P, false>(U, a);
+  stage_input<T, P, false, ORD>(U, a);
+  if constexpr (ORD) {
+    const unsigned long long m = cta_max(mag_as_double_bits(U.mx), &s_slot);
+    if (threadIdx.x == 0 && a.bnd_out) a.bnd_out[item] = m;
+  }
   stage_split<T, P>(U);
   __syncthreads();
   stage_col1<T, P>(U, 2 * (U.mg / 2), 2 * ((U.mg + U.K + 1) / 2));
@@ -1077,11 +1343,13 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_sky_spec(Src src) {
 // unit's output stage starts: its reductions leave the HBM reads free, and the
 // data is in L2 when the next unit's spectrum stage reads it.  (Prefetching a
 // whole unit ahead was slower: the prefetches then compete with the current
-// unit's spectrum loads.)
+// unit's spectrum loads.)  One problem: the overlap-add is exact in two words.
 template <typename T, int P, typename Src>
 __global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_from_spec(Src src, int units) {
   using R = Tr<T, P>;
+  constexpr bool ORD = std::is_same<Src, OneProblem>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ unsigned long long s_slot;
   Unit<T, P> U;
   pdl_trigger();
   int g = blockIdx.x;
@@ -1092,6 +1360,11 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_from_spec(Src src, int uni
   prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
   pdl_wait();
   if (threadIdx.x == 32) prefetch_l2(U.spec, sizeof(cx<T>) * P * R::H);
+  Split2<T> sp{};
+  if constexpr (ORD) {
+    int lu;
+    sp = output_splitter<T>(src.at(g, lu), &s_slot);
+  }
   for (;;) {
     const int gn = g + (int)gridDim.x;
     stage_mid<T, P, MID_FROM_SPEC, false>(U);
@@ -1109,7 +1382,7 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_from_spec(Src src, int uni
     }
     {
       int lu;
-      stage_output<T, P, false>(U, src.at(g, lu));
+      stage_output<T, P, false, ORD>(U, src.at(g, lu), sp);
     }
     if (gn >= units) break;
     __syncthreads();  // the output stage's last staging reads before the next mid writes
@@ -1119,9 +1392,9 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_from_spec(Src src, int uni
   }
 }
 
-// Adjoint, module-shared: per unit, cotangent spectrum * conj(PSF spectrum)
-// added into the patch's (zero) accumulator; the CTAs also clear the
-// (E,nx,ny) output that the next kernel adds into when called alone ...
+// Adjoint, module-shared, over a list of problems: per unit, cotangent spectrum
+// * conj(PSF spectrum) added into the patch's (zero) accumulator by L2
+// reductions ...
 // A loop over units: CTA b takes units b, b + G, b + 2G, ... (G = gridDim.x,
 // as many CTAs as fit on the GPU at once; one per SM at P = 192).  The next unit's first input chunk is issued into the
 // staging area before this unit's spectrum stage, which leaves the staging
@@ -1176,29 +1449,118 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_to_spec(Src src, int units
   }
 }
 
-// ... then, per (energy, patch), one inverse transform -> window -> gradient;
-// the accumulator is cleared as it is read.
+// Shared memory of the ordered adjoint beyond the tile: column 0's two terms
+// and running sum (3 P complex values).
+template <typename T, int P>
+constexpr size_t ord_extra_smem() { return 3 * (size_t)P * sizeof(cx<T>); }
+
+// Adjoint, module-shared, one problem, in unit order: CTA b of G takes the
+// contiguous units [b U / G, (b + 1) U / G) -- the modules of a patch one after
+// another -- and sums each patch's products over modules in TMEM in module
+// order (stage_acc_tmem).  Module 0's CTA writes the patch's accumulator; a
+// CTA whose range starts inside a patch writes its part to its spill slot,
+// which the next kernel adds in CTA order.  No atomics, no clearing of the
+// accumulator: the sums are the same bits on every run.  The CTAs clear the
+// gradient's low words (and, when asked, the gradient) and record the largest
+// cotangent magnitude they read (the bound of the gradient terms).
+template <typename T, int P>
+__global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_to_spec_ord(Args a, int units) {
+  using R = Tr<T, P>;
+  using TG = TmemGeom<T, P>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ uint32_t s_tmem;
+  __shared__ unsigned long long s_slot;
+  cx<T>* c0 = reinterpret_cast<cx<T>*>(smem_raw + R::SMEM);
+  pdl_trigger();
+  const int64_t G = gridDim.x, b = blockIdx.x;
+  const int lo = (int)(b * units / G), hi = (int)((b + 1) * units / G);
+  Unit<T, P> U;
+  U.init(a, smem_raw, true, lo);
+  prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
+  if (U.warp == 0) tmem_alloc(&s_tmem, TG::NCOLS);
+  tmem_fence_before_sync();
+  __syncthreads();
+  tmem_fence_after_sync();
+  const uint32_t tbase = s_tmem;
+  pdl_wait();
+  const int64_t gbytes = (int64_t)a.E * a.nx * a.ny * (int64_t)sizeof(T);
+  if (a.zero_out) zero_slice(a.out, gbytes, a.zchunk);
+  if (a.out_lo) zero_slice(a.out_lo, gbytes, a.zchunk);
+  bool pre = false;
+  for (int g = lo; g < hi; ++g) {
+    stage_input<T, P, true, true>(U, a, pre);
+    stage_split<T, P>(U);
+    __syncthreads();
+    stage_col1<T, P>(U, 0, P);
+    __syncthreads();
+    if (g + 1 < hi) {  // the next unit's first input chunk, into the staging area
+      Unit<T, P> N;
+      N.geom(a, smem_raw, true, g + 1);
+      input_issue<T, P, true>(N, a, InChunks<T, P, true>(N), 0);
+    }
+    const bool first = g == lo || U.m == 0;
+    const bool last = g == hi - 1 || U.m == a.M - 1;
+    cx<T>* dest = (g - U.m >= lo) ? U.spec : (cx<T>*)a.spill + b * (int64_t)(P * R::H);
+    stage_acc_tmem<T, P>(U, tbase, first, last, dest, c0, c0 + P, c0 + 2 * P);
+    if (g + 1 >= hi) break;
+    __syncthreads();
+    U.geom(a, smem_raw, true, g + 1);
+    prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
+    pre = true;
+  }
+  const unsigned long long m = cta_max(mag_as_double_bits(U.mx), &s_slot);
+  if (threadIdx.x == 0 && a.bnd_out) a.bnd_out[b] = m;
+  tmem_fence_before_sync();
+  __syncthreads();
+  tmem_fence_after_sync();
+  if (U.warp == 0) tmem_dealloc(tbase, TG::NCOLS);
+}
+
+// ... then, per (energy, patch), one inverse transform -> window -> gradient.
+// One problem: the accumulator plus the continuing CTAs' spill slots (in CTA
+// order), and the gradient accumulates exactly in two words.  A list of
+// problems: the accumulator is cleared as it is read.
 template <typename T, int P, typename Src>
 __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_from_spec(Src src) {
   using R = Tr<T, P>;
+  constexpr bool ORD = std::is_same<Src, OneProblem>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ unsigned long long s_slot;
   Unit<T, P> U;
   pdl_trigger();
   int item;
   const Args& a = src.at((int)blockIdx.x, item);
   U.init(a, smem_raw, false, item);
+  if constexpr (ORD) {
+    // CTAs b of the ordered adjoint whose first unit lies inside this patch:
+    // floor(b U / G) in (u0, u0 + M)
+    const int64_t Ut = (int64_t)a.M * a.E * a.n * a.n, G = a.loop_grid;
+    const int64_t u0 = (int64_t)item * a.M;
+    int64_t b = ((u0 + 1) * G + Ut - 1) / Ut;
+    U.sp0 = (const cx<T>*)a.spill + b * (int64_t)(P * R::H);
+    int n = 0;
+    while (b < G && (b * Ut) / G < u0 + a.M) {
+      ++n;
+      ++b;
+    }
+    U.nsp = n;
+  }
   pdl_wait();
+  Split2<T> sp{};
+  if constexpr (ORD) sp = output_splitter<T>(a, &s_slot);
   stage_mid<T, P, MID_FROM_ACC, true>(U);
   __syncthreads();
   stage_invB<T, P, 0>(U, U.tid, R::NT);
   __syncthreads();
   stage_combine<T, P>(U, U.mg / 2, (U.mg + U.K + 1) / 2);
   __syncthreads();
-  stage_output<T, P, true>(U, a);
-  // leave this patch's accumulator zero for the next call (read in the first stage)
-  float4* z = reinterpret_cast<float4*>(U.spec);
-  constexpr int n16 = (int)(sizeof(cx<T>) * P * R::H / 16);
-  for (int i = threadIdx.x; i < n16; i += R::NT) z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  stage_output<T, P, true, ORD>(U, a, sp);
+  if constexpr (!ORD) {
+    // leave this patch's accumulator zero for the next call (read in the first stage)
+    float4* z = reinterpret_cast<float4*>(U.spec);
+    constexpr int n16 = (int)(sizeof(cx<T>) * P * R::H / 16);
+    for (int i = threadIdx.x; i < n16; i += R::NT) z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
 }
 
 template <typename KernelT>
@@ -1220,7 +1582,7 @@ std::mutex g_occ_mu;
 std::vector<OccEntry> g_occ;
 
 template <typename T, int P, typename KernelT>
-int64_t loop_grid(KernelT kern, int64_t count) {
+int64_t loop_grid(KernelT kern, int64_t count, size_t smem = Tr<T, P>::SMEM) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
   int per_sm = 0;
@@ -1230,8 +1592,8 @@ int64_t loop_grid(KernelT kern, int64_t count) {
       if (e.kern == (const void*)kern && e.dev == dev) per_sm = e.per_sm;
   }
   if (!per_sm) {
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, Tr<T, P>::NT,
-                                                      Tr<T, P>::SMEM) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, Tr<T, P>::NT, smem) !=
+            cudaSuccess ||
         per_sm < 1) {
       cudaGetLastError();
       per_sm = 1;
@@ -1283,7 +1645,34 @@ Args make_args(const Geom& g, const FusedLaunch& f, int which, size_t esz) {
   a.in_rs = f.in_rs > 0 ? f.in_rs : (int64_t)g.ny;
   a.in_ps = f.in_ps > 0 ? f.in_ps : g.pixels();
   a.in_exp = f.in_exp ? 1 : 0;
+  a.out_lo = f.out_lo;
+  a.bnd_in = (const unsigned long long*)f.bnd_in;
+  a.bnd_n = f.bnd_n;
+  a.bnd_log2 = f.bnd_log2;
+  a.bnd_scale = f.bnd_scale;
+  a.bnd_out = (unsigned long long*)f.bnd_out;
+  a.spill = f.spill;
+  a.loop_grid = (int)f.loop_grid;
   return a;
+}
+
+// Dynamic shared memory of the ordered adjoint: the tile, column 0's arrays,
+// and -- where more CTAs would fit an SM than its 512 TMEM columns serve --
+// enough extra that no more than that many CTAs share an SM.
+template <typename T, int P>
+size_t ord_smem_bytes() {
+  const size_t s = Tr<T, P>::SMEM + ord_extra_smem<T, P>();
+  const int cap = 512 / TmemGeom<T, P>::NCOLS;
+  int dev = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) !=
+          cudaSuccess ||
+      per_sm <= 0) {
+    cudaGetLastError();
+    per_sm = 233472;
+  }
+  const size_t floor_s = (((size_t)per_sm / (size_t)(cap + 1) + 1) + 127) & ~(size_t)127;
+  return std::max(s, floor_s);
 }
 
 // The shared-memory opt-in is a per-device function attribute: set it once per
@@ -1307,12 +1696,12 @@ int ensure_smem_attrs() {
     JUBIK_TRY(set_smem(k_fused_group<T, P, true>, smem));
     JUBIK_TRY(set_smem(k_sky_spec<T, P, OneProblem>, smem));
     JUBIK_TRY(set_smem(k_adj_from_spec<T, P, OneProblem>, smem));
-    JUBIK_TRY(set_smem(k_adj_to_spec<T, P, OneProblem>, smem));
     JUBIK_TRY(set_smem(k_fwd_from_spec<T, P, OneProblem>, smem));
     JUBIK_TRY(set_smem(k_sky_spec<T, P, ProblemList>, smem));
     JUBIK_TRY(set_smem(k_adj_from_spec<T, P, ProblemList>, smem));
     JUBIK_TRY(set_smem(k_adj_to_spec<T, P, ProblemList>, smem));
     JUBIK_TRY(set_smem(k_fwd_from_spec<T, P, ProblemList>, smem));
+    JUBIK_TRY(set_smem(k_adj_to_spec_ord<T, P>, ord_smem_bytes<T, P>()));
     attr_set[dev] = true;
   }
   return JUBIK_OK;
@@ -1320,6 +1709,22 @@ int ensure_smem_attrs() {
 
 // Launch with programmatic stream serialisation when pdl: the kernel may be
 // scheduled while the previous kernel of the stream drains (see pdl_wait).
+template <typename T, int P, typename KernelT, typename... ArgsT>
+int launch_pdl_smem(KernelT kern, int64_t grid, size_t smem, bool pdl, cudaStream_t s,
+                    ArgsT... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(Tr<T, P>::NT);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cuda_status(cudaLaunchKernelEx(&cfg, kern, args...), "fused kernel launch");
+}
+
 template <typename T, int P, typename KernelT, typename... ArgsT>
 int launch_pdl(KernelT kern, int64_t grid, bool pdl, cudaStream_t s, ArgsT... args) {
   cudaLaunchConfig_t cfg = {};
@@ -1333,6 +1738,13 @@ int launch_pdl(KernelT kern, int64_t grid, bool pdl, cudaStream_t s, ArgsT... ar
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   return cuda_status(cudaLaunchKernelEx(&cfg, kern, args...), "fused kernel launch");
+}
+
+// Grid of the ordered adjoint over g's units (its CTAs' unit ranges and spill
+// slots depend on it).
+template <typename T, int P>
+int64_t ord_grid(const Geom& g) {
+  return loop_grid<T, P>(k_adj_to_spec_ord<T, P>, g.units(), ord_smem_bytes<T, P>());
 }
 
 template <typename T, int P>
@@ -1350,25 +1762,44 @@ int launch_one(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
     set_error("module-shared kernels need the spectrum workspace");
     return JUBIK_ERR_STATE;
   }
+  // every one-problem launch accumulates its output exactly in two words
+  auto need = [&](bool ok, const char* what) {
+    if (!ok) set_error("fused stage %d: %s missing", which, what);
+    return ok;
+  };
   switch (which) {
-    case FUSED_FWD_UNITS: return launch_pdl<T, P>(k_fused<T, P, false>, units, f.pdl, s, a);
-    case FUSED_ADJ_UNITS: return launch_pdl<T, P>(k_fused<T, P, true>, units, f.pdl, s, a);
+    case FUSED_FWD_UNITS:
+    case FUSED_ADJ_UNITS:
+      if (!need(f.out_lo && f.bnd_in && f.bnd_n > 0, "low-word plane or input bound"))
+        return JUBIK_ERR_STATE;
+      return which == FUSED_FWD_UNITS
+                 ? launch_pdl<T, P>(k_fused<T, P, false>, units, f.pdl, s, a)
+                 : launch_pdl<T, P>(k_fused<T, P, true>, units, f.pdl, s, a);
     case FUSED_FWD_SKY:
+      if (!need(f.out_lo && f.bnd_out, "low-word plane or bound record")) return JUBIK_ERR_STATE;
       return launch_pdl<T, P>(k_sky_spec<T, P, OneProblem>, patches, f.pdl, s, OneProblem{a});
     case FUSED_FWD_FROM_SPEC:
+      if (!need(f.out_lo && f.bnd_in && f.bnd_n == patches, "low-word plane or input bound"))
+        return JUBIK_ERR_STATE;
       return launch_pdl<T, P>(k_fwd_from_spec<T, P, OneProblem>,
                               loop_grid<T, P>(k_fwd_from_spec<T, P, OneProblem>, units), f.pdl,
                               s, OneProblem{a}, (int)units);
     case FUSED_ADJ_TO_SPEC: {
-      // as many CTAs as fit at once, looping over the units
-      const int64_t grid = loop_grid<T, P>(k_adj_to_spec<T, P, OneProblem>, units);
+      // contiguous unit ranges, as many CTAs as fit at once (and as the spill holds)
+      const int64_t grid = ord_grid<T, P>(g);
+      if (!need(f.spill && f.bnd_out && f.loop_grid == grid, "spill slots or bound record"))
+        return JUBIK_ERR_STATE;
       Args al = a;
       const int64_t zbytes = (int64_t)g.E * g.pixels() * (int64_t)sizeof(T);
       al.zchunk = ((zbytes + grid - 1) / grid + 15) & ~(int64_t)15;
-      return launch_pdl<T, P>(k_adj_to_spec<T, P, OneProblem>, grid, f.pdl, s, OneProblem{al},
-                              (int)units);
+      return launch_pdl_smem<T, P>(k_adj_to_spec_ord<T, P>, grid, ord_smem_bytes<T, P>(), f.pdl,
+                                   s, al, (int)units);
     }
     case FUSED_ADJ_FROM_SPEC:
+      if (!need(f.out_lo && f.bnd_in && f.spill && f.loop_grid == ord_grid<T, P>(g) &&
+                    f.bnd_n == f.loop_grid,
+                "low-word plane, spill slots or input bound"))
+        return JUBIK_ERR_STATE;
       return launch_pdl<T, P>(k_adj_from_spec<T, P, OneProblem>, patches, f.pdl, s,
                               OneProblem{a});
     default:
@@ -1517,10 +1948,53 @@ size_t fused_spec_bytes(const Geom& g, int dtype) {
   return c * (size_t)g.E * g.n * g.n * g.P * (g.P / 2);
 }
 
+template <typename T>
+int ensure_attrs_dispatch(int P) {
+  switch (P) {
+    case 32: return ensure_smem_attrs<T, 32>();
+    case 64: return ensure_smem_attrs<T, 64>();
+    case 96: return ensure_smem_attrs<T, 96>();
+    case 128: return ensure_smem_attrs<T, 128>();
+    case 160:
+      if constexpr (sizeof(T) == 4) return ensure_smem_attrs<T, 160>();
+      break;
+    case 192:
+      if constexpr (sizeof(T) == 4) return ensure_smem_attrs<T, 192>();
+      break;
+    default: break;
+  }
+  return JUBIK_ERR_UNSUPPORTED;
+}
+
+template <typename T>
+int64_t ord_grid_dispatch(const Geom& g) {
+  switch (g.P) {
+    case 32: return ord_grid<T, 32>(g);
+    case 64: return ord_grid<T, 64>(g);
+    case 96: return ord_grid<T, 96>(g);
+    case 128: return ord_grid<T, 128>(g);
+    case 160:
+      if constexpr (sizeof(T) == 4) return ord_grid<T, 160>(g);
+      break;
+    case 192:
+      if constexpr (sizeof(T) == 4) return ord_grid<T, 192>(g);
+      break;
+    default: break;
+  }
+  return 0;
+}
+
 size_t fused_smem_bytes(int P, int dtype) {
   const size_t c = dtype == JUBIK_F32 ? 8 : 16;
   const size_t H = P / 2, TP = P + 1, CH = H < 32 ? H : 32;
   return c * (H * TP + CH * TP);
+}
+
+int64_t fused_adj_grid(const Geom& g, int dtype) {
+  if (!fused_supported(g.P, dtype)) return 0;
+  if ((dtype == JUBIK_F32 ? ensure_attrs_dispatch<float>(g.P) : ensure_attrs_dispatch<double>(g.P)))
+    return 0;
+  return dtype == JUBIK_F32 ? ord_grid_dispatch<float>(g) : ord_grid_dispatch<double>(g);
 }
 
 int fused_run(const Geom& g, int dtype, const FusedLaunch& a, int which, cudaStream_t s) {

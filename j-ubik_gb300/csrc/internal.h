@@ -97,7 +97,25 @@ struct FusedLaunch {
   int64_t in_rs = 0, in_ps = 0;
   bool in_exp = false;
   bool clear = true;    // false: the kernels clear nothing (grouped launches clear first)
+  // One-problem launches accumulate their output exactly in two words: `out`
+  // and its low-word plane out_lo (same layout).  The terms are bounded by
+  // bnd_scale * the largest of the bnd_n magnitude maxima at bnd_in (device
+  // doubles' bits), at most 2^bnd_log2 terms per element.  bnd_out receives
+  // the maxima a kernel records (sky spectra: one per (energy, patch); ordered
+  // adjoint: one per CTA).
+  void* out_lo = nullptr;
+  const void* bnd_in = nullptr;
+  int bnd_n = 0, bnd_log2 = 0;
+  double bnd_scale = 0.0;
+  void* bnd_out = nullptr;
+  // ordered module-shared adjoint: spill slots (loop_grid x P x P/2 complex)
+  // and its grid (fused_adj_grid)
+  void* spill = nullptr;
+  int64_t loop_grid = 0;
 };
+// CTAs of the ordered module-shared adjoint for geometry g (0 where the fused
+// path does not cover g.P): the count of its unit ranges and spill slots.
+int64_t fused_adj_grid(const Geom& g, int dtype);
 size_t fused_spec_bytes(const Geom& g, int dtype);
 // Grouped per-unit launches over independent problems of one FFT side: the
 // kernel-argument block of one problem's stage (fused_args_size() bytes,
@@ -110,7 +128,7 @@ struct PoissonJob {
   const void* eps;
   const int32_t* dimg;
   int64_t npix;
-  void* lam;
+  void* wts;  // metric weights eps^2 / lam (image space)
   void* resid;
   double* partials;
   unsigned int* counter;
@@ -179,19 +197,35 @@ int slice_patches_adjoint_op(const void* patches, int64_t batch, int nx, int ny,
 // response epilogues / prologues over the (M,E,nx,ny) image
 template <typename T>
 int readout_gather(const void* img, const void* eps, const int64_t* idx, int64_t nread,
-                   void* out, cudaStream_t s);
+                   void* out, cudaStream_t s, const void* img_lo = nullptr);
 template <typename T>
 int readout_scatter(const void* vec, const void* eps, const int64_t* idx, int64_t nread,
                     void* img, cudaStream_t s);
 template <typename T>
-int poisson_image(const void* conv, const void* eps, const int32_t* dimg, int64_t npix,
-                  void* lam_cache, void* resid, double* partials, unsigned int* counter,
-                  double* energy, bool pdl, cudaStream_t s);
+int poisson_image(const void* conv, const void* conv_lo, const void* eps, const int32_t* dimg,
+                  int64_t npix, void* lam_cache, void* resid, double* partials,
+                  unsigned int* counter, double* energy, bool pdl, cudaStream_t s);
+// Largest magnitude of an (E, rows, cols) array with plane stride ps and row
+// stride rs (of exp(value) when exp_of), as nb <= kMaxBoundBlocks maxima
+// (bits of non-negative doubles) at out; returns nb.
+constexpr int kMaxBoundBlocks = 256;
+template <typename T>
+int absmax_blocks(const void* in, int E, int rows, int cols, int64_t ps, int64_t rs, bool exp_of,
+                  void* out, int* nb, bool pdl, cudaStream_t s);
+// hi[i] += lo[i] for n elements: the value of a two-word accumulation
+template <typename T>
+int combine_words(void* hi, const void* lo, int64_t n, bool pdl, cudaStream_t s);
 int count_image(const int32_t* ridx, const int32_t* data, int64_t npix, int32_t* dimg,
                 cudaStream_t s);
+// wts = eps^2 / lam with lam = eps * conv (conv_lo: the low words of a
+// two-word conv, or nullptr) at read-out pixels (ridx >= 0), 0 elsewhere
 template <typename T>
-int metric_weights(const void* conv_v, const void* eps, const int32_t* ridx, const void* lam_cache,
-                   int64_t npix, void* resid, cudaStream_t s);
+int metric_weights(const void* conv, const void* conv_lo, const void* eps, const int32_t* ridx,
+                   int64_t npix, void* wts, cudaStream_t s);
+// out = w * (hi + lo) (lo nullptr: w * hi), n elements
+template <typename T>
+int apply_weights(const void* hi, const void* lo, const void* w, int64_t n, void* out, bool pdl,
+                  cudaStream_t s);
 template <typename T>
 int poisson_vec(const void* lam, const int32_t* data, int64_t n, double* partials,
                 unsigned int* counter, double* energy, void* grad, cudaStream_t s);

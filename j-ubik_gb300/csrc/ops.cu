@@ -1,4 +1,5 @@
 // Gather/scatter, spectrum preparation, unfused-path and likelihood kernels.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 
@@ -51,16 +52,29 @@ __global__ void k_psf_to_cplx(const T* __restrict__ psf, int layout, int e_bcast
     if (ib < 0) ib += ny;
     return (double)psf[((mk * Esrc + esrc) * nx + ia) * (int64_t)ny + ib];
   };
-  double acc = 0.0;
-  for (int i = threadIdx.x; i < K * K; i += blockDim.x) acc += fetch(i / K, i % K);
+  double acc = 0.0, aacc = 0.0;
+  for (int i = threadIdx.x; i < K * K; i += blockDim.x) {
+    const double v = fetch(i / K, i % K);
+    acc += v;
+    aacc += fabs(v);
+  }
+  __shared__ double ared[kBlock];
   red[threadIdx.x] = acc;
+  ared[threadIdx.x] = aacc;
   __syncthreads();
   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    if (threadIdx.x < w) {
+      red[threadIdx.x] += red[threadIdx.x + w];
+      ared[threadIdx.x] += ared[threadIdx.x + w];
+    }
     __syncthreads();
   }
   const double sum = red[0];
-  if (threadIdx.x == 0) sums[blockIdx.x] = sum;
+  // (sum, sum of magnitudes) of the window: the normalisation and its gain
+  if (threadIdx.x == 0) {
+    sums[2 * blockIdx.x] = sum;
+    sums[2 * blockIdx.x + 1] = ared[0];
+  }
   double2* dst = buf + (int64_t)blockIdx.x * P * P;
   for (int i = threadIdx.x; i < P * P; i += blockDim.x) dst[i] = make_double2(0.0, 0.0);
   __syncthreads();
@@ -441,11 +455,12 @@ __global__ void k_slice_patches_adjoint(const T* __restrict__ pt, int64_t batch,
 template <typename T>
 __global__ void k_readout_gather(const T* __restrict__ img, const T* __restrict__ eps,
                                  const int64_t* __restrict__ idx, int64_t nread,
-                                 T* __restrict__ out) {
+                                 T* __restrict__ out, const T* __restrict__ img_lo) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nread;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t p = idx[i];
-    out[i] = eps ? eps[p] * img[p] : img[p];
+    const T v = img_lo ? img[p] + img_lo[p] : img[p];  // a two-word image: hi + lo
+    out[i] = eps ? eps[p] * v : v;
   }
 }
 
@@ -533,29 +548,32 @@ __device__ __forceinline__ void block_reduce2(double a, double b, double* partia
 
 // One pass over the (M,E,nx,ny) images: lam = eps * conv where a pixel is read
 // out (count image >= 0), the energy terms, the residual eps * (1 - d/lam)
-// (0 elsewhere) and, optionally, lam itself for later metric products.
+// (0 elsewhere) and, optionally, the metric weight eps^2 / lam (0 elsewhere)
+// that later Fisher-metric products apply to R v: the image-space weights of
+// R^T diag(1/lam) R (the exposure enters once from R and once from R^T).
 template <typename T>
-__device__ __forceinline__ void poisson_px(T conv, T ep, int32_t d, T& lam_o, T& res_o,
+__device__ __forceinline__ void poisson_px(T conv, T ep, int32_t d, T& w_o, T& res_o,
                                            Kahan<T>& s_lam, Kahan<T>& s_dlog) {
   if (d < 0) {
     res_o = (T)0;
-    lam_o = (T)0;
+    w_o = (T)0;
     return;
   }
   const T lam = ep * conv;
   const T dd = (T)d;
   s_lam.add(lam);
   s_dlog.add(dd * log(lam));
-  lam_o = lam;
+  w_o = (ep * ep) / lam;
   res_o = ep * ((T)1 - dd / lam);
 }
 
 // One problem's pass over its (M,E,nx,ny) images by block bid of nblocks.
 template <typename T>
 __device__ __forceinline__ void poisson_image_body(const T* __restrict__ conv,
+                                                   const T* __restrict__ conv_lo,
                                                    const T* __restrict__ eps,
                                                    const int32_t* __restrict__ dimg, int64_t npix,
-                                                   T* __restrict__ lam_cache, T* __restrict__ resid,
+                                                   T* __restrict__ wts, T* __restrict__ resid,
                                                    double* partials, unsigned int* counter,
                                                    double* energy, unsigned int bid,
                                                    unsigned int nblocks) {
@@ -575,41 +593,53 @@ __device__ __forceinline__ void poisson_image_body(const T* __restrict__ conv,
       poisson_px<T>(c.z, ep.z, d.z, l.z, r.z, s_lam, s_dlog);
       poisson_px<T>(c.w, ep.w, d.w, l.w, r.w, s_lam, s_dlog);
       if (resid) reinterpret_cast<float4*>(resid)[g] = r;
-      if (lam_cache) __stcs(reinterpret_cast<float4*>(lam_cache) + g, l);
+      if (wts) __stcs(reinterpret_cast<float4*>(wts) + g, l);
     };
     int64_t g = bid * (int64_t)blockDim.x + threadIdx.x;
+    // a two-word image (exact overlap-add): the value is hi + lo
+    const float4* l4 = reinterpret_cast<const float4*>(conv_lo);
+    auto cval = [&](int64_t i) {
+      float4 c = __ldcs(c4 + i);
+      if (l4) {
+        const float4 l = __ldcs(l4 + i);
+        c = make_float4(c.x + l.x, c.y + l.y, c.z + l.z, c.w + l.w);
+      }
+      return c;
+    };
     for (; g + stride < n4; g += 2 * stride) {
-      const float4 ca = __ldcs(c4 + g), cb = __ldcs(c4 + g + stride);
+      const float4 ca = cval(g), cb = cval(g + stride);
       const float4 ea = eps ? __ldcs(e4 + g) : make_float4(1, 1, 1, 1);
       const float4 eb = eps ? __ldcs(e4 + g + stride) : make_float4(1, 1, 1, 1);
       const int4 da = __ldcs(d4 + g), db = __ldcs(d4 + g + stride);
       px4(g, ca, ea, da);
       px4(g + stride, cb, eb, db);
     }
-    if (g < n4) px4(g, __ldcs(c4 + g), eps ? __ldcs(e4 + g) : make_float4(1, 1, 1, 1), __ldcs(d4 + g));
+    if (g < n4) px4(g, cval(g), eps ? __ldcs(e4 + g) : make_float4(1, 1, 1, 1), __ldcs(d4 + g));
     p0 = n4 * 4;
   }
   for (int64_t p = p0 + bid * (int64_t)blockDim.x + threadIdx.x; p < npix; p += stride) {
     T l, r;
-    poisson_px<T>(conv[p], eps ? eps[p] : (T)1, dimg[p], l, r, s_lam, s_dlog);
+    poisson_px<T>(conv_lo ? conv[p] + conv_lo[p] : conv[p], eps ? eps[p] : (T)1, dimg[p], l, r,
+                  s_lam, s_dlog);
     if (resid) resid[p] = r;
-    if (lam_cache) lam_cache[p] = l;
+    if (wts) wts[p] = l;
   }
   block_reduce2_of(s_lam.value(), s_dlog.value(), partials, counter, energy, bid, nblocks);
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kBlock)
-    k_poisson_image(const T* __restrict__ conv, const T* __restrict__ eps,
-                    const int32_t* __restrict__ dimg, int64_t npix, T* __restrict__ lam_cache,
+    k_poisson_image(const T* __restrict__ conv, const T* __restrict__ conv_lo,
+                    const T* __restrict__ eps,
+                    const int32_t* __restrict__ dimg, int64_t npix, T* __restrict__ wts,
                     T* __restrict__ resid, double* partials, unsigned int* counter,
                     double* energy) {
   // launched with programmatic stream serialisation after the forward kernels:
   // let the adjoint be scheduled early, wait for the forward image
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   asm volatile("griddepcontrol.wait;" ::: "memory");
-  poisson_image_body<T>(conv, eps, dimg, npix, lam_cache, resid, partials, counter, energy,
-                        blockIdx.x, gridDim.x);
+  poisson_image_body<T>(conv, conv_lo, eps, dimg, npix, wts, resid, partials, counter,
+                        energy, blockIdx.x, gridDim.x);
 }
 
 // Grouped launch: job j (one problem) owns blocks [starts[j], starts[j + 1]).
@@ -633,7 +663,7 @@ __global__ void __launch_bounds__(kBlock)
   }
   __syncthreads();
   const PoissonJob jb = jobs[s_job];
-  poisson_image_body<T>((const T*)jb.conv, (const T*)jb.eps, jb.dimg, jb.npix, (T*)jb.lam,
+  poisson_image_body<T>((const T*)jb.conv, nullptr, (const T*)jb.eps, jb.dimg, jb.npix, (T*)jb.wts,
                         (T*)jb.resid, jb.partials, jb.counter, jb.energy,
                         blockIdx.x - starts[s_job], starts[s_job + 1] - starts[s_job]);
 }
@@ -694,19 +724,53 @@ __global__ void __launch_bounds__(kBlock)
   block_reduce2(s_lam.value(), s_dlog.value(), partials, counter, energy);
 }
 
+// Metric weights eps^2 / lam of a fresh lam = eps * conv (conv in two words,
+// conv_lo nullptr for one): the same expression as the likelihood pass.
 template <typename T>
-__global__ void k_metric_weights(const T* __restrict__ conv_v, const T* __restrict__ eps,
-                                 const int32_t* __restrict__ ridx, const T* __restrict__ lam,
-                                 int64_t npix, T* __restrict__ resid) {
+__global__ void k_metric_weights(const T* __restrict__ conv, const T* __restrict__ conv_lo,
+                                 const T* __restrict__ eps, const int32_t* __restrict__ ridx,
+                                 int64_t npix, T* __restrict__ wts) {
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npix;
        p += (int64_t)gridDim.x * blockDim.x) {
     if (ridx[p] < 0) {
-      resid[p] = (T)0;
+      wts[p] = (T)0;
       continue;
     }
     const T ep = eps ? eps[p] : (T)1;
-    resid[p] = ep * ((ep * conv_v[p]) / lam[p]);
+    const T c = conv_lo ? conv[p] + conv_lo[p] : conv[p];
+    wts[p] = (ep * ep) / (ep * c);
   }
+}
+
+// resid = w * (hi + lo): the weighted image a metric product hands to the
+// adjoint, made in the same pass that adds the two words of R v.
+template <typename T>
+__global__ void __launch_bounds__(kBlock)
+    k_apply_weights(const T* __restrict__ hi, const T* __restrict__ lo, const T* __restrict__ w,
+                    int64_t n, T* __restrict__ out) {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t i0 = 0;
+  if constexpr (sizeof(T) == 4) {  // all plan buffers are 16-byte aligned
+    const int64_t n4 = n / 4;
+    const float4* h4 = reinterpret_cast<const float4*>(hi);
+    const float4* l4 = reinterpret_cast<const float4*>(lo);
+    const float4* w4 = reinterpret_cast<const float4*>(w);
+    float4* o4 = reinterpret_cast<float4*>(out);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n4; i += stride) {
+      float4 h = __ldcs(h4 + i);
+      if (lo) {
+        const float4 l = __ldcs(l4 + i);
+        h = make_float4(h.x + l.x, h.y + l.y, h.z + l.z, h.w + l.w);
+      }
+      const float4 ww = __ldg(w4 + i);
+      o4[i] = make_float4(ww.x * h.x, ww.y * h.y, ww.z * h.z, ww.w * h.w);
+    }
+    i0 = n4 * 4;
+  }
+  for (int64_t i = i0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride)
+    out[i] = w[i] * (lo ? hi[i] + lo[i] : hi[i]);
 }
 
 template <typename T>
@@ -870,10 +934,10 @@ int slice_patches_adjoint_op(const void* patches, int64_t batch, int nx, int ny,
 
 template <typename T>
 int readout_gather(const void* img, const void* eps, const int64_t* idx, int64_t nread,
-                   void* out, cudaStream_t s) {
+                   void* out, cudaStream_t s, const void* img_lo) {
   if (nread <= 0) return JUBIK_OK;
   k_readout_gather<T><<<grid_for(nread), kBlock, 0, s>>>((const T*)img, (const T*)eps, idx,
-                                                         nread, (T*)out);
+                                                         nread, (T*)out, (const T*)img_lo);
   return cuda_status(cudaGetLastError(), "k_readout_gather");
 }
 
@@ -887,9 +951,9 @@ int readout_scatter(const void* vec, const void* eps, const int64_t* idx, int64_
 }
 
 template <typename T>
-int poisson_image(const void* conv, const void* eps, const int32_t* dimg, int64_t npix,
-                  void* lam_cache, void* resid, double* partials, unsigned int* counter,
-                  double* energy, bool pdl, cudaStream_t s) {
+int poisson_image(const void* conv, const void* conv_lo, const void* eps, const int32_t* dimg,
+                  int64_t npix, void* wts, void* resid, double* partials,
+                  unsigned int* counter, double* energy, bool pdl, cudaStream_t s) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(kRedBlocks);
   cfg.blockDim = dim3(kBlock);
@@ -899,9 +963,9 @@ int poisson_image(const void* conv, const void* eps, const int32_t* dimg, int64_
   attr[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cuda_status(cudaLaunchKernelEx(&cfg, k_poisson_image<T>, (const T*)conv, (const T*)eps,
-                                        dimg, npix, (T*)lam_cache, (T*)resid, partials, counter,
-                                        energy),
+  return cuda_status(cudaLaunchKernelEx(&cfg, k_poisson_image<T>, (const T*)conv,
+                                        (const T*)conv_lo, (const T*)eps, dimg, npix,
+                                        (T*)wts, (T*)resid, partials, counter, energy),
                      "k_poisson_image");
 }
 
@@ -912,11 +976,30 @@ int count_image(const int32_t* ridx, const int32_t* data, int64_t npix, int32_t*
 }
 
 template <typename T>
-int metric_weights(const void* conv_v, const void* eps, const int32_t* ridx, const void* lam_cache,
-                   int64_t npix, void* resid, cudaStream_t s) {
-  k_metric_weights<T><<<grid_for(npix), kBlock, 0, s>>>((const T*)conv_v, (const T*)eps, ridx,
-                                                        (const T*)lam_cache, npix, (T*)resid);
+int metric_weights(const void* conv, const void* conv_lo, const void* eps, const int32_t* ridx,
+                   int64_t npix, void* wts, cudaStream_t s) {
+  k_metric_weights<T><<<grid_for(npix), kBlock, 0, s>>>((const T*)conv, (const T*)conv_lo,
+                                                        (const T*)eps, ridx, npix, (T*)wts);
   return cuda_status(cudaGetLastError(), "k_metric_weights");
+}
+
+template <typename T>
+int apply_weights(const void* hi, const void* lo, const void* w, int64_t n, void* out, bool pdl,
+                  cudaStream_t s) {
+  if (n <= 0) return JUBIK_OK;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)std::min<int64_t>(4096, std::max<int64_t>(1, (n / 4 + kBlock - 1) /
+                                                                              kBlock)));
+  cfg.blockDim = dim3(kBlock);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cuda_status(cudaLaunchKernelEx(&cfg, k_apply_weights<T>, (const T*)hi, (const T*)lo,
+                                        (const T*)w, n, (T*)out),
+                     "k_apply_weights");
 }
 
 template <typename T>
@@ -933,6 +1016,109 @@ int elementwise_op(int op, const void* a, const void* b, const int32_t* d, int64
   if (n <= 0) return JUBIK_OK;
   k_elementwise<T><<<grid_for(n), kBlock, 0, s>>>(op, (const T*)a, (const T*)b, d, n, (T*)out);
   return cuda_status(cudaGetLastError(), "k_elementwise");
+}
+
+// Largest magnitude of an (E, rows, cols) view (exp of the values when
+// exp_of): one maximum per block, as the bits of a non-negative double (a NaN
+// sorts above every number).  Grid-stride over the view.
+template <typename T>
+__global__ void __launch_bounds__(kBlock)
+    k_absmax(const T* __restrict__ in, int E, int rows, int cols, int64_t ps, int64_t rs,
+             int exp_of, unsigned long long* __restrict__ out) {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  const int64_t n = (int64_t)E * rows * cols;
+  // the largest value (exp_of: exp is increasing, applied once at the end) or magnitude
+  T m = exp_of ? (T)-INFINITY : (T)0;
+  bool nan = false;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = i / ((int64_t)rows * cols), rc = i - e * rows * cols;
+    const int64_t r = rc / cols, c = rc - r * cols;
+    const T v = in[e * ps + r * rs + c];
+    const T a = exp_of ? v : (v < (T)0 ? -v : v);
+    nan |= (a != a);
+    m = a > m ? a : m;
+  }
+  __shared__ unsigned long long red[kBlock / 32];
+  const double md = exp_of ? exp((double)m) : (double)m;  // exp(-inf) = 0 for an empty share
+  unsigned long long b = nan ? 0x7ff8000000000000ull : (unsigned long long)__double_as_longlong(md);
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long t = __shfl_xor_sync(0xffffffffu, b, o);
+    b = t > b ? t : b;
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = b;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long r = 0ull;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = red[w] > r ? red[w] : r;
+    out[blockIdx.x] = r;
+  }
+}
+
+template <typename T>
+int absmax_blocks(const void* in, int E, int rows, int cols, int64_t ps, int64_t rs, bool exp_of,
+                  void* out, int* nb, bool pdl, cudaStream_t s) {
+  const int64_t n = (int64_t)E * rows * cols;
+  int blocks = (int)std::min<int64_t>(kMaxBoundBlocks, std::max<int64_t>(1, (n + kBlock - 1) /
+                                                                               kBlock));
+  *nb = blocks;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(kBlock);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cuda_status(cudaLaunchKernelEx(&cfg, k_absmax<T>, (const T*)in, E, rows, cols, ps, rs,
+                                        exp_of ? 1 : 0, (unsigned long long*)out),
+                     "k_absmax");
+}
+
+// hi[i] += lo[i]: the value of an exact two-word accumulation, rounded once.
+template <typename T>
+__global__ void __launch_bounds__(kBlock)
+    k_combine(T* __restrict__ hi, const T* __restrict__ lo, int64_t n) {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t i0 = 0;
+  if constexpr (sizeof(T) == 4) {  // all plan buffers are 16-byte aligned
+    const int64_t n4 = n / 4;
+    float4* h4 = reinterpret_cast<float4*>(hi);
+    const float4* l4 = reinterpret_cast<const float4*>(lo);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n4; i += stride) {
+      float4 h = h4[i];
+      const float4 l = __ldcs(l4 + i);
+      h4[i] = make_float4(h.x + l.x, h.y + l.y, h.z + l.z, h.w + l.w);
+    }
+    i0 = n4 * 4;
+  }
+  for (int64_t i = i0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride)
+    hi[i] = hi[i] + lo[i];
+}
+
+template <typename T>
+int combine_words(void* hi, const void* lo, int64_t n, bool pdl, cudaStream_t s) {
+  if (n <= 0) return JUBIK_OK;
+  if ((reinterpret_cast<uintptr_t>(hi) | reinterpret_cast<uintptr_t>(lo)) & 15) {
+    set_error("combine_words: buffers must be 16-byte aligned");
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)std::min<int64_t>(4096, std::max<int64_t>(1, (n / 4 + kBlock - 1) /
+                                                                              kBlock)));
+  cfg.blockDim = dim3(kBlock);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cuda_status(cudaLaunchKernelEx(&cfg, k_combine<T>, (T*)hi, (const T*)lo, n),
+                     "k_combine");
 }
 
 #define JUBIK_INST(T)                                                                            \
@@ -955,13 +1141,19 @@ int elementwise_op(int op, const void* a, const void* b, const int32_t* d, int64
   template int slice_patches_adjoint_op<T>(const void*, int64_t, int, int, int, int, void*,      \
                                            cudaStream_t);                                        \
   template int readout_gather<T>(const void*, const void*, const int64_t*, int64_t, void*,       \
-                                 cudaStream_t);                                                  \
+                                 cudaStream_t, const void*);                                     \
   template int readout_scatter<T>(const void*, const void*, const int64_t*, int64_t, void*,      \
                                   cudaStream_t);                                                 \
-  template int poisson_image<T>(const void*, const void*, const int32_t*, int64_t, void*, void*, \
-                                double*, unsigned int*, double*, bool, cudaStream_t);            \
-  template int metric_weights<T>(const void*, const void*, const int32_t*, const void*, int64_t, \
+  template int poisson_image<T>(const void*, const void*, const void*, const int32_t*, int64_t,  \
+                                void*, void*, double*, unsigned int*, double*, bool,             \
+                                cudaStream_t);                                                   \
+  template int absmax_blocks<T>(const void*, int, int, int, int64_t, int64_t, bool, void*, int*,  \
+                                bool, cudaStream_t);                                             \
+  template int combine_words<T>(void*, const void*, int64_t, bool, cudaStream_t);                \
+  template int metric_weights<T>(const void*, const void*, const void*, const int32_t*, int64_t, \
                                  void*, cudaStream_t);                                           \
+  template int apply_weights<T>(const void*, const void*, const void*, int64_t, void*, bool,     \
+                                cudaStream_t);                                                   \
   template int poisson_vec<T>(const void*, const int32_t*, int64_t, double*, unsigned int*,      \
                               double*, void*, cudaStream_t);                                     \
   template int elementwise_op<T>(int, const void*, const void*, const int32_t*, int64_t, void*,  \

@@ -147,7 +147,8 @@ class ResponsePlan:
     def _s(self):
         return stream_handle(self.device)
 
-    PHASES = ("forward", "adjoint", "likelihood", "memset", "forward_patch", "adjoint_patch")
+    PHASES = ("forward", "adjoint", "likelihood", "memset", "forward_patch", "adjoint_patch",
+              "finish")
 
     def set_dependent_launch(self, on: bool = True) -> "ResponsePlan":
         """Programmatic dependent launch between the kernels of a call (default on)."""

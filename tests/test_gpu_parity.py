@@ -343,14 +343,13 @@ def test_dependent_launch_switch_keeps_results(cuda, dtype):
     plan.set_exposure(inst.exposure, inst.readmask)
     lam = plan.response(inst.sky).double().cpu().numpy()
     plan.set_data(synthetic.poisson_data(lam, 2))
-    tol = 1e-13 if dtype == torch.float64 else 1e-6
     e1, g1 = plan.energy_and_grad(inst.sky)
     g1 = g1.clone()
     plan.set_dependent_launch(False)
-    for _ in range(2):  # twice: the adjoint accumulator is left zero after each call
+    for _ in range(2):  # twice, serialised launches: the same bits as the chained call
         e2, g2 = plan.energy_and_grad(inst.sky)
-        assert abs(float(e2) - float(e1)) <= tol * abs(float(e1))
-        assert rel(g2, g1.double().cpu().numpy()) < (1e-13 if dtype == torch.float64 else 1e-5)
+        assert float(e2) == float(e1)
+        assert torch.equal(g2, g1)
     plan.close()
 
 
@@ -422,8 +421,8 @@ def test_non_finite_sky_propagates_without_fault(cuda):
         assert not np.isfinite(float(e))
         assert not bool(torch.isfinite(g).all())
     e1, g1 = plan.energy_and_grad(inst.sky)
-    assert abs(float(e1) - e0) <= 1e-9 * abs(e0)
-    assert rel(g1, g0.double().cpu().numpy()) < 1e-5
+    # the fused sums are exact in any order: the finite call returns the same bits
+    assert float(e1) == e0 and torch.equal(g1, g0)
     plan.close()
 
 
