@@ -456,14 +456,24 @@ int do_forward(jubik_plan* p, const void* x, void* out, void* out_lo, double sca
 
 // transpose: out_x (E,nx,ny) = scale * sum_m psf_m^T cot[m]; on the fused path
 // in two words (out_x, out_lo), the caller adding them (combine_words)
+// bnd_n: block maxima of |cot| that the kernel which wrote cot left in
+// p->bnd_a (0: none, a pass over cot records them)
 int do_adjoint(jubik_plan* p, const void* cot, void* out_x, void* out_lo, double scale,
-               cudaStream_t s, bool out_zeroed = false) {
+               cudaStream_t s, bool out_zeroed = false, int bnd_n = 0) {
   const Geom& g = p->g;
   if (p->path == JUBIK_PATH_FUSED) {
     const int L = adj_terms_log2(g);
     // every partial sum of a gradient pixel is bounded by (windows x modules) x
     // (kernel gain) x |scale| x the largest cotangent magnitude
     const double bscale = 2.0 * (double)(int64_t(1) << L) * p->kmax * std::fabs(scale);
+    if (bnd_n <= 0) {
+      Phase ph(p, 3, s);
+      JUBIK_TRY(p->dtype == JUBIK_F32
+                    ? absmax_blocks<float>(cot, g.M * g.E, g.nx, g.ny, g.pixels(), g.ny, false,
+                                           p->bnd_a, &bnd_n, p->pdl, s)
+                    : absmax_blocks<double>(cot, g.M * g.E, g.nx, g.ny, g.pixels(), g.ny, false,
+                                            p->bnd_a, &bnd_n, p->pdl, s));
+    }
     if (!p->spec) {
       {
         Phase ph(p, 3, s);
@@ -475,15 +485,9 @@ int do_adjoint(jubik_plan* p, const void* cot, void* out_x, void* out_lo, double
       a.out_lo = out_lo;
       a.bnd_log2 = L;
       a.bnd_scale = bscale;
-      Phase ph(p, 1, s);
-      int nb = 0;
-      JUBIK_TRY(p->dtype == JUBIK_F32
-                    ? absmax_blocks<float>(cot, g.M * g.E, g.nx, g.ny, g.pixels(), g.ny, false,
-                                           p->bnd_a, &nb, p->pdl, s)
-                    : absmax_blocks<double>(cot, g.M * g.E, g.nx, g.ny, g.pixels(), g.ny, false,
-                                            p->bnd_a, &nb, p->pdl, s));
       a.bnd_in = p->bnd_a;
-      a.bnd_n = nb;
+      a.bnd_n = bnd_n;
+      Phase ph(p, 1, s);
       return fused_run(g, p->dtype, a, FUSED_ADJ_UNITS, s);
     }
     // ordered per-unit kernel: clears out_x (unless zeroed) and out_lo, sums each
@@ -499,13 +503,11 @@ int do_adjoint(jubik_plan* p, const void* cot, void* out_x, void* out_lo, double
     a.bnd_scale = bscale;
     {
       Phase ph(p, 1, s);
-      a.bnd_out = p->bnd_a;
       JUBIK_TRY(fused_run(g, p->dtype, a, FUSED_ADJ_TO_SPEC, s));
     }
     Phase ph(p, 5, s);
-    a.bnd_out = nullptr;
     a.bnd_in = p->bnd_a;
-    a.bnd_n = (int)p->adj_grid;
+    a.bnd_n = bnd_n;
     return fused_run(g, p->dtype, a, FUSED_ADJ_FROM_SPEC, s);
   }
   Phase ph(p, 1, s);
@@ -680,8 +682,8 @@ int jubik_plan_create(const jubik_plan_desc* d, jubik_plan** out) {
     if ((st = p->alloc(&p->bnd_f, sizeof(uint64_t) * std::max<int64_t>(patches,
                                                                         kMaxBoundBlocks))))
       return fail(st);
-    if ((st = p->alloc(&p->bnd_a, sizeof(uint64_t) * std::max<int64_t>(p->adj_grid,
-                                                                        kMaxBoundBlocks))))
+    if ((st = p->alloc(&p->bnd_a, sizeof(uint64_t) *
+                                      std::max<int64_t>(energy_partials_count(), kMaxBoundBlocks))))
       return fail(st);
   } else {
     if ((st = p->alloc(&p->hfull, (size_t)units * g.P * (g.P / 2 + 1) * csz))) return fail(st);
@@ -993,14 +995,15 @@ int jubik_poisson_energy_grad(jubik_plan* p, const void* x, double* energy, void
   JUBIK_TRY(p->dtype == JUBIK_F32
                 ? poisson_image<float>(p->conv, lo, p->eps, p->dimg, img, p->wts,
                                        grad_x ? p->resid : nullptr, p->partials, p->counter,
-                                       energy, p->pdl, s)
+                                       energy, p->pdl, s, grad_x ? p->bnd_a : nullptr)
                 : poisson_image<double>(p->conv, lo, p->eps, p->dimg, img, p->wts,
                                         grad_x ? p->resid : nullptr, p->partials, p->counter,
-                                        energy, p->pdl, s));
+                                        energy, p->pdl, s, grad_x ? p->bnd_a : nullptr));
   }
   p->lam_valid = true;
   if (!grad_x) return JUBIK_OK;
-  JUBIK_TRY(do_adjoint(p, p->resid, grad_x, p->grad_lo, p->desc.pixel_area, s, grad_zeroed));
+  JUBIK_TRY(do_adjoint(p, p->resid, grad_x, p->grad_lo, p->desc.pixel_area, s, grad_zeroed,
+                       energy_partials_count()));
   Phase ph(p, 6, s);
   return finish_words(p, grad_x, p->grad_lo, (int64_t)p->g.E * p->g.pixels(), s);
 }
@@ -1034,14 +1037,16 @@ int jubik_poisson_energy_grad_logsky(jubik_plan* p, const void* s_log, int32_t e
     JUBIK_TRY(p->dtype == JUBIK_F32
                   ? poisson_image<float>(p->conv, lo, p->eps, p->dimg, img, p->wts,
                                          grad_s ? p->resid : nullptr, p->partials, p->counter,
-                                         energy, p->pdl, s)
+                                         energy, p->pdl, s, grad_s ? p->bnd_a : nullptr)
                   : poisson_image<double>(p->conv, lo, p->eps, p->dimg, img, p->wts,
                                           grad_s ? p->resid : nullptr, p->partials,
-                                          p->counter, energy, p->pdl, s));
+                                          p->counter, energy, p->pdl, s,
+                                          grad_s ? p->bnd_a : nullptr));
   }
   p->lam_valid = true;
   if (!grad_s) return JUBIK_OK;
-  JUBIK_TRY(do_adjoint(p, p->resid, p->xgrad, p->grad_lo, p->desc.pixel_area, s, grad_zeroed));
+  JUBIK_TRY(do_adjoint(p, p->resid, p->xgrad, p->grad_lo, p->desc.pixel_area, s, grad_zeroed,
+                       energy_partials_count()));
   const void* glo = p->path == JUBIK_PATH_FUSED ? p->grad_lo : nullptr;
   const int64_t n = (int64_t)e_pad * nx_pad * ny_pad;
   if (p->dtype == JUBIK_F32)
@@ -1078,15 +1083,16 @@ int jubik_metric_apply(jubik_plan* p, const void* x, const void* v, void* out, v
   bool out_zeroed = false;
   JUBIK_TRY(do_forward(p, v, p->conv_v, p->conv_v_lo, p->desc.pixel_area, s, out,
                        (int64_t)p->g.E * p->g.pixels() * (int64_t)p->esz, &out_zeroed));
+  int nb = 0;
   {
     Phase ph(p, 2, s);
     JUBIK_TRY(p->dtype == JUBIK_F32
                   ? apply_weights<float>(p->conv_v, two ? p->conv_v_lo : nullptr, p->wts, img,
-                                         p->resid, p->pdl, s)
+                                         p->resid, p->pdl, s, p->bnd_a, &nb)
                   : apply_weights<double>(p->conv_v, two ? p->conv_v_lo : nullptr, p->wts, img,
-                                          p->resid, p->pdl, s));
+                                          p->resid, p->pdl, s, p->bnd_a, &nb));
   }
-  JUBIK_TRY(do_adjoint(p, p->resid, out, p->grad_lo, p->desc.pixel_area, s, out_zeroed));
+  JUBIK_TRY(do_adjoint(p, p->resid, out, p->grad_lo, p->desc.pixel_area, s, out_zeroed, nb));
   Phase ph(p, 6, s);
   return finish_words(p, out, p->grad_lo, (int64_t)p->g.E * p->g.pixels(), s);
 }

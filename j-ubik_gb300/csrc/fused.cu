@@ -1392,6 +1392,153 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_from_spec(Src src, int uni
   }
 }
 
+// ---- forward of aligned geometries in runs of vertically adjacent patches
+// When P = 3 dx with dx = 64 and margin dx / 2, a patch's P x P output covers
+// exactly three block rows of dx field rows (i - 1, i, i + 1 for patch row i),
+// and the staging chunks of the output stage (32 pair rows) are those block
+// rows.  A CTA then takes runs of kRun vertically adjacent patches of one
+// module and adds the block rows they share in TMEM, in patch order, before
+// they leave the CTA: each block row of a run is reduced into the image once
+// (as an exact two-word sum), 6 block rows per run of 4 patches instead of 12.
+// The 7 modules of a run are consecutive work items, which neighbouring CTAs
+// run at the same time, so the shared sky spectra still meet in L2.
+constexpr int kRun = 4;
+constexpr int kRunCols = 96;  // TMEM columns of one pending block row (per lane)
+
+// Output stage of patch s (0 .. kRun - 1) of a run: chunk c is block row
+// i - 1 + c.  Thread (warp w, lane) owns row (32 (w % 4) + lane) / 2 of each
+// chunk, columns 96 ((32 (w % 4) + lane) % 2) + 32 (w / 4) .. + 32, and the same
+// positions of the two pending block rows in its TMEM lane (slot = block row % 2).
+template <typename T, int P>
+__device__ __forceinline__ void stage_output_run(Unit<T, P>& U, const Args& a,
+                                                 const Split2<T>& sp, uint32_t tbase, int s) {
+  static_assert(sizeof(T) == 4 && P == 192, "runs cover FP32 patches of side 192");
+  using R = Tr<T, P>;
+  constexpr int L1 = R::L1, TP = R::TP, CH = R::CH;
+  const T scale = (T)a.scale;
+  const int lane128 = 32 * (U.warp & 3) + U.lane, gcol = U.warp >> 2;
+  const int rr = lane128 >> 1, x0 = (lane128 & 1) * 96 + gcol * 32;
+  const uint32_t tl = tbase + ((uint32_t)(32 * (U.warp & 3)) << 16) + (uint32_t)(gcol * 32);
+  const int64_t plane = ((int64_t)U.m * a.E + U.e) * U.npix;
+  T* __restrict__ dst = (T*)a.out + plane;
+  T* __restrict__ dlo = (T*)a.out_lo + plane;
+  const int col = U.cb + x0;  // a multiple of 32: the group lies wholly in or out of the field
+  const bool col_in = col >= 0 && col + 32 <= a.ny;
+  const int i = U.k % a.n;    // patch row
+  for (int c = 0; c < 3; ++c) {
+    const int j0 = c * CH;
+    cx<T>* stg = (c & 1) ? U.tile + (j0 - CH) * TP : U.stg;
+    {  // inverse variant-A phase 2 of the chunk's 32 pair rows -> natural order
+      const int jj = U.lane;
+      const cx<T>* srcr = U.tile + (j0 + jj) * TP + 16 * U.cls;
+      cx<T> v[16];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) v[q] = q ? cmulc<T>(srcr[q], U.wq[q]) : srcr[q];
+      Dft<16, true, T>::run(v);
+#pragma unroll
+      for (int q = 0; q < 16; ++q) stg[jj * TP + U.cls + L1 * q] = v[q];
+    }
+    __syncthreads();
+    const cx<T>* sr = stg + (rr >> 1) * TP + x0;
+    T v[32];
+    if (rr & 1) {
+#pragma unroll
+      for (int j = 0; j < 32; ++j) v[j] = scale * sr[j].y;
+    } else {
+#pragma unroll
+      for (int j = 0; j < 32; ++j) v[j] = scale * sr[j].x;
+    }
+    const int br = i - 1 + c;  // block row of the field
+    const uint32_t ta = tl + (uint32_t)(((br + 2) & 1) * kRunCols);
+    // warp-uniform: pending rows exist from the run's previous patch; a row
+    // leaves the CTA once no later patch of the run adds to it
+    if (s > 0 && c < 2) {
+      uint32_t r[32];
+      tmem_ld32(ta, r);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) v[j] += __uint_as_float(r[j]);
+    }
+    if (c == 0 || s == kRun - 1) {
+      const int row = U.rb + 2 * j0 + rr;
+      if (col_in && row >= 0 && row < a.nx) {
+        const int64_t o = (int64_t)row * a.ny + col;
+#pragma unroll
+        for (int g = 0; g < 8; ++g)
+          acc4<true>((float*)(dst + o + 4 * g), (float*)(dlo + o + 4 * g),
+                     (const Split2<float>&)sp, v[4 * g], v[4 * g + 1], v[4 * g + 2],
+                     v[4 * g + 3]);
+      }
+    } else {
+      uint32_t r[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) r[j] = __float_as_uint(v[j]);
+      tmem_st32(ta, r);
+    }
+  }
+  tmem_wait_st();
+}
+
+// Work item w of the run-ordered forward: module fastest, then the run q of
+// kRun patch rows, the patch column j, the energy e.  Returns unit (w, s).
+__device__ __forceinline__ int run_unit(const Args& a, int w, int s) {
+  const int nq = a.n / kRun;
+  const int m = w % a.M;
+  int t = w / a.M;
+  const int q = t % nq;
+  t /= nq;
+  const int j = t % a.n, e = t / a.n;
+  const int k = kRun * q + s + a.n * j;
+  return ((e * a.n * a.n + k) * a.M + m);
+}
+
+template <typename T, int P>
+__global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_run(Args a, int items) {
+  using R = Tr<T, P>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ unsigned long long s_slot;
+  __shared__ uint32_t s_tmem;
+  pdl_trigger();
+  int w = blockIdx.x, s = 0;
+  Unit<T, P> U;
+  U.init(a, smem_raw, true, run_unit(a, w, 0));
+  prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
+  if (U.warp == 0) tmem_alloc(&s_tmem, 2 * kRunCols <= 256 ? 256 : 512);
+  tmem_fence_before_sync();
+  __syncthreads();
+  tmem_fence_after_sync();
+  const uint32_t tbase = s_tmem;
+  pdl_wait();
+  if (threadIdx.x == 32) prefetch_l2(U.spec, sizeof(cx<T>) * P * R::H);
+  const Split2<T> sp = output_splitter<T>(a, &s_slot);
+  for (;;) {
+    const int sn = s + 1 < kRun ? s + 1 : 0;
+    const int wn = s + 1 < kRun ? w : w + (int)gridDim.x;
+    const bool more = wn < items;
+    stage_mid<T, P, MID_FROM_SPEC, false>(U);
+    __syncthreads();
+    stage_invB<T, P, 0>(U, U.tid, R::NT);
+    __syncthreads();
+    stage_combine<T, P>(U, 0, R::H);
+    __syncthreads();
+    if (more) {  // the output stage's reductions leave HBM reads free
+      Unit<T, P> N;
+      N.geom(a, smem_raw, true, run_unit(a, wn, sn));
+      prefetch_unit(N.hmain, sizeof(cx<T>) * P * R::H, N.hnyq, sizeof(cx<T>) * P);
+      if (threadIdx.x == 32) prefetch_l2(N.spec, sizeof(cx<T>) * P * R::H);
+    }
+    stage_output_run<T, P>(U, a, sp, tbase, s);
+    if (!more) break;
+    __syncthreads();  // the output stage's last staging reads before the next mid writes
+    w = wn;
+    s = sn;
+    U.geom(a, smem_raw, true, run_unit(a, w, s));
+  }
+  tmem_fence_before_sync();
+  __syncthreads();
+  tmem_fence_after_sync();
+  if (U.warp == 0) tmem_dealloc(tbase, 2 * kRunCols <= 256 ? 256 : 512);
+}
+
 // Adjoint, module-shared, over a list of problems: per unit, cotangent spectrum
 // * conj(PSF spectrum) added into the patch's (zero) accumulator by L2
 // reductions ...
@@ -1454,28 +1601,74 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_to_spec(Src src, int units
 template <typename T, int P>
 constexpr size_t ord_extra_smem() { return 3 * (size_t)P * sizeof(cx<T>); }
 
-// Adjoint, module-shared, one problem, in unit order: CTA b of G takes the
-// contiguous units [b U / G, (b + 1) U / G) -- the modules of a patch one after
-// another -- and sums each patch's products over modules in TMEM in module
-// order (stage_acc_tmem).  Module 0's CTA writes the patch's accumulator; a
-// CTA whose range starts inside a patch writes its part to its spill slot,
-// which the next kernel adds in CTA order.  No atomics, no clearing of the
-// accumulator: the sums are the same bits on every run.  The CTAs clear the
-// gradient's low words (and, when asked, the gradient) and record the largest
-// cotangent magnitude they read (the bound of the gradient terms).
+// Unit schedule of the ordered adjoint over P patches of M modules on G CTAs:
+// R = floor(P / G) full rounds in which CTA b takes patch b + r G with all its
+// modules (neighbouring CTAs work on neighbouring patches at the same time, so
+// the overlapping cotangent windows meet in L2), then the units of the
+// remaining patches in Gt = min(G, tail units) non-empty contiguous ranges
+// (CTAs b >= Gt have none).  Tail units are u = tail0 ... (unit u = patch * M +
+// module).
+struct OrdSchedule {
+  int64_t G, M, rounds, tail0, tail_units, Gt;
+  __device__ __forceinline__ OrdSchedule(int64_t g, int64_t m, int64_t patches)
+      : G(g), M(m), rounds(patches / g), tail0((patches / g) * g * m),
+        tail_units((patches - (patches / g) * g) * m),
+        Gt(tail_units < g ? tail_units : g) {}
+  __device__ __forceinline__ int64_t tail_lo(int64_t b) const {
+    return b >= Gt ? tail0 + tail_units : tail0 + b * tail_units / Gt;
+  }
+  __device__ __forceinline__ int64_t count(int64_t b) const {
+    return rounds * M + tail_lo(b + 1) - tail_lo(b);
+  }
+  __device__ __forceinline__ int64_t unit(int64_t b, int64_t t) const {
+    if (t < rounds * M) return (b + (t / M) * G) * M + t % M;
+    return tail_lo(b) + (t - rounds * M);
+  }
+};
+
+// Adjoint, module-shared, one problem, in module order: each CTA takes its
+// units from OrdSchedule -- the modules of a patch one after another -- and
+// sums each patch's products over modules in TMEM in module order
+// (stage_acc_tmem).  The CTA holding module 0 of a patch writes the patch's
+// accumulator; a CTA whose tail range starts inside a patch writes its part to
+// its spill slot, which the next kernel adds in CTA order.  No atomics, no
+// clearing of the accumulator: the sums are the same bits on every run.  The
+// CTAs clear the gradient's low words (and, when asked, the gradient); the
+// bound of the gradient terms comes from the kernel that wrote the cotangent.
+//
+// Position in a CTA's unit sequence of OrdSchedule, advanced without divisions.
+struct OrdCursor {
+  int64_t t, r, m, g;
+  __device__ __forceinline__ OrdCursor(const OrdSchedule& s, int64_t b)
+      : t(0), r(0), m(0), g(s.unit(b, 0)) {}
+  __device__ __forceinline__ void advance(const OrdSchedule& s, int64_t b, int64_t tlo) {
+    ++t;
+    if (t < s.rounds * s.M) {
+      if (++m == s.M) {
+        m = 0;
+        ++r;
+      }
+      g = (b + r * s.G) * s.M + m;
+    } else {
+      g = tlo + (t - s.rounds * s.M);
+    }
+  }
+};
+
 template <typename T, int P>
 __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_to_spec_ord(Args a, int units) {
   using R = Tr<T, P>;
   using TG = TmemGeom<T, P>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ uint32_t s_tmem;
-  __shared__ unsigned long long s_slot;
   cx<T>* c0 = reinterpret_cast<cx<T>*>(smem_raw + R::SMEM);
   pdl_trigger();
-  const int64_t G = gridDim.x, b = blockIdx.x;
-  const int lo = (int)(b * units / G), hi = (int)((b + 1) * units / G);
+  const int64_t b = blockIdx.x;
+  const OrdSchedule sch(gridDim.x, a.M, units / a.M);
+  const int64_t cnt = sch.count(b), tlo = sch.tail_lo(b), tail_start = sch.rounds * sch.M;
+  OrdCursor cur(sch, b);
   Unit<T, P> U;
-  U.init(a, smem_raw, true, lo);
+  U.init(a, smem_raw, true, (int)cur.g);
   prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
   if (U.warp == 0) tmem_alloc(&s_tmem, TG::NCOLS);
   tmem_fence_before_sync();
@@ -1487,29 +1680,32 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_to_spec_ord(Args a, int un
   if (a.zero_out) zero_slice(a.out, gbytes, a.zchunk);
   if (a.out_lo) zero_slice(a.out_lo, gbytes, a.zchunk);
   bool pre = false;
-  for (int g = lo; g < hi; ++g) {
-    stage_input<T, P, true, true>(U, a, pre);
+  while (cur.t < cnt) {
+    const int64_t t = cur.t, g = cur.g;
+    stage_input<T, P, true>(U, a, pre);
     stage_split<T, P>(U);
     __syncthreads();
     stage_col1<T, P>(U, 0, P);
     __syncthreads();
-    if (g + 1 < hi) {  // the next unit's first input chunk, into the staging area
-      Unit<T, P> N;
-      N.geom(a, smem_raw, true, g + 1);
+    OrdCursor nx = cur;
+    nx.advance(sch, b, tlo);
+    Unit<T, P> N;
+    if (nx.t < cnt) {  // the next unit's first input chunk, into the staging area
+      N.geom(a, smem_raw, true, (int)nx.g);
       input_issue<T, P, true>(N, a, InChunks<T, P, true>(N), 0);
     }
-    const bool first = g == lo || U.m == 0;
-    const bool last = g == hi - 1 || U.m == a.M - 1;
-    cx<T>* dest = (g - U.m >= lo) ? U.spec : (cx<T>*)a.spill + b * (int64_t)(P * R::H);
+    const bool first = U.m == 0 || t == tail_start;
+    const bool last = U.m == a.M - 1 || t == cnt - 1;
+    const bool owner = t < tail_start || g - U.m >= tlo;  // module 0 of this patch is ours
+    cx<T>* dest = owner ? U.spec : (cx<T>*)a.spill + b * (int64_t)(P * R::H);
     stage_acc_tmem<T, P>(U, tbase, first, last, dest, c0, c0 + P, c0 + 2 * P);
-    if (g + 1 >= hi) break;
+    if (nx.t >= cnt) break;
     __syncthreads();
-    U.geom(a, smem_raw, true, g + 1);
+    cur = nx;
+    U.geom(a, smem_raw, true, (int)cur.g);
     prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
     pre = true;
   }
-  const unsigned long long m = cta_max(mag_as_double_bits(U.mx), &s_slot);
-  if (threadIdx.x == 0 && a.bnd_out) a.bnd_out[b] = m;
   tmem_fence_before_sync();
   __syncthreads();
   tmem_fence_after_sync();
@@ -1532,17 +1728,18 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_from_spec(Src src) {
   const Args& a = src.at((int)blockIdx.x, item);
   U.init(a, smem_raw, false, item);
   if constexpr (ORD) {
-    // CTAs b of the ordered adjoint whose first unit lies inside this patch:
-    // floor(b U / G) in (u0, u0 + M)
-    const int64_t Ut = (int64_t)a.M * a.E * a.n * a.n, G = a.loop_grid;
+    // CTAs of the ordered adjoint whose tail range starts inside this patch:
+    // tail_lo(b) in (u0, u0 + M) (none for the patches of the full rounds)
+    const int64_t G = a.loop_grid, patches = (int64_t)a.E * a.n * a.n;
+    const OrdSchedule sch(G, a.M, patches);
     const int64_t u0 = (int64_t)item * a.M;
-    int64_t b = ((u0 + 1) * G + Ut - 1) / Ut;
-    U.sp0 = (const cx<T>*)a.spill + b * (int64_t)(P * R::H);
     int n = 0;
-    while (b < G && (b * Ut) / G < u0 + a.M) {
-      ++n;
-      ++b;
+    int64_t b = 0;
+    if (u0 >= sch.tail0 && sch.tail_units > 0) {
+      b = ((u0 + 1 - sch.tail0) * sch.Gt + sch.tail_units - 1) / sch.tail_units;
+      while (b + n < sch.Gt && sch.tail_lo(b + n) < u0 + a.M) ++n;
     }
+    U.sp0 = (const cx<T>*)a.spill + b * (int64_t)(P * R::H);
     U.nsp = n;
   }
   pdl_wait();
@@ -1702,6 +1899,7 @@ int ensure_smem_attrs() {
     JUBIK_TRY(set_smem(k_adj_to_spec<T, P, ProblemList>, smem));
     JUBIK_TRY(set_smem(k_fwd_from_spec<T, P, ProblemList>, smem));
     JUBIK_TRY(set_smem(k_adj_to_spec_ord<T, P>, ord_smem_bytes<T, P>()));
+    if constexpr (sizeof(T) == 4 && P == 192) JUBIK_TRY(set_smem(k_fwd_run<T, P>, smem));
     attr_set[dev] = true;
   }
   return JUBIK_OK;
@@ -1738,6 +1936,14 @@ int launch_pdl(KernelT kern, int64_t grid, bool pdl, cudaStream_t s, ArgsT... ar
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   return cuda_status(cudaLaunchKernelEx(&cfg, kern, args...), "fused kernel launch");
+}
+
+// Geometries whose patch outputs share whole block rows of 64 field rows (see
+// k_fwd_run): P = 192 from 64-row strides and a 32-pixel margin, a field of
+// whole strides (no clamped start), and runs of kRun patch rows.
+inline bool run_geometry(const Geom& g) {
+  return g.P == 192 && g.dx == 64 && g.margin == 32 && g.nx == g.n * 64 && g.ny == g.n * 64 &&
+         g.n % kRun == 0 && g.M >= 2;
 }
 
 // Grid of the ordered adjoint over g's units (its CTAs' unit ranges and spill
@@ -1781,14 +1987,20 @@ int launch_one(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
     case FUSED_FWD_FROM_SPEC:
       if (!need(f.out_lo && f.bnd_in && f.bnd_n == patches, "low-word plane or input bound"))
         return JUBIK_ERR_STATE;
+      if constexpr (sizeof(T) == 4 && P == 192) {
+        if (run_geometry(g)) {
+          const int64_t items = units / kRun;
+          return launch_pdl<T, P>(k_fwd_run<T, P>, loop_grid<T, P>(k_fwd_run<T, P>, items),
+                                  f.pdl, s, a, (int)items);
+        }
+      }
       return launch_pdl<T, P>(k_fwd_from_spec<T, P, OneProblem>,
                               loop_grid<T, P>(k_fwd_from_spec<T, P, OneProblem>, units), f.pdl,
                               s, OneProblem{a}, (int)units);
     case FUSED_ADJ_TO_SPEC: {
       // contiguous unit ranges, as many CTAs as fit at once (and as the spill holds)
       const int64_t grid = ord_grid<T, P>(g);
-      if (!need(f.spill && f.bnd_out && f.loop_grid == grid, "spill slots or bound record"))
-        return JUBIK_ERR_STATE;
+      if (!need(f.spill && f.loop_grid == grid, "spill slots")) return JUBIK_ERR_STATE;
       Args al = a;
       const int64_t zbytes = (int64_t)g.E * g.pixels() * (int64_t)sizeof(T);
       al.zchunk = ((zbytes + grid - 1) / grid + 15) & ~(int64_t)15;
@@ -1796,8 +2008,8 @@ int launch_one(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
                                    s, al, (int)units);
     }
     case FUSED_ADJ_FROM_SPEC:
-      if (!need(f.out_lo && f.bnd_in && f.spill && f.loop_grid == ord_grid<T, P>(g) &&
-                    f.bnd_n == f.loop_grid,
+      if (!need(f.out_lo && f.bnd_in && f.bnd_n > 0 && f.spill &&
+                    f.loop_grid == ord_grid<T, P>(g),
                 "low-word plane, spill slots or input bound"))
         return JUBIK_ERR_STATE;
       return launch_pdl<T, P>(k_adj_from_spec<T, P, OneProblem>, patches, f.pdl, s,

@@ -201,10 +201,13 @@ int readout_gather(const void* img, const void* eps, const int64_t* idx, int64_t
 template <typename T>
 int readout_scatter(const void* vec, const void* eps, const int64_t* idx, int64_t nread,
                     void* img, cudaStream_t s);
+// (rmax: energy_partials_count() block maxima of |resid|, the bound of an
+// adjoint of resid, or nullptr)
 template <typename T>
 int poisson_image(const void* conv, const void* conv_lo, const void* eps, const int32_t* dimg,
-                  int64_t npix, void* lam_cache, void* resid, double* partials,
-                  unsigned int* counter, double* energy, bool pdl, cudaStream_t s);
+                  int64_t npix, void* wts, void* resid, double* partials,
+                  unsigned int* counter, double* energy, bool pdl, cudaStream_t s,
+                  void* rmax = nullptr);
 // Largest magnitude of an (E, rows, cols) array with plane stride ps and row
 // stride rs (of exp(value) when exp_of), as nb <= kMaxBoundBlocks maxima
 // (bits of non-negative doubles) at out; returns nb.
@@ -222,10 +225,11 @@ int count_image(const int32_t* ridx, const int32_t* data, int64_t npix, int32_t*
 template <typename T>
 int metric_weights(const void* conv, const void* conv_lo, const void* eps, const int32_t* ridx,
                    int64_t npix, void* wts, cudaStream_t s);
-// out = w * (hi + lo) (lo nullptr: w * hi), n elements
+// out = w * (hi + lo) (lo nullptr: w * hi), n elements; *nb block maxima of
+// |out| at rmax (nullptr: none)
 template <typename T>
 int apply_weights(const void* hi, const void* lo, const void* w, int64_t n, void* out, bool pdl,
-                  cudaStream_t s);
+                  cudaStream_t s, void* rmax = nullptr, int* nb = nullptr);
 template <typename T>
 int poisson_vec(const void* lam, const int32_t* data, int64_t n, double* partials,
                 unsigned int* counter, double* energy, void* grad, cudaStream_t s);

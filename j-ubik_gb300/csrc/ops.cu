@@ -567,6 +567,44 @@ __device__ __forceinline__ void poisson_px(T conv, T ep, int32_t d, T& w_o, T& r
   res_o = ep * ((T)1 - dd / lam);
 }
 
+// Block maximum of per-thread magnitudes (float or double bits; a NaN sorts
+// last), stored as the bits of a non-negative double at out[bid] by thread 0.
+__device__ __forceinline__ void store_block_max(unsigned long long v, unsigned long long* out,
+                                                unsigned int bid) {
+  __shared__ unsigned long long red[kBlock / 32];
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long t = __shfl_xor_sync(0xffffffffu, v, o);
+    v = t > v ? t : v;
+  }
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long r = 0ull;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = red[w] > r ? red[w] : r;
+    out[bid] = r;
+  }
+}
+__device__ __forceinline__ unsigned long long mag64(float v) {
+  return (unsigned long long)__double_as_longlong((double)fabsf(v));
+}
+__device__ __forceinline__ unsigned long long mag64(double v) {
+  return (unsigned long long)__double_as_longlong(fabs(v));
+}
+template <typename T>
+struct MagMax {  // running largest |v| of one thread, in T (a NaN is kept)
+  T m = (T)0;
+  bool nan = false;
+  __device__ __forceinline__ void add(T v) {
+    const T a = v < (T)0 ? -v : v;
+    nan |= (a != a);
+    m = a > m ? a : m;
+  }
+  __device__ __forceinline__ unsigned long long bits() const {
+    return nan ? 0x7ff8000000000000ull : mag64(m);
+  }
+};
+
 // One problem's pass over its (M,E,nx,ny) images by block bid of nblocks.
 template <typename T>
 __device__ __forceinline__ void poisson_image_body(const T* __restrict__ conv,
@@ -576,8 +614,10 @@ __device__ __forceinline__ void poisson_image_body(const T* __restrict__ conv,
                                                    T* __restrict__ wts, T* __restrict__ resid,
                                                    double* partials, unsigned int* counter,
                                                    double* energy, unsigned int bid,
-                                                   unsigned int nblocks) {
+                                                   unsigned int nblocks,
+                                                   unsigned long long* rmax) {
   Kahan<T> s_lam, s_dlog;
+  MagMax<T> mr;  // the residual's largest magnitude (bound of the adjoint's terms)
   const int64_t stride = (int64_t)nblocks * blockDim.x;
   int64_t p0 = 0;
   if constexpr (sizeof(T) == 4) {
@@ -593,6 +633,12 @@ __device__ __forceinline__ void poisson_image_body(const T* __restrict__ conv,
       poisson_px<T>(c.z, ep.z, d.z, l.z, r.z, s_lam, s_dlog);
       poisson_px<T>(c.w, ep.w, d.w, l.w, r.w, s_lam, s_dlog);
       if (resid) reinterpret_cast<float4*>(resid)[g] = r;
+      if (rmax) {
+        mr.add(r.x);
+        mr.add(r.y);
+        mr.add(r.z);
+        mr.add(r.w);
+      }
       if (wts) __stcs(reinterpret_cast<float4*>(wts) + g, l);
     };
     int64_t g = bid * (int64_t)blockDim.x + threadIdx.x;
@@ -623,7 +669,9 @@ __device__ __forceinline__ void poisson_image_body(const T* __restrict__ conv,
                   s_lam, s_dlog);
     if (resid) resid[p] = r;
     if (wts) wts[p] = l;
+    if (rmax) mr.add(r);
   }
+  if (rmax) store_block_max(mr.bits(), rmax, bid);
   block_reduce2_of(s_lam.value(), s_dlog.value(), partials, counter, energy, bid, nblocks);
 }
 
@@ -633,13 +681,13 @@ __global__ void __launch_bounds__(kBlock)
                     const T* __restrict__ eps,
                     const int32_t* __restrict__ dimg, int64_t npix, T* __restrict__ wts,
                     T* __restrict__ resid, double* partials, unsigned int* counter,
-                    double* energy) {
+                    double* energy, unsigned long long* rmax) {
   // launched with programmatic stream serialisation after the forward kernels:
   // let the adjoint be scheduled early, wait for the forward image
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   asm volatile("griddepcontrol.wait;" ::: "memory");
   poisson_image_body<T>(conv, conv_lo, eps, dimg, npix, wts, resid, partials, counter,
-                        energy, blockIdx.x, gridDim.x);
+                        energy, blockIdx.x, gridDim.x, rmax);
 }
 
 // Grouped launch: job j (one problem) owns blocks [starts[j], starts[j + 1]).
@@ -665,7 +713,7 @@ __global__ void __launch_bounds__(kBlock)
   const PoissonJob jb = jobs[s_job];
   poisson_image_body<T>((const T*)jb.conv, nullptr, (const T*)jb.eps, jb.dimg, jb.npix, (T*)jb.wts,
                         (T*)jb.resid, jb.partials, jb.counter, jb.energy,
-                        blockIdx.x - starts[s_job], starts[s_job + 1] - starts[s_job]);
+                        blockIdx.x - starts[s_job], starts[s_job + 1] - starts[s_job], nullptr);
 }
 
 // Grouped clearing: job j owns blocks [starts[j], starts[j + 1]) and clears its
@@ -747,10 +795,11 @@ __global__ void k_metric_weights(const T* __restrict__ conv, const T* __restrict
 template <typename T>
 __global__ void __launch_bounds__(kBlock)
     k_apply_weights(const T* __restrict__ hi, const T* __restrict__ lo, const T* __restrict__ w,
-                    int64_t n, T* __restrict__ out) {
+                    int64_t n, T* __restrict__ out, unsigned long long* __restrict__ rmax) {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   asm volatile("griddepcontrol.wait;" ::: "memory");
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  MagMax<T> mr;  // the weighted image's largest magnitude (bound of the adjoint's terms)
   int64_t i0 = 0;
   if constexpr (sizeof(T) == 4) {  // all plan buffers are 16-byte aligned
     const int64_t n4 = n / 4;
@@ -765,12 +814,20 @@ __global__ void __launch_bounds__(kBlock)
         h = make_float4(h.x + l.x, h.y + l.y, h.z + l.z, h.w + l.w);
       }
       const float4 ww = __ldg(w4 + i);
-      o4[i] = make_float4(ww.x * h.x, ww.y * h.y, ww.z * h.z, ww.w * h.w);
+      const float4 o = make_float4(ww.x * h.x, ww.y * h.y, ww.z * h.z, ww.w * h.w);
+      o4[i] = o;
+      mr.add(o.x);
+      mr.add(o.y);
+      mr.add(o.z);
+      mr.add(o.w);
     }
     i0 = n4 * 4;
   }
-  for (int64_t i = i0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride)
+  for (int64_t i = i0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
     out[i] = w[i] * (lo ? hi[i] + lo[i] : hi[i]);
+    mr.add(out[i]);
+  }
+  if (rmax) store_block_max(mr.bits(), rmax, blockIdx.x);
 }
 
 template <typename T>
@@ -953,7 +1010,7 @@ int readout_scatter(const void* vec, const void* eps, const int64_t* idx, int64_
 template <typename T>
 int poisson_image(const void* conv, const void* conv_lo, const void* eps, const int32_t* dimg,
                   int64_t npix, void* wts, void* resid, double* partials,
-                  unsigned int* counter, double* energy, bool pdl, cudaStream_t s) {
+                  unsigned int* counter, double* energy, bool pdl, cudaStream_t s, void* rmax) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(kRedBlocks);
   cfg.blockDim = dim3(kBlock);
@@ -965,7 +1022,8 @@ int poisson_image(const void* conv, const void* conv_lo, const void* eps, const 
   cfg.numAttrs = 1;
   return cuda_status(cudaLaunchKernelEx(&cfg, k_poisson_image<T>, (const T*)conv,
                                         (const T*)conv_lo, (const T*)eps, dimg, npix,
-                                        (T*)wts, (T*)resid, partials, counter, energy),
+                                        (T*)wts, (T*)resid, partials, counter, energy,
+                                        (unsigned long long*)rmax),
                      "k_poisson_image");
 }
 
@@ -985,11 +1043,12 @@ int metric_weights(const void* conv, const void* conv_lo, const void* eps, const
 
 template <typename T>
 int apply_weights(const void* hi, const void* lo, const void* w, int64_t n, void* out, bool pdl,
-                  cudaStream_t s) {
-  if (n <= 0) return JUBIK_OK;
+                  cudaStream_t s, void* rmax, int* nb) {
+  const unsigned grid = (unsigned)std::min<int64_t>(
+      kRedBlocks, std::max<int64_t>(1, (n / 4 + kBlock - 1) / kBlock));
+  if (nb) *nb = (int)grid;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)std::min<int64_t>(4096, std::max<int64_t>(1, (n / 4 + kBlock - 1) /
-                                                                              kBlock)));
+  cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(kBlock);
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
@@ -998,7 +1057,7 @@ int apply_weights(const void* hi, const void* lo, const void* w, int64_t n, void
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   return cuda_status(cudaLaunchKernelEx(&cfg, k_apply_weights<T>, (const T*)hi, (const T*)lo,
-                                        (const T*)w, n, (T*)out),
+                                        (const T*)w, n, (T*)out, (unsigned long long*)rmax),
                      "k_apply_weights");
 }
 
@@ -1146,14 +1205,14 @@ int combine_words(void* hi, const void* lo, int64_t n, bool pdl, cudaStream_t s)
                                   cudaStream_t);                                                 \
   template int poisson_image<T>(const void*, const void*, const void*, const int32_t*, int64_t,  \
                                 void*, void*, double*, unsigned int*, double*, bool,             \
-                                cudaStream_t);                                                   \
+                                cudaStream_t, void*);                                            \
   template int absmax_blocks<T>(const void*, int, int, int, int64_t, int64_t, bool, void*, int*,  \
                                 bool, cudaStream_t);                                             \
   template int combine_words<T>(void*, const void*, int64_t, bool, cudaStream_t);                \
   template int metric_weights<T>(const void*, const void*, const void*, const int32_t*, int64_t, \
                                  void*, cudaStream_t);                                           \
   template int apply_weights<T>(const void*, const void*, const void*, int64_t, void*, bool,     \
-                                cudaStream_t);                                                   \
+                                cudaStream_t, void*, int*);                                      \
   template int poisson_vec<T>(const void*, const int32_t*, int64_t, double*, unsigned int*,      \
                               double*, void*, cudaStream_t);                                     \
   template int elementwise_op<T>(int, const void*, const void*, const int32_t*, int64_t, void*,  \

@@ -278,23 +278,34 @@ def test_chandra_demo_geometry_unfused(cuda, dtype):
     plan.close()
 
 
-def test_fp32_gradient_and_metric_against_the_fp32_lambda_floor(cuda, deriv_case):
-    """The FP32 Poisson gradient R^T(1 - d/lam) and metric R^T(R t / lam) are
-    limited by lam itself: rounding the exact lam once to FP32, with every
-    other operation in float64, already moves them by `floor` (the conditioning
-    of 1 - d/lam and 1/lam at faint pixels).  The fused FP32 path's own
-    errors are reported beside that floor; they stay within a small multiple
-    of it while every other output meets 1e-6."""
+def test_fp32_gradient_and_metric_errors_come_from_the_fp32_forward(cuda, deriv_case):
+    """Where the FP32 Poisson gradient R^T(1 - d/lam) and metric R^T(R t / lam)
+    lose accuracy.  Rounding the exact lam once to FP32 (everything else in
+    float64) moves them only by `floor`.  An FP32 FFT convolution's error is
+    absolute, of order 1e-7 of a patch's brightest values, so faint pixels get
+    a much larger relative error of lam, which d/lam and 1/lam pass on: a
+    float64 gradient computed from the FP32 forward's lam already shows the
+    whole FP32 gradient error.  So the fused path's adjoint, likelihood pass
+    and overlap-add add nothing of their own; the limit is FP32 FFT
+    convolution itself."""
     c = deriv_case
-    plan = make_plan(c["inst"], F32)
+    inst = c["inst"]
+    E, nx = inst.n_energies, inst.shape[0]
+    R = O.Response(O.Domain((E, nx, nx), (1.0, 1.0, 1.0)), inst.psf, inst.n_patches,
+                   inst.margin, inst.exposure, inst.readmask)
+    plan = make_plan(inst, F32)
     try:
         plan.set_data(c["data"])
-        _, g = plan.energy_and_grad(c["inst"].sky)
-        m = plan.metric(c["inst"].sky, c["t"])
+        _, g = plan.energy_and_grad(inst.sky)
+        m = plan.metric(inst.sky, c["t"])
+        lam32 = plan.response(inst.sky).double().cpu().numpy()
         eg, em = rel(g, c["grad"]), rel(m, c["metric"])
-        print(f"FP32 gradient {eg:.3e} (floor {c['floor_grad']:.3e}), "
-              f"metric {em:.3e} (floor {c['floor_metric']:.3e})")
-        assert eg <= 10 * c["floor_grad"] + 1e-6
-        assert em <= 10 * c["floor_metric"] + 1e-6
+        e_lam = rel(R.adjoint([1.0 - c["data"] / lam32]), c["grad"])
+        m_lam = rel(R.adjoint([c["jvp"] / lam32]), c["metric"])
+        print(f"FP32 gradient {eg:.3e}: from the FP32 lam alone {e_lam:.3e}, lam rounding "
+              f"floor {c['floor_grad']:.3e}; metric {em:.3e}: from the FP32 lam alone "
+              f"{m_lam:.3e}, floor {c['floor_metric']:.3e}")
+        assert abs(eg - e_lam) <= 0.1 * e_lam + 1e-6
+        assert em <= m_lam + 1e-6
     finally:
         plan.close()
