@@ -55,9 +55,12 @@ def parse():
                     help="skip the FP64 comparison and the CPU baseline")
     ap.add_argument("--profile-only", action="store_true",
                     help="one warm-up and two steps (for a launch list under a profiler)")
-    ap.add_argument("--leg", choices=["step", "sky", "batch"], default="step",
+    ap.add_argument("--leg", choices=["step", "sky", "batch", "fp64", "psf", "sampling"],
+                    default="step",
                     help="with --profile-only: the response step, the correlated-field sky "
-                         "(log-sky and VJP), or the grouped uneven batch")
+                         "(log-sky and VJP), the grouped uneven batch, the FP64 unfused step, "
+                         "the PSF-patch interpolation, or the sampling kernels (FP64 dot "
+                         "products, Poisson draws)")
     return ap.parse_args()
 
 
@@ -365,6 +368,57 @@ def profile_batch_leg(dev, passes=3):
     b.close()
 
 
+def profile_fp64_leg(dev, inst, data, passes=2):
+    """The FP64 unfused energy + gradient step on the workload, ``passes`` times."""
+    import torch
+
+    import jubik_gb300 as ju
+    M, E = inst.n_modules, inst.n_energies
+    plan = ju.ResponsePlan(M, E, inst.shape, inst.n_patches, inst.margin, dtype=torch.float64,
+                           path="plain", device=dev)
+    plan.set_psf(inst.psf.astype(np.float64))
+    plan.set_exposure(inst.exposure.astype(np.float64), inst.readmask)
+    plan.set_data(data)
+    x = torch.as_tensor(inst.sky, dtype=torch.float64, device=dev)
+    for _ in range(passes):
+        plan.energy_and_grad(x)
+    torch.cuda.synchronize()
+    plan.close()
+
+
+def profile_psf_leg(dev, nx, passes=2):
+    """PSF patches of one eROSITA-like module (16 x 16 patches, 3 energies, pre-cut
+    windows) interpolated from gridded PSFs, ``passes`` times."""
+    import torch
+
+    from jubik_gb300 import psf as jpsf
+    from jubik_gb300 import synthetic
+    infos = synthetic.erosita_like_psf_infos(n_energies=3, field=(nx, nx), grid=128, seed=1)
+    dom = ju_domain((3, nx, nx), (1.0, 1.0, 1.0))
+    for _ in range(passes):
+        jpsf.psf_interpolator(dom, nx // 64, infos, layout="precut", dtype=torch.float64)
+    torch.cuda.synchronize()
+
+
+def ju_domain(shape, distances):
+    import jubik_gb300 as ju
+    return ju.Domain(shape, distances)
+
+
+def profile_sampling_leg(dev, lam, passes=2):
+    """The sampling kernels of the MGVI loop on workload-sized vectors: FP64 dot
+    products of FP32 vectors and Poisson draws of the expected counts."""
+    import torch
+
+    from jubik_gb300 import sampling
+    a = torch.randn(lam.numel(), device=dev)
+    b = torch.randn(lam.numel(), device=dev)
+    for i in range(passes):
+        sampling.dot(a, b)
+        sampling.random_poisson(lam, seed=7, offset=i)
+    torch.cuda.synchronize()
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -407,6 +461,12 @@ def main():
             profile_sky_leg(dev, nx, E)
         elif args.leg == "batch":
             profile_batch_leg(dev)
+        elif args.leg == "fp64":
+            profile_fp64_leg(dev, inst, data)
+        elif args.leg == "psf":
+            profile_psf_leg(dev, nx)
+        elif args.leg == "sampling":
+            profile_sampling_leg(dev, plan.response(x))
         else:
             step()
             step()

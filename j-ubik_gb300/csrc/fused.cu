@@ -1406,9 +1406,11 @@ constexpr int kRun = 4;
 constexpr int kRunCols = 96;  // TMEM columns of one pending block row (per lane)
 
 // Output stage of patch s (0 .. kRun - 1) of a run: chunk c is block row
-// i - 1 + c.  Thread (warp w, lane) owns row (32 (w % 4) + lane) / 2 of each
-// chunk, columns 96 ((32 (w % 4) + lane) % 2) + 32 (w / 4) .. + 32, and the same
-// positions of the two pending block rows in its TMEM lane (slot = block row % 2).
+// i - 1 + c.  Thread (warp w, lane) owns, in every chunk, the warp tiles of
+// the overlap-add (8 pair rows x 16 columns; the tile row tau = 0..3 gives pair
+// rows 8 tau + lane / 4, columns 16 w + 4 (lane % 4) .. + 4): 32 values, kept for
+// the pending block rows in its TMEM lane 32 (w % 4) + lane, columns
+// 96 slot + 32 (w / 4) .. + 32 (slot = block row % 2).
 template <typename T, int P>
 __device__ __forceinline__ void stage_output_run(Unit<T, P>& U, const Args& a,
                                                  const Split2<T>& sp, uint32_t tbase, int s) {
@@ -1416,15 +1418,15 @@ __device__ __forceinline__ void stage_output_run(Unit<T, P>& U, const Args& a,
   using R = Tr<T, P>;
   constexpr int L1 = R::L1, TP = R::TP, CH = R::CH;
   const T scale = (T)a.scale;
-  const int lane128 = 32 * (U.warp & 3) + U.lane, gcol = U.warp >> 2;
-  const int rr = lane128 >> 1, x0 = (lane128 & 1) * 96 + gcol * 32;
-  const uint32_t tl = tbase + ((uint32_t)(32 * (U.warp & 3)) << 16) + (uint32_t)(gcol * 32);
+  const uint32_t tl = tbase + ((uint32_t)(32 * (U.warp & 3)) << 16) +
+                      (uint32_t)((U.warp >> 2) * 32);
   const int64_t plane = ((int64_t)U.m * a.E + U.e) * U.npix;
   T* __restrict__ dst = (T*)a.out + plane;
   T* __restrict__ dlo = (T*)a.out_lo + plane;
-  const int col = U.cb + x0;  // a multiple of 32: the group lies wholly in or out of the field
-  const bool col_in = col >= 0 && col + 32 <= a.ny;
-  const int i = U.k % a.n;    // patch row
+  const int x = 16 * U.warp + 4 * (U.lane & 3);
+  const int col = U.cb + x;  // a multiple of 4: the group lies wholly in or out of the field
+  const bool col_in = col >= 0 && col + 4 <= a.ny;
+  const int i = U.k % a.n;  // patch row
   for (int c = 0; c < 3; ++c) {
     const int j0 = c * CH;
     cx<T>* stg = (c & 1) ? U.tile + (j0 - CH) * TP : U.stg;
@@ -1439,14 +1441,16 @@ __device__ __forceinline__ void stage_output_run(Unit<T, P>& U, const Args& a,
       for (int q = 0; q < 16; ++q) stg[jj * TP + U.cls + L1 * q] = v[q];
     }
     __syncthreads();
-    const cx<T>* sr = stg + (rr >> 1) * TP + x0;
-    T v[32];
-    if (rr & 1) {
+    T v[32];  // tile row tau: v[8 tau .. + 4] row 2 jj, v[8 tau + 4 .. + 4] row 2 jj + 1
 #pragma unroll
-      for (int j = 0; j < 32; ++j) v[j] = scale * sr[j].y;
-    } else {
+    for (int tau = 0; tau < 4; ++tau) {
+      const cx<T>* sq = stg + (8 * tau + (U.lane >> 2)) * TP + x;
 #pragma unroll
-      for (int j = 0; j < 32; ++j) v[j] = scale * sr[j].x;
+      for (int t = 0; t < 4; ++t) {
+        const cx<T> z = sq[t];
+        v[8 * tau + t] = scale * z.x;
+        v[8 * tau + 4 + t] = scale * z.y;
+      }
     }
     const int br = i - 1 + c;  // block row of the field
     const uint32_t ta = tl + (uint32_t)(((br + 2) & 1) * kRunCols);
@@ -1459,14 +1463,19 @@ __device__ __forceinline__ void stage_output_run(Unit<T, P>& U, const Args& a,
       for (int j = 0; j < 32; ++j) v[j] += __uint_as_float(r[j]);
     }
     if (c == 0 || s == kRun - 1) {
-      const int row = U.rb + 2 * j0 + rr;
-      if (col_in && row >= 0 && row < a.nx) {
-        const int64_t o = (int64_t)row * a.ny + col;
+      if (col_in) {
 #pragma unroll
-        for (int g = 0; g < 8; ++g)
-          acc4<true>((float*)(dst + o + 4 * g), (float*)(dlo + o + 4 * g),
-                     (const Split2<float>&)sp, v[4 * g], v[4 * g + 1], v[4 * g + 2],
-                     v[4 * g + 3]);
+        for (int tau = 0; tau < 4; ++tau) {
+          const int row = U.rb + 2 * (j0 + 8 * tau + (U.lane >> 2));
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            if (row + h < 0 || row + h >= a.nx) continue;
+            const int64_t o = (int64_t)(row + h) * a.ny + col;
+            const int q = 8 * tau + 4 * h;
+            acc4<true>((float*)(dst + o), (float*)(dlo + o), (const Split2<float>&)sp, v[q],
+                       v[q + 1], v[q + 2], v[q + 3]);
+          }
+        }
       }
     } else {
       uint32_t r[32];

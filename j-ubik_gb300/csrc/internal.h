@@ -211,7 +211,7 @@ int poisson_image(const void* conv, const void* conv_lo, const void* eps, const 
 // Largest magnitude of an (E, rows, cols) array with plane stride ps and row
 // stride rs (of exp(value) when exp_of), as nb <= kMaxBoundBlocks maxima
 // (bits of non-negative doubles) at out; returns nb.
-constexpr int kMaxBoundBlocks = 256;
+constexpr int kMaxBoundBlocks = 1024;
 template <typename T>
 int absmax_blocks(const void* in, int E, int rows, int cols, int64_t ps, int64_t rs, bool exp_of,
                   void* out, int* nb, bool pdl, cudaStream_t s);

@@ -1090,14 +1090,33 @@ __global__ void __launch_bounds__(kBlock)
   // the largest value (exp_of: exp is increasing, applied once at the end) or magnitude
   T m = exp_of ? (T)-INFINITY : (T)0;
   bool nan = false;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t e = i / ((int64_t)rows * cols), rc = i - e * rows * cols;
-    const int64_t r = rc / cols, c = rc - r * cols;
-    const T v = in[e * ps + r * rs + c];
+  auto take = [&](T v) {
     const T a = exp_of ? v : (v < (T)0 ? -v : v);
     nan |= (a != a);
     m = a > m ? a : m;
+  };
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  if (sizeof(T) == 4 && rs == cols && ps == (int64_t)rows * cols &&
+      (reinterpret_cast<uintptr_t>(in) & 15) == 0) {
+    // a contiguous array: 16-byte loads
+    const int64_t n4 = n / 4;
+    const float4* in4 = reinterpret_cast<const float4*>(in);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n4; i += stride) {
+      const float4 q = __ldcs(in4 + i);
+      take((T)q.x);
+      take((T)q.y);
+      take((T)q.z);
+      take((T)q.w);
+    }
+    for (int64_t i = n4 * 4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += stride)
+      take(in[i]);
+  } else {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+      const int64_t e = i / ((int64_t)rows * cols), rc = i - e * rows * cols;
+      const int64_t r = rc / cols, c = rc - r * cols;
+      take(in[e * ps + r * rs + c]);
+    }
   }
   __shared__ unsigned long long red[kBlock / 32];
   const double md = exp_of ? exp((double)m) : (double)m;  // exp(-inf) = 0 for an empty share
