@@ -568,11 +568,16 @@ def main():
     fft_unit = 5.0 * P * P * np.log2(P)      # one real 2-D FFT of side P (5 N log2 N / 2)
     mul_unit = 6.0 * P * (P // 2)
     shared = plan.shared_spectra
+    # whole 64-row block rows per patch output (P 192, stride 64, margin 32, runs of
+    # 4 patch rows, 2+ modules): the forward runs the run-ordered kernel
+    run = (P == 192 and inst.dx == 64 and inst.margin == 32 and nx == inst.n_patches * 64
+           and inst.n_patches % 4 == 0 and M >= 2)
+    fwd_kernel = "k_fwd_run<float,192>" if run else "k_fwd_from_spec<float,192>"
     kinfo = {  # phase -> (kernel, bytes, flops)
-        "forward": ("k_fwd_from_spec<float,192>" if shared else "k_fused<float,192,fwd>",
+        "forward": (fwd_kernel if shared else "k_fused<float,192,fwd>",
                     spec + (pspec if shared else sky) + img,
                     U * (fft_unit * (1 if shared else 2) + mul_unit)),
-        "adjoint": ("k_adj_to_spec<float,192>" if shared else "k_fused<float,192,adj>",
+        "adjoint": ("k_adj_to_spec_ord<float,192>" if shared else "k_fused<float,192,adj>",
                     spec + img + (pspec if shared else sky),
                     U * (fft_unit * (1 if shared else 2) + mul_unit)),
         "forward_patch": ("k_sky_spec<float,192>", sky + pspec, NP * fft_unit),

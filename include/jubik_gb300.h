@@ -212,7 +212,8 @@ JUBIK_API int jubik_convolve2d(const void* kernel, int64_t bk, const void* signa
  * npatch patches per axis.  layout JUBIK_PSF_FULL: out (npatch^2, E, nx, ny),
  * the reference's rolled full-field array; JUBIK_PSF_PRECUT: out (npatch^2,
  * E, 2 nx/npatch, 2 ny/npatch), the windows jubik_plan_set_psf takes, without
- * forming the full field.  out in `dtype`; arithmetic in FP64. */
+ * forming the full field.  out in `dtype`; arithmetic in FP64.  At most 2048
+ * radii (JUBIK_ERR_INVALID_ARGUMENT beyond). */
 JUBIK_API int jubik_psf_interpolate(const double* psfs, const double* rs,
                                     const double* center_ids, const double* deltas,
                                     const double* pointing, int32_t n_energies, int32_t n_radii,
@@ -293,9 +294,11 @@ JUBIK_API int jubik_random_normal(void* out, int64_t n, int32_t dtype, uint64_t 
  * (jax.random.poisson of each module's masked expected counts). */
 JUBIK_API int jubik_random_poisson(const void* lam, int64_t n, int32_t dtype, uint64_t seed,
                                    uint32_t offset, int32_t* out, void* stream);
-/* out (device double[1]) = sum_i a[i] b[i], accumulated in FP64 in a fixed
- * order (deterministic): the global dot products of the conjugate-gradient
- * solve of an MGVI linear sample.  n = 0 writes 0 (a, b may then be NULL). */
+/* out (device double[1]) = sum_i a[i] b[i] in a fixed order (deterministic): the
+ * global dot products of the conjugate-gradient solve of an MGVI linear sample.
+ * FP64 operands accumulate in FP64; FP32 operands as exact FP32 product splits
+ * in compensated FP32 sums (about 48 bits) flushed into FP64 every 128 elements.
+ * n = 0 writes 0 (a, b may then be NULL). */
 JUBIK_API int jubik_dot(const void* a, const void* b, int64_t n, int32_t dtype, double* out,
                         void* stream);
 

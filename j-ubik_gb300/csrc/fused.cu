@@ -182,19 +182,32 @@ __device__ __forceinline__ void red_add_cx(double2* p, double2 v) {
 template <typename T>
 struct Split2 {
   T m1, m2;
+  // The grid constants from the bits of the bound, in integer arithmetic (the
+  // FP64 pipe of this GPU is narrow, and every thread runs this).
   __device__ __forceinline__ void init(double bound, int L) {
     constexpr int D = sizeof(T) == 4 ? 24 : 53;
     constexpr int EMIN = sizeof(T) == 4 ? -75 : -900, EMAX = sizeof(T) == 4 ? 120 : 1000;
-    if (!(bound <= 1.0e308)) {  // a NaN or infinite input: every result becomes NaN
+    const unsigned long long b = (unsigned long long)__double_as_longlong(bound);
+    const int be = (int)((b >> 52) & 0x7ff);
+    if (be == 0x7ff || (b >> 63)) {  // a NaN, infinite or negative bound: results become NaN
       m1 = m2 = (T)NAN;
       return;
     }
-    int e = 0;
-    frexp(bound, &e);  // bound < 2^e
+    // bound < 2^e: e = unbiased exponent + 1 (a zero or subnormal bound takes EMIN)
+    int e = be == 0 ? EMIN : be - 1023 + 1;
     e = e < EMIN ? EMIN : (e > EMAX ? EMAX : e);
     const int q1 = e - (D - 2), q2 = q1 + L + 1 - D;
-    m1 = (T)ldexp(1.5, q1 + D - 1);
-    m2 = (T)ldexp(1.5, q2 + D - 1);
+    m1 = pow2_times_1_5(q1 + D - 1);
+    m2 = pow2_times_1_5(q2 + D - 1);
+  }
+  // 1.5 * 2^k as T, built from its bits (k within T's normal range here)
+  __device__ __forceinline__ static T pow2_times_1_5(int k) {
+    if constexpr (sizeof(T) == 4) {
+      return __uint_as_float(((unsigned)(k + 127) << 23) | 0x400000u);
+    } else {
+      return __longlong_as_double((long long)(((unsigned long long)(k + 1023) << 52) |
+                                              0x8000000000000ull));
+    }
   }
   __device__ __forceinline__ void split(T v, T& hi, T& lo) const {
     if constexpr (sizeof(T) == 4) {

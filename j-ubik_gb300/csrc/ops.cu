@@ -1119,7 +1119,7 @@ __global__ void __launch_bounds__(kBlock)
     }
   }
   __shared__ unsigned long long red[kBlock / 32];
-  const double md = exp_of ? exp((double)m) : (double)m;  // exp(-inf) = 0 for an empty share
+  const double md = (double)(exp_of ? exp(m) : m);  // in T: exp(-inf) = 0 for an empty share
   unsigned long long b = nan ? 0x7ff8000000000000ull : (unsigned long long)__double_as_longlong(md);
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long t = __shfl_xor_sync(0xffffffffu, b, o);

@@ -16,7 +16,17 @@
 // evaluates that window directly -- window pixel a sits at offset a - dx --
 // so the full-field array (n^2 E N0 N1 values, 45 GB in float64 for seven
 // modules at 1024^2) is never formed.  Layout FULL writes the reference's
-// array.  One thread per output pixel, all arithmetic in FP64.
+// array.  All arithmetic in FP64.
+//
+// A block row (blockIdx.y) takes one (patch, energy) item at a time: the
+// patch's radial weights and its rotation (cos, sin of the angle phi) are
+// computed once per item, and each pixel offset (dra, ddec) is rotated by
+// phi directly -- x = dra cos phi + ddec sin phi, y = ddec cos phi - dra sin phi,
+// the same point as the reference's ri cos(th - phi), ri sin(th - phi) with
+// th = atan2(ddec, dra), to rounding -- so no trigonometric function runs per
+// pixel (on this GPU the FP64 pipe is narrow).  Likewise the grid coordinate
+// (x + c d) / d is formed as x (1 / d) + c, and only the radii with a nonzero
+// weight (at most two for ascending radii) are visited, in ascending order.
 #include <cmath>
 #include <cstdio>
 
@@ -53,53 +63,80 @@ __device__ double bilinear_nearest(const double* img, int h, int w, double q0, d
          t0 * t1 * img[(int64_t)b0 * w + b1];
 }
 
+constexpr int kMaxRadii = 2048;  // radial weights and nonzero list of one item in shared memory
+
 template <typename T>
-__global__ void k_psf_interp(InterpArgs a, T* __restrict__ out) {
+__global__ void __launch_bounds__(kThreads) k_psf_interp(InterpArgs a, T* __restrict__ out) {
+  extern __shared__ double s_w[];  // radial weight of each gridded PSF for this item
+  __shared__ double s_rot[2];      // cos phi, sin phi
+  __shared__ int s_nz;             // radii with a nonzero weight, listed in s_j
+  int* s_j = reinterpret_cast<int*>(s_w + a.R);
   const int64_t per = (int64_t)a.out0 * a.out1;
-  const int64_t total = (int64_t)a.npatch * a.npatch * a.E * per;
-  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t pix = idx % per;
-    const int64_t ke = idx / per;
+  const int64_t nke = (int64_t)a.npatch * a.npatch * a.E;
+  const int ps0i = a.n0 / a.npatch, ps1i = a.n1 / a.npatch;
+  for (int64_t ke = blockIdx.y; ke < nke; ke += gridDim.y) {
     const int e = (int)(ke % a.E);
     const int k = (int)(ke / a.E);
-    const int i0 = (int)(pix / a.out1), i1 = (int)(pix % a.out1);
     // patch centre: dec along k % n, ra reversed along k / n
-    const double ps0 = (double)(a.n0 / a.npatch), ps1 = (double)(a.n1 / a.npatch);
+    const double ps0 = (double)ps0i, ps1 = (double)ps1i;
     const double c_dec = ((double)(k % a.npatch) * ps0 + ps0 / 2.0) * a.dist0;
     const double c_ra = ((double)(a.npatch - 1 - k / a.npatch) * ps1 + ps1 / 2.0) * a.dist1;
     const double cc0 = c_ra - a.pointing[2 * e], cc1 = c_dec - a.pointing[2 * e + 1];
     const double r = sqrt(cc0 * cc0 + cc1 * cc1);
-    const double phi = atan2(cc1, cc0) - kHalfPi;
-    // pixel offset (dec, -ra) of this output pixel
-    double g0, g1;
-    if (a.layout == JUBIK_PSF_PRECUT) {
-      g0 = (double)(i0 - a.n0 / a.npatch) * a.dist0;
-      g1 = (double)(i1 - a.n1 / a.npatch) * a.dist1;
-    } else {  // rolled by half the field
-      g0 = ((double)((i0 + a.n0 / 2) % a.n0) - (double)a.n0 / 2.0) * a.dist0;
-      g1 = ((double)((i1 + a.n1 / 2) % a.n1) - (double)a.n1 / 2.0) * a.dist1;
-    }
-    const double ddec = g0, dra = -1.0 * g1;
-    const double ri = sqrt(dra * dra + ddec * ddec);
-    const double ph = (atan2(ddec, dra) - kHalfPi) - phi;
-    const double x = ri * cos(ph + kHalfPi), y = ri * sin(ph + kHalfPi);
     const double* rs = a.rs + (int64_t)e * a.R;
-    const double d0 = a.deltas[2 * e], d1 = a.deltas[2 * e + 1];
-    double acc = 0.0;
-    for (int j = 0; j < a.R; ++j) {
+    __syncthreads();  // the previous item's pixels no longer read s_w, s_rot
+    if (threadIdx.x == 0) {
+      const double phi = atan2(cc1, cc0) - kHalfPi;
+      s_rot[0] = cos(phi);
+      s_rot[1] = sin(phi);
+    }
+    for (int j = threadIdx.x; j < a.R; j += blockDim.x) {
       // radial weight of PSF j (the clamp and the interval both count at r == rs[R-1])
       double wj = 0.0;
       if (j == 0 && r <= rs[0]) wj += 1.0;
       if (j == a.R - 1 && r >= rs[a.R - 1]) wj += 1.0;
       if (j + 1 < a.R && rs[j] < r && r <= rs[j + 1]) wj += 1.0 - (r - rs[j]) / (rs[j + 1] - rs[j]);
       if (j > 0 && rs[j - 1] < r && r <= rs[j]) wj += (r - rs[j - 1]) / (rs[j] - rs[j - 1]);
-      if (wj == 0.0) continue;
-      const double* cid = a.cids + ((int64_t)e * a.R + j) * 2;
-      const double q0 = (x + cid[0] * d0) / d0, q1 = (y + cid[1] * d1) / d1;
-      acc += wj * bilinear_nearest(a.psfs + ((int64_t)e * a.R + j) * a.h * a.w, a.h, a.w, q0, q1);
+      s_w[j] = wj;
     }
-    out[idx] = (T)acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {  // the nonzero weights in ascending j (the order of the sum)
+      int nz = 0;
+      for (int j = 0; j < a.R; ++j)
+        if (s_w[j] != 0.0) s_j[nz++] = j;
+      s_nz = nz;
+    }
+    __syncthreads();
+    const double cph = s_rot[0], sph = s_rot[1];
+    const int nz = s_nz;
+    const double d0 = a.deltas[2 * e], d1 = a.deltas[2 * e + 1];
+    const double inv0 = 1.0 / d0, inv1 = 1.0 / d1;
+    T* __restrict__ dst = out + ke * per;
+    for (int64_t pix = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; pix < per;
+         pix += (int64_t)gridDim.x * blockDim.x) {
+      const int i0 = (int)(pix / a.out1), i1 = (int)(pix - (int64_t)i0 * a.out1);
+      // pixel offset (dec, -ra) of this output pixel
+      double g0, g1;
+      if (a.layout == JUBIK_PSF_PRECUT) {
+        g0 = (double)(i0 - ps0i) * a.dist0;
+        g1 = (double)(i1 - ps1i) * a.dist1;
+      } else {  // rolled by half the field
+        g0 = ((double)((i0 + a.n0 / 2) % a.n0) - (double)a.n0 / 2.0) * a.dist0;
+        g1 = ((double)((i1 + a.n1 / 2) % a.n1) - (double)a.n1 / 2.0) * a.dist1;
+      }
+      const double ddec = g0, dra = -1.0 * g1;
+      const double x = dra * cph + ddec * sph, y = ddec * cph - dra * sph;
+      double acc = 0.0;
+      for (int t = 0; t < nz; ++t) {
+        const int j = s_j[t];
+        const double wj = s_w[j];
+        const double* cid = a.cids + ((int64_t)e * a.R + j) * 2;
+        const double q0 = fma(x, inv0, cid[0]), q1 = fma(y, inv1, cid[1]);
+        acc += wj * bilinear_nearest(a.psfs + ((int64_t)e * a.R + j) * a.h * a.w, a.h, a.w, q0,
+                                     q1);
+      }
+      dst[pix] = (T)acc;
+    }
   }
 }
 
@@ -144,14 +181,23 @@ int jubik_psf_interpolate(const double* psfs, const double* rs, const double* ce
   a.out1 = layout == JUBIK_PSF_PRECUT ? 2 * (ny / npatch) : ny;
   a.dist0 = dist_x;
   a.dist1 = dist_y;
-  const int64_t total = (int64_t)npatch * npatch * n_energies * a.out0 * a.out1;
-  int64_t blocks = (total + kThreads - 1) / kThreads;
-  if (blocks > 1048576) blocks = 1048576;
+  if (n_radii > kMaxRadii) {
+    set_error("psf_interpolate: at most %d radii", kMaxRadii);
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  // x: pixels of one (patch, energy) item; y: the items (looped beyond 65535)
+  const int64_t per = (int64_t)a.out0 * a.out1;
+  const int64_t nke = (int64_t)npatch * npatch * n_energies;
+  int64_t gx = (per + kThreads - 1) / kThreads;
+  if (gx > 1024) gx = 1024;
+  const int64_t gy = nke < 65535 ? nke : 65535;
+  const dim3 grid((unsigned)gx, (unsigned)gy);
+  const size_t smem = (size_t)n_radii * (sizeof(double) + sizeof(int));
   cudaStream_t s = (cudaStream_t)stream;
   if (dtype == JUBIK_F32)
-    k_psf_interp<float><<<(unsigned)blocks, kThreads, 0, s>>>(a, (float*)out);
+    k_psf_interp<float><<<grid, kThreads, smem, s>>>(a, (float*)out);
   else
-    k_psf_interp<double><<<(unsigned)blocks, kThreads, 0, s>>>(a, (double*)out);
+    k_psf_interp<double><<<grid, kThreads, smem, s>>>(a, (double*)out);
   return cuda_status(cudaGetLastError(), "k_psf_interp");
 }
 

@@ -151,15 +151,104 @@ __global__ void k_poisson_sample(const T* __restrict__ lam, int64_t n, uint2 key
     out[i] = poisson_one((double)lam[i], (uint64_t)i, off, key);
 }
 
-// ------------------------------------------------------------------ FP64 dot
+// ------------------------------------------------------------------ dot
+// Sum of a[i] b[i] into FP64 in a fixed order.  FP64 operands: one FP64 fma
+// each.  FP32 operands: the FP64 pipe of this GPU is far too narrow to convert
+// and fma every element at HBM speed, so each thread sums its products on the
+// FP32 pipe with the compensated dot product "Dot2" of Ogita, Rump & Oishi
+// (SIAM J. Sci. Comput. 26, 2005): the product split exactly into p + e
+// (p = fl(x y), e = fma(x, y, -p)), p added with Knuth's TwoSum, the two error
+// terms gathered in a second word.  Every kDotFlush elements the two words go
+// into the thread's FP64 total.  A group whose words are not finite (an inf or
+// NaN operand or an overflow), or whose products are all tiny while some pair
+// of operands is nonzero (an underflowed product, or an error term below about
+// 2^-102 that is not exact), is summed again in FP64.
+constexpr int kDotFlush = 32;  // float4 chunks (128 elements) per FP64 flush
+
+struct Dot2 {
+  float s = 0.0f, c = 0.0f;  // sum and the gathered error terms
+  float pmax = 0.0f;         // largest |fl(x y)|
+  float zmax = 0.0f;         // largest min(|x|, |y|): positive when some pair is nonzero
+  __device__ __forceinline__ void add(float x, float y);
+  // the two words hold the group's sum to about 2^-48 of its terms
+  __device__ __forceinline__ bool exact() const {
+    return isfinite(s) && isfinite(c) && (pmax >= 0x1p-60f || zmax == 0.0f);
+  }
+};
+
+__device__ __forceinline__ void Dot2::add(float x, float y) {
+  const float p = __fmul_rn(x, y);  // no contraction into the sum below
+  const float e = fmaf(x, y, -p);
+  const float t = __fadd_rn(s, p);
+  const float bp = __fsub_rn(t, s);
+  const float sg = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+  s = t;
+  c = __fadd_rn(c, __fadd_rn(e, sg));
+  pmax = fmaxf(pmax, fabsf(p));
+  zmax = fmaxf(zmax, fminf(fabsf(x), fabsf(y)));
+}
+
+__device__ __forceinline__ double dot_f32_share(const float* __restrict__ a,
+                                                const float* __restrict__ b, int64_t n) {
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const bool vec = ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) & 15) == 0;
+  double acc = 0.0;
+  int64_t nv = 0;  // elements covered by float4 chunks
+  if (vec) {
+    const float4* a4 = reinterpret_cast<const float4*>(a);
+    const float4* b4 = reinterpret_cast<const float4*>(b);
+    const int64_t n4 = n >> 2;
+    nv = n4 << 2;
+    for (int64_t j0 = tid; j0 < n4; j0 += stride * kDotFlush) {
+      Dot2 d;
+      int64_t j = j0;
+      for (int g = 0; g < kDotFlush && j < n4; ++g, j += stride) {
+        const float4 x = __ldcs(a4 + j), y = __ldcs(b4 + j);
+        d.add(x.x, y.x);
+        d.add(x.y, y.y);
+        d.add(x.z, y.z);
+        d.add(x.w, y.w);
+      }
+      if (d.exact()) {
+        acc += (double)d.s;
+        acc += (double)d.c;
+      } else {  // the same chunks again in FP64
+        j = j0;
+        for (int g = 0; g < kDotFlush && j < n4; ++g, j += stride)
+          for (int q = 0; q < 4; ++q) acc = fma((double)a[4 * j + q], (double)b[4 * j + q], acc);
+      }
+    }
+  }
+  // the rest (everything when the operands are not 16-byte aligned), element-wise
+  for (int64_t i0 = nv + tid; i0 < n; i0 += stride * (4 * kDotFlush)) {
+    Dot2 d;
+    int64_t i = i0;
+    for (int g = 0; g < 4 * kDotFlush && i < n; ++g, i += stride) d.add(a[i], b[i]);
+    if (d.exact()) {
+      acc += (double)d.s;
+      acc += (double)d.c;
+    } else {
+      i = i0;
+      for (int g = 0; g < 4 * kDotFlush && i < n; ++g, i += stride)
+        acc = fma((double)a[i], (double)b[i], acc);
+    }
+  }
+  return acc;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
     k_dot(const T* __restrict__ a, const T* __restrict__ b, int64_t n, double* partials,
           unsigned int* counter, double* out) {
   double acc = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    acc = fma((double)a[i], (double)b[i], acc);
+  if constexpr (sizeof(T) == 4) {
+    acc = dot_f32_share(a, b, n);
+  } else {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+      acc = fma(a[i], b[i], acc);
+  }
   __shared__ double red[kThreads];
   __shared__ bool last;
   red[threadIdx.x] = acc;

@@ -58,7 +58,8 @@ def random_poisson(lam, seed: int = 0, offset: int = 0,
 
 
 def dot(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
-    """sum(a * b) as a float64 0-d device tensor (deterministic FP64 sum)."""
+    """sum(a * b) as a float64 0-d device tensor, summed in a fixed order
+    (float32 operands: compensated FP32 partial sums flushed into FP64)."""
     if a.shape != b.shape or a.dtype != b.dtype:
         raise ValueError("dot needs two tensors of the same shape and dtype")
     dev = a.device

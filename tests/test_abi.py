@@ -107,3 +107,23 @@ def test_convolve2d_argument_errors_without_a_gpu():
     assert lib.jubik_convolve2d_noalloc(dummy, huge, dummy, huge, 64, 64, 1.0, _lib.F64, dummy,
                                         None) == _lib.ERR_INVALID_ARGUMENT
     assert "exceed" in _lib.last_error()
+
+
+@pytest.mark.skipif(not _built(), reason="library not built")
+def test_psf_interpolate_argument_errors_without_a_gpu():
+    """The PSF interpolator rejects bad layouts, fields and too many radii before any
+    CUDA call."""
+    lib = _lib.load()
+    d = out = ctypes.c_void_p(16)  # never dereferenced: the checks run first
+    fn = lib.jubik_psf_interpolate
+    ok = dict(E=1, R=3, h=16, w=16, nx=64, ny=64, npatch=4, layout=0, dtype=_lib.F64)
+
+    def call(**kw):
+        k = dict(ok, **kw)
+        return fn(d, d, d, d, d, k["E"], k["R"], k["h"], k["w"], k["nx"], k["ny"],
+                  1.0, 1.0, k["npatch"], k["layout"], k["dtype"], out, None)
+
+    assert call(layout=7) == _lib.ERR_INVALID_ARGUMENT
+    assert call(nx=62) == _lib.ERR_INVALID_ARGUMENT
+    assert call(R=2049) == _lib.ERR_INVALID_ARGUMENT
+    assert "radii" in _lib.last_error()

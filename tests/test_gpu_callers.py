@@ -1,6 +1,8 @@
 """GPU callers around the response: samplers against their element-by-element
 oracle, the FP64 dot, mock data, noise-weighted residuals and the MGVI
 linear-sample CG solve."""
+import math
+
 import numpy as np
 import pytest
 import torch
@@ -73,6 +75,46 @@ def test_dot_fp64_deterministic(cuda, dtype):
     assert d1 == d2
     assert abs(d1 - ref) <= 1e-13 * np.sqrt(a.size)
     assert float(sampling.dot(ta[:0], tb[:0])) == 0.0
+
+
+def _fsum_dot(a, b):
+    return math.fsum((np.asarray(a, np.float64) * np.asarray(b, np.float64)).tolist())
+
+
+def test_dot_fp32_compensated_sums(cuda):
+    """FP32 operands: exact product splits in compensated FP32 sums; groups with a
+    non-finite word, or whose products all underflow, are summed again in FP64."""
+    rng = np.random.default_rng(3)
+    n = 20_000_003
+    a = rng.normal(size=n).astype(np.float32)
+    b = rng.normal(size=n).astype(np.float32)
+    ta, tb = torch.from_numpy(a).to(cuda), torch.from_numpy(b).to(cuda)
+    ref = _fsum_dot(a, b)
+    assert abs(float(sampling.dot(ta, tb)) - ref) <= 1e-13 * np.sqrt(n)
+    # unaligned views take the element-wise loop
+    ref1 = _fsum_dot(a[1:], b[1:])
+    assert abs(float(sampling.dot(ta[1:], tb[1:])) - ref1) <= 1e-13 * np.sqrt(n)
+    # heavy cancellation: the error scales with the terms, not the result
+    c = np.concatenate([a[:1000], -a[:1000]])
+    d = np.concatenate([b[:1000], b[:1000]])
+    got = float(sampling.dot(torch.from_numpy(c).to(cuda), torch.from_numpy(d).to(cuda)))
+    assert abs(got) <= 1e-15 * float(np.abs(c.astype(np.float64) * d).sum())
+    # products below the FP32 range (1e-25 * 1e-25) go through the FP64 path
+    t = np.full(4096, 1e-25, np.float32)
+    got = float(sampling.dot(torch.from_numpy(t).to(cuda), torch.from_numpy(t).to(cuda)))
+    assert got == pytest.approx(_fsum_dot(t, t), rel=1e-12)
+    # an infinite or NaN operand
+    e = a[:5000].copy()
+    e[1234] = np.inf
+    te = torch.from_numpy(e).to(cuda)
+    tb5 = torch.from_numpy(np.abs(b[:5000]) + 1.0).to(cuda)
+    assert float(sampling.dot(te, tb5)) == np.inf
+    e[1234] = np.nan
+    assert np.isnan(float(sampling.dot(torch.from_numpy(e).to(cuda), tb5)))
+    # products beyond the FP32 range (1e30 * 1e30) are finite in FP64
+    big = np.full(1000, 1e30, np.float32)
+    tbig = torch.from_numpy(big).to(cuda)
+    assert float(sampling.dot(tbig, tbig)) == pytest.approx(_fsum_dot(big, big), rel=1e-12)
 
 
 @pytest.fixture(scope="module")
