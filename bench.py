@@ -282,6 +282,58 @@ def uneven_batch_leg(dev, n_streams=8, passes=10, modules=1, count=64):
         b.close()
 
 
+def erosita_demo_leg(dev, passes=20):
+    """The geometry of the reference's eROSITA demo (demos/configs/eROSITA_demo.yaml:
+    a 512^2 sky, telescope modules 1 and 2, 3 energy bins, 8 x 8 patches and margin
+    fraction 0.062, i.e. margin 32 and FFT side 192) on synthetic inputs:
+    energy + gradient steps with the library's forward run length, then with the
+    one ResponsePlan.autotune measures fastest."""
+    import torch
+
+    import jubik_gb300 as ju
+    from jubik_gb300 import synthetic
+
+    inst = synthetic.config2(nx=512, n_modules=2, n_energies=3, dtype=np.float32)
+    M, E, nx = inst.n_modules, inst.n_energies, inst.shape[0]
+    mpix = M * E * nx * nx / 1e6
+    plan = ju.ResponsePlan(M, E, inst.shape, inst.n_patches, inst.margin, dtype=torch.float32,
+                           device=dev)
+    try:
+        plan.set_psf(inst.psf)
+        plan.set_exposure(inst.exposure, inst.readmask)
+        x = torch.as_tensor(inst.sky, device=dev)
+        plan.set_data(synthetic.poisson_data(plan.response(x).double().cpu().numpy(), seed=1))
+        energy = torch.empty((), dtype=torch.float64, device=dev)
+        grad = torch.empty_like(x)
+        s = torch.cuda.current_stream(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+
+        def timed():
+            for _ in range(5):
+                plan.energy_and_grad(x, energy=energy, grad=grad)
+            torch.cuda.synchronize(dev)
+            e0.record(s)
+            for _ in range(passes):
+                plan.energy_and_grad(x, energy=energy, grad=grad)
+            e1.record(s)
+            torch.cuda.synchronize(dev)
+            return e0.elapsed_time(e1) / passes
+
+        auto_run = plan.forward_run
+        auto_ms = timed()
+        tuned = plan.autotune(x, reps=passes)
+        tuned_ms = timed()
+        return {"geometry": "512^2 x 2 modules x 3 energies, 8 x 8 patches, margin 32, P 192",
+                "mpix": mpix, "auto_run": auto_run, "auto_ms": auto_ms,
+                "auto_mpix_s": mpix / (auto_ms / 1e3),
+                "autotune_ms": {str(k): v for k, v in tuned.items()},
+                "tuned_run": plan.forward_run, "tuned_ms": tuned_ms,
+                "tuned_mpix_s": mpix / (tuned_ms / 1e3)}
+    finally:
+        plan.close()
+
+
 # ------------------------------------------------------------------ GPU leg
 def sky_model_leg(plan, dev, nx, E, mpix, reps=20):
     """The diffuse sky model in front of the response: two correlated fields
@@ -609,7 +661,7 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded GRF sky, Moffat PSFs, Poisson counts)",
-        "config": dict(workload(args.nx), path=plan.path,
+        "config": dict(workload(args.nx), path=plan.path, forward_run=plan.forward_run,
                        parallelism="replicas" if world > 1 else "1gpu"),
         "e2e": {"value": e2e_value, "unit": "Mpix/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
@@ -700,6 +752,7 @@ def main():
         line["uneven_batch"] = uneven_batch_leg(dev)
         # the same geometry with the 7 modules of an eROSITA field, 16 fields
         line["uneven_batch_7_modules"] = uneven_batch_leg(dev, modules=7, count=16)
+        line["erosita_demo"] = erosita_demo_leg(dev)
         line["sky_model"] = sky_model_leg(plan, dev, nx, E, mpix)
         line["rel_err_vs_fp64_gpu"] = err
         line["fp64_plain_ms_per_step"] = fp64_ms

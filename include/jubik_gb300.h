@@ -164,6 +164,17 @@ JUBIK_API int jubik_metric_apply(jubik_plan* plan, const void* x, const void* v,
  * branches of one CUDA graph) may switch it off, so that waiting kernels do
  * not hold SMs the other streams could use. */
 JUBIK_API int jubik_plan_set_dependent_launch(jubik_plan* plan, int32_t on);
+/* Schedule of the module-shared FP32 forward at FFT side 192 (no counterpart in
+ * the reference): a CTA takes runs of run_len vertically adjacent patches of
+ * one module and sums the field rows they share in tensor memory before they
+ * leave the CTA.  run_len 4 reduces fewest rows, 2 or 1 (one patch at a time)
+ * give more work items for small fields; 0 (the default) lets the library
+ * choose from the field size and the SM count.  Results agree to FP32 rounding
+ * across run lengths and are the same bits for a given one.  Returns
+ * JUBIK_ERR_UNSUPPORTED for runs the plan's geometry cannot take. */
+JUBIK_API int jubik_plan_set_forward_run(jubik_plan* plan, int32_t run_len);
+/* The run length the plan's forward uses (1 where it does not run in runs). */
+JUBIK_API int jubik_plan_forward_run(const jubik_plan* plan, int32_t* run_len);
 JUBIK_API int jubik_plan_set_profiling(jubik_plan* plan, int32_t on);
 /* ms and launch counts per phase accumulated since profiling was switched on. */
 JUBIK_API int jubik_plan_profile(const jubik_plan* plan, double* ms, int64_t* launches);

@@ -85,6 +85,8 @@ _SIGS = {
     "jubik_random_poisson": ([_vp, _i64, _i32, C.c_uint64, C.c_uint32, _vp, _vp], C.c_int),
     "jubik_dot": ([_vp, _vp, _i64, _i32, _vp, _vp], C.c_int),
     "jubik_plan_set_dependent_launch": ([_vp, _i32], C.c_int),
+    "jubik_plan_set_forward_run": ([_vp, _i32], C.c_int),
+    "jubik_plan_forward_run": ([_vp, _vp], C.c_int),
     "jubik_group_create": ([_vp, _i32, _vp], C.c_int),
     "jubik_group_set_io": ([_vp, _vp, _vp, _vp], C.c_int),
     "jubik_group_energy_grad": ([_vp, _vp], C.c_int),

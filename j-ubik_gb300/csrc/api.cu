@@ -238,6 +238,7 @@ struct jubik_plan {
   void* hfull = nullptr;
   void* spec = nullptr;  // per-(energy, patch) spectra shared by the modules
   bool pdl = true;       // programmatic dependent launch between the kernels of a call
+  int fwd_run = 0;       // module-shared forward: patches per run (0: the library's choice)
   void* acc = nullptr;   // per-(energy, patch) adjoint sums over modules (written whole by
                          // the ordered adjoint; grouped launches clear it before they add)
   // exact two-word accumulation (fused path): low-word planes of the images and
@@ -391,6 +392,7 @@ int do_forward(jubik_plan* p, const void* x, void* out, void* out_lo, double sca
   if (p->path == JUBIK_PATH_FUSED) {
     FusedLaunch a{x, out, p->hmain, p->hnyq, p->tw, p->wt, scale, p->spec};
     a.pdl = p->pdl;
+    a.fwd_run = p->fwd_run;
     a.in_ps = view.ps;
     a.in_rs = view.rs;
     a.in_exp = view.exp;
@@ -743,6 +745,33 @@ int jubik_plan_path(const jubik_plan* plan, int32_t* path) {
 int jubik_plan_set_dependent_launch(jubik_plan* p, int32_t on) {
   JUBIK_TRY(check_plan(p));
   p->pdl = on != 0;
+  return JUBIK_OK;
+}
+
+int jubik_plan_set_forward_run(jubik_plan* p, int32_t run_len) {
+  JUBIK_TRY(check_plan(p));
+  if (run_len != 0 && run_len != 1 && run_len != 2 && run_len != 4) {
+    set_error("set_forward_run: run length %d is not 0, 1, 2 or 4", run_len);
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  if (run_len > 1 && (p->path != JUBIK_PATH_FUSED || !p->spec ||
+                      fused_fwd_run_len(p->g, p->dtype, run_len) < 0)) {
+    set_error("set_forward_run: runs of %d patches need the module-shared FP32 kernels at FFT "
+              "side 192 with 64-pixel strides, a 32-pixel margin and %d | n", run_len, run_len);
+    return JUBIK_ERR_UNSUPPORTED;
+  }
+  p->fwd_run = run_len;
+  return JUBIK_OK;
+}
+
+int jubik_plan_forward_run(const jubik_plan* p, int32_t* run_len) {
+  JUBIK_TRY(check_plan(p));
+  if (!run_len) {
+    set_error("forward_run: null output");
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  *run_len = (p->path == JUBIK_PATH_FUSED && p->spec)
+                 ? fused_fwd_run_len(p->g, p->dtype, p->fwd_run) : 1;
   return JUBIK_OK;
 }
 

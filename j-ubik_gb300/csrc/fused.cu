@@ -87,6 +87,7 @@ struct Args {
   // the patch a CTA continues (one slot per CTA of the loop grid `loop_grid`)
   void* spill;
   int loop_grid;
+  int run_len;  // run-ordered forward: patches per run (2 or 4)
 };
 
 __device__ __forceinline__ float2 ldg2(const float2* p) { return __ldg(p); }
@@ -1409,16 +1410,17 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_from_spec(Src src, int uni
 // When P = 3 dx with dx = 64 and margin dx / 2, a patch's P x P output covers
 // exactly three block rows of dx field rows (i - 1, i, i + 1 for patch row i),
 // and the staging chunks of the output stage (32 pair rows) are those block
-// rows.  A CTA then takes runs of kRun vertically adjacent patches of one
-// module and adds the block rows they share in TMEM, in patch order, before
-// they leave the CTA: each block row of a run is reduced into the image once
-// (as an exact two-word sum), 6 block rows per run of 4 patches instead of 12.
-// The 7 modules of a run are consecutive work items, which neighbouring CTAs
-// run at the same time, so the shared sky spectra still meet in L2.
-constexpr int kRun = 4;
+// rows.  A CTA then takes runs of a.run_len (2 or 4) vertically adjacent
+// patches of one module and adds the block rows they share in TMEM, in patch
+// order, before they leave the CTA: each block row of a run is reduced into the
+// image once (as an exact two-word sum), 6 block rows per run of 4 patches
+// instead of 12.  The modules of a run are consecutive work items, which
+// neighbouring CTAs run at the same time, so the shared sky spectra still meet
+// in L2.  Longer runs mean fewer reductions but fewer work items: the run
+// length is a schedule choice (auto_run_len, or set per plan).
 constexpr int kRunCols = 96;  // TMEM columns of one pending block row (per lane)
 
-// Output stage of patch s (0 .. kRun - 1) of a run: chunk c is block row
+// Output stage of patch s (0 .. run_len - 1) of a run: chunk c is block row
 // i - 1 + c.  Thread (warp w, lane) owns, in every chunk, the warp tiles of
 // the overlap-add (8 pair rows x 16 columns; the tile row tau = 0..3 gives pair
 // rows 8 tau + lane / 4, columns 16 w + 4 (lane % 4) .. + 4): 32 values, kept for
@@ -1475,7 +1477,7 @@ __device__ __forceinline__ void stage_output_run(Unit<T, P>& U, const Args& a,
 #pragma unroll
       for (int j = 0; j < 32; ++j) v[j] += __uint_as_float(r[j]);
     }
-    if (c == 0 || s == kRun - 1) {
+    if (c == 0 || s == a.run_len - 1) {
       if (col_in) {
 #pragma unroll
         for (int tau = 0; tau < 4; ++tau) {
@@ -1501,15 +1503,15 @@ __device__ __forceinline__ void stage_output_run(Unit<T, P>& U, const Args& a,
 }
 
 // Work item w of the run-ordered forward: module fastest, then the run q of
-// kRun patch rows, the patch column j, the energy e.  Returns unit (w, s).
+// run_len patch rows, the patch column j, the energy e.  Returns unit (w, s).
 __device__ __forceinline__ int run_unit(const Args& a, int w, int s) {
-  const int nq = a.n / kRun;
+  const int nq = a.n / a.run_len;
   const int m = w % a.M;
   int t = w / a.M;
   const int q = t % nq;
   t /= nq;
   const int j = t % a.n, e = t / a.n;
-  const int k = kRun * q + s + a.n * j;
+  const int k = a.run_len * q + s + a.n * j;
   return ((e * a.n * a.n + k) * a.M + m);
 }
 
@@ -1533,8 +1535,8 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_run(Args a, int items) {
   if (threadIdx.x == 32) prefetch_l2(U.spec, sizeof(cx<T>) * P * R::H);
   const Split2<T> sp = output_splitter<T>(a, &s_slot);
   for (;;) {
-    const int sn = s + 1 < kRun ? s + 1 : 0;
-    const int wn = s + 1 < kRun ? w : w + (int)gridDim.x;
+    const int sn = s + 1 < a.run_len ? s + 1 : 0;
+    const int wn = s + 1 < a.run_len ? w : w + (int)gridDim.x;
     const bool more = wn < items;
     stage_mid<T, P, MID_FROM_SPEC, false>(U);
     __syncthreads();
@@ -1872,6 +1874,7 @@ Args make_args(const Geom& g, const FusedLaunch& f, int which, size_t esz) {
   a.bnd_out = (unsigned long long*)f.bnd_out;
   a.spill = f.spill;
   a.loop_grid = (int)f.loop_grid;
+  a.run_len = 0;
   return a;
 }
 
@@ -1962,10 +1965,35 @@ int launch_pdl(KernelT kern, int64_t grid, bool pdl, cudaStream_t s, ArgsT... ar
 
 // Geometries whose patch outputs share whole block rows of 64 field rows (see
 // k_fwd_run): P = 192 from 64-row strides and a 32-pixel margin, a field of
-// whole strides (no clamped start), and runs of kRun patch rows.
-inline bool run_geometry(const Geom& g) {
-  return g.P == 192 && g.dx == 64 && g.margin == 32 && g.nx == g.n * 64 && g.ny == g.n * 64 &&
-         g.n % kRun == 0 && g.M >= 2;
+// whole strides (no clamped start), and runs of run_len (2 or 4) patch rows.
+inline bool run_geometry(const Geom& g, int run_len) {
+  return (run_len == 2 || run_len == 4) && g.P == 192 && g.dx == 64 && g.margin == 32 &&
+         g.nx == g.n * 64 && g.ny == g.n * 64 && g.n % run_len == 0 && g.M >= 2;
+}
+
+// Run length of the module-shared forward when the plan leaves it to the
+// library: the one whose busiest CTA does the least work.  A CTA of the
+// 152-CTA loop processes ceil(items / G) items of run_len units each, and a
+// unit inside a run costs about 0.87 (runs of 4) or 0.93 (runs of 2) of one
+// reduced on its own (fewer block-row reductions; measured forward times at
+// 768^2 and 1024^2 x 7 modules x 3 energies, where every choice gives the
+// busiest CTA the same number of units).
+inline int auto_run_len(const Geom& g) {
+  const int64_t G = sm_count(), U = g.units();
+  int best = 1;
+  double best_cost = (double)((U + G - 1) / G);
+  const int cand[2] = {2, 4};
+  const double f[2] = {0.93, 0.87};
+  for (int i = 0; i < 2; ++i) {
+    if (!run_geometry(g, cand[i])) continue;
+    const int64_t items = U / cand[i];
+    const double cost = (double)((items + G - 1) / G) * cand[i] * f[i];
+    if (cost < best_cost) {
+      best_cost = cost;
+      best = cand[i];
+    }
+  }
+  return best;
 }
 
 // Grid of the ordered adjoint over g's units (its CTAs' unit ranges and spill
@@ -2010,10 +2038,13 @@ int launch_one(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
       if (!need(f.out_lo && f.bnd_in && f.bnd_n == patches, "low-word plane or input bound"))
         return JUBIK_ERR_STATE;
       if constexpr (sizeof(T) == 4 && P == 192) {
-        if (run_geometry(g)) {
-          const int64_t items = units / kRun;
+        const int r = f.fwd_run > 0 ? f.fwd_run : auto_run_len(g);
+        if (run_geometry(g, r)) {
+          const int64_t items = units / r;
+          Args ar = a;
+          ar.run_len = r;
           return launch_pdl<T, P>(k_fwd_run<T, P>, loop_grid<T, P>(k_fwd_run<T, P>, items),
-                                  f.pdl, s, a, (int)items);
+                                  f.pdl, s, ar, (int)items);
         }
       }
       return launch_pdl<T, P>(k_fwd_from_spec<T, P, OneProblem>,
@@ -2229,6 +2260,16 @@ int64_t fused_adj_grid(const Geom& g, int dtype) {
   if ((dtype == JUBIK_F32 ? ensure_attrs_dispatch<float>(g.P) : ensure_attrs_dispatch<double>(g.P)))
     return 0;
   return dtype == JUBIK_F32 ? ord_grid_dispatch<float>(g) : ord_grid_dispatch<double>(g);
+}
+
+// Run length the module-shared forward of geometry g uses for a request
+// (0: the library's choice): 2 or 4 for the run-ordered kernel, 1 for one
+// unit at a time.  Returns -1 for a request the geometry cannot take.
+int fused_fwd_run_len(const Geom& g, int dtype, int requested) {
+  const bool fits = dtype == JUBIK_F32 && g.P == 192;
+  if (requested == 0) return fits ? auto_run_len(g) : 1;
+  if (requested == 1) return 1;
+  return fits && run_geometry(g, requested) ? requested : -1;
 }
 
 int fused_run(const Geom& g, int dtype, const FusedLaunch& a, int which, cudaStream_t s) {

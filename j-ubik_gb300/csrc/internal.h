@@ -112,10 +112,16 @@ struct FusedLaunch {
   // and its grid (fused_adj_grid)
   void* spill = nullptr;
   int64_t loop_grid = 0;
+  // module-shared forward: patches per run of the run-ordered kernel (0: the
+  // library's choice, 1: one unit at a time; see fused_fwd_run_len)
+  int fwd_run = 0;
 };
 // CTAs of the ordered module-shared adjoint for geometry g (0 where the fused
 // path does not cover g.P): the count of its unit ranges and spill slots.
 int64_t fused_adj_grid(const Geom& g, int dtype);
+// Run length of the module-shared forward for a request (0 = the library's
+// choice): 1, 2 or 4, or -1 where geometry g cannot take the request.
+int fused_fwd_run_len(const Geom& g, int dtype, int requested);
 size_t fused_spec_bytes(const Geom& g, int dtype);
 // Grouped per-unit launches over independent problems of one FFT side: the
 // kernel-argument block of one problem's stage (fused_args_size() bytes,

@@ -1138,8 +1138,11 @@ template <typename T>
 int absmax_blocks(const void* in, int E, int rows, int cols, int64_t ps, int64_t rs, bool exp_of,
                   void* out, int* nb, bool pdl, cudaStream_t s) {
   const int64_t n = (int64_t)E * rows * cols;
-  int blocks = (int)std::min<int64_t>(kMaxBoundBlocks, std::max<int64_t>(1, (n + kBlock - 1) /
-                                                                               kBlock));
+  // at least 16 values per thread: every kernel that reads the bound reduces
+  // these nb maxima once per CTA, so fewer, fuller blocks serve them better
+  constexpr int64_t kPerBlock = (int64_t)kBlock * 16;
+  int blocks = (int)std::min<int64_t>(kMaxBoundBlocks,
+                                      std::max<int64_t>(1, (n + kPerBlock - 1) / kPerBlock));
   *nb = blocks;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(blocks);

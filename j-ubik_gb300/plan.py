@@ -155,6 +155,51 @@ class ResponsePlan:
         _lib.call("jubik_plan_set_dependent_launch", self._h, 1 if on else 0)
         return self
 
+    def set_forward_run(self, run_len: int = 0) -> "ResponsePlan":
+        """Patches per run of the module-shared FP32 forward at FFT side 192: 4
+        reduces the fewest field rows, 2 and 1 give more work items for small
+        fields, 0 lets the library choose (the default).  Raises
+        JubikUnsupported for runs the geometry cannot take, ValueError for
+        other lengths."""
+        _lib.call("jubik_plan_set_forward_run", self._h, int(run_len))
+        return self
+
+    @property
+    def forward_run(self) -> int:
+        """The run length the forward uses (1 where it does not run in runs)."""
+        r = C.c_int32()
+        _lib.call("jubik_plan_forward_run", self._h, C.byref(r))
+        return int(r.value)
+
+    def autotune(self, x, candidates: Sequence[int] = (1, 2, 4), reps: int = 5) -> dict:
+        """Time one energy-and-gradient pass on sky x (the plan's data must be
+        set) for each applicable forward run length, keep the fastest, and
+        return {run length: ms per pass}."""
+        x = self._sky(x)
+        grad = torch.empty((self.n_energies,) + self.shape, dtype=self.dtype,
+                           device=self.device)
+        energy = torch.empty((), dtype=torch.float64, device=self.device)
+        times = {}
+        with torch.cuda.device(self.device):
+            stream = torch.cuda.current_stream(self.device)
+            for r in candidates:
+                try:
+                    self.set_forward_run(r)
+                except _lib.JubikUnsupported:
+                    continue
+                for _ in range(2):
+                    self.energy_and_grad(x, energy=energy, grad=grad)
+                t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                t0.record(stream)
+                for _ in range(reps):
+                    self.energy_and_grad(x, energy=energy, grad=grad)
+                t1.record(stream)
+                t1.synchronize()
+                times[int(r)] = t0.elapsed_time(t1) / reps
+        if times:
+            self.set_forward_run(min(times, key=times.get))
+        return times
+
     def set_profiling(self, on: bool = True) -> None:
         """Bracket every kernel phase with CUDA events (resets the totals)."""
         _lib.call("jubik_plan_set_profiling", self._h, int(bool(on)))
