@@ -266,6 +266,7 @@ def uneven_batch_leg(dev, n_streams=8, passes=10, modules=1, count=64):
         out = {"problems": len(insts), "modules": modules, "mpix_per_pass": b.mpix,
                "streams": n_streams,
                "paths": {str(k): v for k, v in chosen.items()},
+               "autotune_ms": {str(k): v for k, v in b.timings.items()},
                "loop_ms": loop_ms, "graph_ms": graph_ms, "loop_launches": 5 * len(insts),
                "loop_mpix_s": b.mpix / (loop_ms / 1e3), "graph_mpix_s": b.mpix / (graph_ms / 1e3),
                "graph_speedup": loop_ms / graph_ms}

@@ -236,10 +236,15 @@ JUBIK_API int jubik_psf_interpolate(const double* psfs, const double* rs,
  * which evaluates one likelihood per call): plans of one dtype on a fused FFT
  * side, grouped by FFT side and kind (per-unit kernels, or module-shared patch
  * spectra for plans with several modules).  One energy+gradient call of the
- * group is one grouped clearing kernel; per side, one forward and one adjoint
- * launch over all of that side's per-unit problems, or two of each (patch
- * spectra, then units) for its module-shared problems; and one grouped
- * likelihood pass -- the work of jubik_poisson_energy_grad on every plan.  The
+ * group is one grouped clearing kernel and one pass over the skies' largest
+ * magnitudes; per side, one forward and one adjoint launch over all of that
+ * side's per-unit problems, or two of each (patch spectra, then units) for its
+ * module-shared problems; one grouped likelihood pass; and one pass that adds
+ * the low words of the gradients -- the work of jubik_poisson_energy_grad on
+ * every plan.  As there, the overlap-adds and gradients are exact two-word
+ * sums and the module sums run in module order, so results are the same bits
+ * on every call (each problem's bound comes from its own sky and residual, so
+ * they can differ from a one-plan call's in the last bit).  The
  * plans must outlive the group, and none of them may run another call while a
  * group call is in flight.  set_io copies the plans' buffer addresses; after a
  * plan's jubik_plan_set_exposure (or its first jubik_plan_set_data) the group's

@@ -137,12 +137,24 @@ class ProblemBatch:
                     res[path] = t0.elapsed_time(t1) / reps
                 finally:
                     plan.close()
-            chosen[P] = min(res, key=res.get)
+            best = min(res, key=res.get)
+            # near ties go to the module-shared kernels: they do less work in all
+            # (one sky spectrum per patch for all modules), which counts once the
+            # problems share the GPU in a graph or a grouped pass
+            if "fused" in res and res["fused"] <= 1.05 * res[best]:
+                best = "fused"
+            chosen[P] = best
             timings[P] = res
         self.timings = timings
         if chosen != {P: self.paths.get(P, "auto") for P in chosen}:
             self.paths.update(chosen)
             self._rebuild()
+        # the forward's run length (patches whose shared block rows meet in TMEM)
+        # on every plan that runs the module-shared FP32 kernels at FFT side 192
+        self.run_timings = {}
+        for k, plan in enumerate(self.plans):
+            if plan.shared_spectra and plan.dtype == torch.float32 and plan.P == 192:
+                self.run_timings[k] = plan.autotune(self.x[k], reps=reps)
         return chosen
 
     def group(self) -> bool:

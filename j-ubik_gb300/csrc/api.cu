@@ -1238,6 +1238,8 @@ struct GroupClass {
   void* adj_list = nullptr;  // device Args per member: adjoint stages
   int* starts = nullptr;     // device: first unit of each member, then the total
   int* item_starts = nullptr;  // device: first item of each member, then the total
+  int* ord_starts = nullptr;   // device (shared): first CTA of each member's ordered adjoint
+  int64_t ord_blocks = 0;      // CTAs of the ordered adjoint over all members
 };
 
 struct jubik_group {
@@ -1252,6 +1254,15 @@ struct jubik_group {
   int* zstarts = nullptr;
   int64_t zblocks = 0;
   int nzero = 0;
+  // exact two-word sums: one forward-bound slot per problem (the largest |sky|),
+  // the grouped maxima pass that fills them, and the final hi + lo pass
+  unsigned long long* bslots = nullptr;
+  AbsmaxJob* ajobs = nullptr;
+  int* astarts = nullptr;
+  int64_t ablocks = 0;
+  CombineJob* cjobs = nullptr;
+  int* cstarts = nullptr;
+  int64_t cblocks = 0;
   bool io_set = false;
   std::vector<void*> allocs;
   int alloc(void** p, size_t n) {
@@ -1264,11 +1275,14 @@ struct jubik_group {
     allocs.clear();
     for (auto& c : classes) {
       c.fwd_list = c.adj_list = nullptr;
-      c.starts = c.item_starts = nullptr;
+      c.starts = c.item_starts = c.ord_starts = nullptr;
     }
     pjobs = nullptr;
     zjobs = nullptr;
-    pstarts = zstarts = nullptr;
+    pstarts = zstarts = astarts = cstarts = nullptr;
+    bslots = nullptr;
+    ajobs = nullptr;
+    cjobs = nullptr;
     io_set = false;
   }
   ~jubik_group() { free_io(); }
@@ -1353,29 +1367,63 @@ int jubik_group_set_io(jubik_group* g, const void* const* x, void* const* grad,
   }
   g->free_io();
   const size_t asz = fused_args_size();
+  // forward-bound slots, one per problem (16-byte multiple for the clearing pass)
+  const int64_t slot_bytes = ((int64_t)n * 8 + 15) & ~(int64_t)15;
+  JUBIK_TRY(g->alloc((void**)&g->bslots, slot_bytes));
   for (auto& c : g->classes) {
     std::vector<unsigned char> fwd(asz * c.members.size()), adj(asz * c.members.size());
-    std::vector<int> starts, item_starts;
-    int64_t b = 0, items = 0;
+    std::vector<int> starts, item_starts, ord_starts;
+    int64_t b = 0, items = 0, ob = 0;
+    // module-shared classes: each problem's ordered adjoint gets CTAs in
+    // proportion to its units (at most its spill slots), about as many in all as
+    // the GPU holds at once
+    int64_t per_cta = 1;
+    if (c.shared) {
+      int64_t total = 0;
+      for (int i : c.members) total += g->plans[i]->g.units();
+      const int64_t cap = std::max<int64_t>(1, fused_ord_capacity(c.P, g->dtype));
+      per_cta = std::max<int64_t>(1, (total + cap - 1) / cap);
+    }
     for (size_t k = 0; k < c.members.size(); ++k) {
       const int i = c.members[k];
       jubik_plan* p = g->plans[i];
+      const Geom& pg = p->g;
       starts.push_back((int)b);
       item_starts.push_back((int)items);
-      b += p->g.units();
-      items += (int64_t)p->g.E * p->g.n * p->g.n;
-      // module-shared plans: the forward stages share p->spec, the adjoint stages sum
-      // into p->acc; nothing is cleared inside them (the clearing kernel runs first)
+      b += pg.units();
+      items += (int64_t)pg.E * pg.n * pg.n;
+      const double area = std::fabs(p->desc.pixel_area);
+      // forward: overlap-add exact in two words, bounded by the problem's largest |sky|
       FusedLaunch f{x[i], p->conv, p->hmain, p->hnyq, p->tw, p->wt, p->desc.pixel_area,
                     c.shared ? p->spec : nullptr};
       f.clear = false;
-      fused_args_fill(p->g, p->dtype, f, c.shared ? FUSED_FWD_SKY : FUSED_FWD_UNITS,
+      f.out_lo = p->conv_lo;
+      f.bnd_in = g->bslots + i;
+      f.bnd_n = 1;
+      f.bnd_log2 = fwd_terms_log2(pg);
+      f.bnd_scale = 2.0 * (double)(int64_t(1) << f.bnd_log2) * p->kmax * area;
+      fused_args_fill(pg, p->dtype, f, c.shared ? FUSED_FWD_SKY : FUSED_FWD_UNITS,
                       fwd.data() + k * asz);
+      // adjoint: gradient exact in two words, bounded by the residual's block maxima
+      // that the grouped likelihood pass leaves in the plan's bnd_a
       FusedLaunch r{p->resid, grad[i], p->hmain, p->hnyq, p->tw, p->wt, p->desc.pixel_area,
                     c.shared ? p->acc : nullptr};
       r.zero_out = false;
       r.clear = false;
-      fused_args_fill(p->g, p->dtype, r, c.shared ? FUSED_ADJ_TO_SPEC : FUSED_ADJ_UNITS,
+      r.out_lo = p->grad_lo;
+      r.bnd_in = p->bnd_a;
+      r.bnd_n = poisson_group_blocks(image_elems(p));
+      r.bnd_log2 = adj_terms_log2(pg);
+      r.bnd_scale = 2.0 * (double)(int64_t(1) << r.bnd_log2) * p->kmax * area;
+      if (c.shared) {  // module sums in module order (ordered adjoint, spill slots)
+        const int64_t G = std::max<int64_t>(
+            1, std::min<int64_t>(p->adj_grid, (pg.units() + per_cta - 1) / per_cta));
+        ord_starts.push_back((int)ob);
+        ob += G;
+        r.spill = p->spill;
+        r.loop_grid = G;
+      }
+      fused_args_fill(pg, p->dtype, r, c.shared ? FUSED_ADJ_TO_SPEC : FUSED_ADJ_UNITS,
                       adj.data() + k * asz);
     }
     if (b > 0x7fffffffLL) {
@@ -1389,42 +1437,64 @@ int jubik_group_set_io(jubik_group* g, const void* const* x, void* const* grad,
     JUBIK_TRY(upload(g, fwd, (unsigned char**)&c.fwd_list));
     JUBIK_TRY(upload(g, adj, (unsigned char**)&c.adj_list));
     JUBIK_TRY(upload(g, starts, &c.starts));
-    if (c.shared) JUBIK_TRY(upload(g, item_starts, &c.item_starts));
+    if (c.shared) {
+      ord_starts.push_back((int)ob);
+      c.ord_blocks = ob;
+      JUBIK_TRY(upload(g, item_starts, &c.item_starts));
+      JUBIK_TRY(upload(g, ord_starts, &c.ord_starts));
+    }
   }
   std::vector<PoissonJob> pj;
   std::vector<ZeroJob> zj;
-  std::vector<int> ps, zs;
-  int64_t pb = 0, zb = 0;
+  std::vector<AbsmaxJob> aj;
+  std::vector<CombineJob> cj;
+  std::vector<int> ps, zs, as, cs;
+  int64_t pb = 0, zb = 0, ab = 0, cb = 0;
+  auto add_zero = [&](void* ptr, int64_t bytes) {
+    zj.push_back(ZeroJob{ptr, bytes});
+    zs.push_back((int)zb);
+    zb += std::max<int64_t>(1, std::min<int64_t>(1024, bytes / (256 * 16 * 8)));
+  };
+  add_zero(g->bslots, slot_bytes);
   for (int i = 0; i < n; ++i) {
     jubik_plan* p = g->plans[i];
     const int64_t img = image_elems(p);
-    pj.push_back(PoissonJob{p->conv, p->eps, p->dimg, img, p->wts, p->resid, p->partials,
-                            p->counter, energies + i});
+    const int64_t sky = (int64_t)p->g.E * p->g.pixels();
+    pj.push_back(PoissonJob{p->conv, p->conv_lo, p->eps, p->dimg, img, p->wts, p->resid,
+                            p->partials, p->counter, energies + i,
+                            (unsigned long long*)p->bnd_a});
     ps.push_back((int)pb);
     pb += poisson_group_blocks(img);
-    // each problem's overlap-add image and gradient start from zero, and so does
-    // the module-shared accumulator that the grouped adjoint adds into (a
-    // one-problem call leaves its last sums there)
-    const int64_t bytes[3] = {img * (int64_t)p->esz,
-                              (int64_t)p->g.E * p->g.pixels() * (int64_t)p->esz,
-                              p->acc ? (int64_t)fused_spec_bytes(p->g, p->dtype) : 0};
-    void* ptrs[3] = {p->conv, grad[i], p->acc};
-    for (int t = 0; t < 3; ++t) {
-      if (!ptrs[t]) continue;
-      zj.push_back(ZeroJob{ptrs[t], bytes[t]});
-      zs.push_back((int)zb);
-      zb += std::max<int64_t>(1, std::min<int64_t>(1024, bytes[t] / (256 * 16 * 8)));
-    }
+    aj.push_back(AbsmaxJob{x[i], sky, g->bslots + i});
+    as.push_back((int)ab);
+    ab += group_blocks(sky);
+    cj.push_back(CombineJob{grad[i], p->grad_lo, sky});
+    cs.push_back((int)cb);
+    cb += group_blocks(sky);
+    // both words of each problem's image and gradient start from zero (the
+    // module sums of the ordered adjoint are written whole)
+    add_zero(p->conv, img * (int64_t)p->esz);
+    add_zero(p->conv_lo, img * (int64_t)p->esz);
+    add_zero(grad[i], sky * (int64_t)p->esz);
+    add_zero(p->grad_lo, sky * (int64_t)p->esz);
   }
   ps.push_back((int)pb);
   zs.push_back((int)zb);
+  as.push_back((int)ab);
+  cs.push_back((int)cb);
   g->pblocks = pb;
   g->zblocks = zb;
+  g->ablocks = ab;
+  g->cblocks = cb;
   g->nzero = (int)zj.size();
   JUBIK_TRY(upload(g, pj, &g->pjobs));
   JUBIK_TRY(upload(g, ps, &g->pstarts));
   JUBIK_TRY(upload(g, zj, &g->zjobs));
   JUBIK_TRY(upload(g, zs, &g->zstarts));
+  JUBIK_TRY(upload(g, aj, &g->ajobs));
+  JUBIK_TRY(upload(g, as, &g->astarts));
+  JUBIK_TRY(upload(g, cj, &g->cjobs));
+  JUBIK_TRY(upload(g, cs, &g->cstarts));
   g->gens.clear();
   for (jubik_plan* p : g->plans) g->gens.push_back(p->layout_gen);
   g->io_set = true;
@@ -1448,6 +1518,7 @@ int jubik_group_energy_grad(jubik_group* g, void* stream) {
     }
   }
   JUBIK_TRY(zero_group_run(g->zjobs, g->zstarts, g->nzero, g->zblocks, true, s));
+  JUBIK_TRY(absmax_group_run(g->dtype, g->ajobs, g->astarts, n, g->ablocks, true, s));
   for (auto& c : g->classes) {
     const int m = (int)c.members.size();
     if (c.shared) {
@@ -1464,7 +1535,7 @@ int jubik_group_energy_grad(jubik_group* g, void* stream) {
   for (auto& c : g->classes) {
     const int m = (int)c.members.size();
     if (c.shared) {
-      JUBIK_TRY(fused_group_shared_run(c.P, g->dtype, c.adj_list, c.starts, m, c.blocks,
+      JUBIK_TRY(fused_group_shared_run(c.P, g->dtype, c.adj_list, c.ord_starts, m, c.ord_blocks,
                                        FUSED_ADJ_TO_SPEC, true, s));
       JUBIK_TRY(fused_group_shared_run(c.P, g->dtype, c.adj_list, c.item_starts, m, c.items,
                                        FUSED_ADJ_FROM_SPEC, true, s));
@@ -1473,6 +1544,7 @@ int jubik_group_energy_grad(jubik_group* g, void* stream) {
                                 s));
     }
   }
+  JUBIK_TRY(combine_group_run(g->dtype, g->cjobs, g->cstarts, n, g->cblocks, true, s));
   for (jubik_plan* p : g->plans) p->lam_valid = true;
   return JUBIK_OK;
 }
@@ -1482,7 +1554,7 @@ int jubik_group_launches(const jubik_group* g, int32_t* launches) {
     set_error("group: invalid arguments");
     return JUBIK_ERR_INVALID_ARGUMENT;
   }
-  int32_t k = 2;
+  int32_t k = 4;  // clearing, sky maxima, likelihood, combine
   for (const auto& c : g->classes) k += c.shared ? 4 : 2;
   *launches = k;
   return JUBIK_OK;

@@ -1261,6 +1261,16 @@ __device__ __forceinline__ Split2<T> output_splitter(const Args& a, unsigned lon
   return sp;
 }
 
+// The same for a bound already reduced to one value (bnd_n == 1), per thread:
+// no CTA-wide step, so a loop over the units of several problems can take
+// each unit's problem's splitter.
+template <typename T>
+__device__ __forceinline__ Split2<T> splitter_one(const Args& a) {
+  Split2<T> sp;
+  sp.init(a.bnd_scale * __longlong_as_double((long long)__ldcg(a.bnd_in)), a.bnd_log2);
+  return sp;
+}
+
 // One CTA per unit: the whole forward or adjoint of one patch.  TWO: the
 // output accumulates in two words (one problem; its input bound was recorded
 // by a pass before this kernel).
@@ -1297,12 +1307,14 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fused(Args a) {
 }
 
 // Grouped launch over independent problems of one FFT side: problem p owns
-// blocks [starts[p], starts[p + 1]) and its own arguments list[p].
+// blocks [starts[p], starts[p + 1]) and its own arguments list[p].  Each
+// problem's output accumulates exactly in two words, with its own bound.
 template <typename T, int P, bool ADJ>
 __global__ void __launch_bounds__(Tr<T, P>::NT)
     k_fused_group(const Args* __restrict__ list, const int* __restrict__ starts, int nprob) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_prob;
+  __shared__ unsigned long long s_slot;
   pdl_trigger();
   if (threadIdx.x == 0) {  // the last problem whose first block is <= blockIdx.x
     int lo = 0, hi = nprob - 1;
@@ -1318,7 +1330,7 @@ __global__ void __launch_bounds__(Tr<T, P>::NT)
   __syncthreads();
   const int p = s_prob;
   const Args a = list[p];
-  fused_unit_body<T, P, ADJ, false>(a, (int)blockIdx.x - starts[p], smem_raw, nullptr);
+  fused_unit_body<T, P, ADJ, true>(a, (int)blockIdx.x - starts[p], smem_raw, &s_slot);
 }
 
 // Forward, module-shared: the sky spectrum of each (energy, patch) once; the
@@ -1381,6 +1393,10 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_from_spec(Src src, int uni
   }
   for (;;) {
     const int gn = g + (int)gridDim.x;
+    if constexpr (!ORD) {  // each problem of a list has its own bound, reduced to one value
+      int lu;
+      sp = splitter_one<T>(src.at(g, lu));
+    }
     stage_mid<T, P, MID_FROM_SPEC, false>(U);
     __syncthreads();
     stage_invB<T, P, 0>(U, U.tid, R::NT);
@@ -1396,7 +1412,7 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_from_spec(Src src, int uni
     }
     {
       int lu;
-      stage_output<T, P, false, ORD>(U, src.at(g, lu), sp);
+      stage_output<T, P, false, true>(U, src.at(g, lu), sp);
     }
     if (gn >= units) break;
     __syncthreads();  // the output stage's last staging reads before the next mid writes
@@ -1679,26 +1695,24 @@ struct OrdCursor {
   }
 };
 
+// The ordered adjoint of one problem on CTA b of the G CTAs given to it.
 template <typename T, int P>
-__global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_to_spec_ord(Args a, int units) {
+__device__ __forceinline__ void ord_adjoint(const Args& a, int64_t b, int64_t G, int units,
+                                            unsigned char* smem_raw, uint32_t* s_tmem) {
   using R = Tr<T, P>;
   using TG = TmemGeom<T, P>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ uint32_t s_tmem;
   cx<T>* c0 = reinterpret_cast<cx<T>*>(smem_raw + R::SMEM);
-  pdl_trigger();
-  const int64_t b = blockIdx.x;
-  const OrdSchedule sch(gridDim.x, a.M, units / a.M);
+  const OrdSchedule sch(G, a.M, units / a.M);
   const int64_t cnt = sch.count(b), tlo = sch.tail_lo(b), tail_start = sch.rounds * sch.M;
   OrdCursor cur(sch, b);
   Unit<T, P> U;
   U.init(a, smem_raw, true, (int)cur.g);
   prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
-  if (U.warp == 0) tmem_alloc(&s_tmem, TG::NCOLS);
+  if (U.warp == 0) tmem_alloc(s_tmem, TG::NCOLS);
   tmem_fence_before_sync();
   __syncthreads();
   tmem_fence_after_sync();
-  const uint32_t tbase = s_tmem;
+  const uint32_t tbase = *s_tmem;
   pdl_wait();
   const int64_t gbytes = (int64_t)a.E * a.nx * a.ny * (int64_t)sizeof(T);
   if (a.zero_out) zero_slice(a.out, gbytes, a.zchunk);
@@ -1736,14 +1750,45 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_to_spec_ord(Args a, int un
   if (U.warp == 0) tmem_dealloc(tbase, TG::NCOLS);
 }
 
-// ... then, per (energy, patch), one inverse transform -> window -> gradient.
-// One problem: the accumulator plus the continuing CTAs' spill slots (in CTA
-// order), and the gradient accumulates exactly in two words.  A list of
-// problems: the accumulator is cleared as it is read.
+template <typename T, int P>
+__global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_to_spec_ord(Args a, int units) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ uint32_t s_tmem;
+  pdl_trigger();
+  ord_adjoint<T, P>(a, blockIdx.x, gridDim.x, units, smem_raw, &s_tmem);
+}
+
+// The ordered adjoint over a list of independent problems: problem p takes CTAs
+// [cta_starts[p], cta_starts[p + 1]) and runs its own schedule on them (its
+// spill slots hold that many CTAs).  The grouped pass clears every output first.
+template <typename T, int P>
+__global__ void __launch_bounds__(Tr<T, P>::NT)
+    k_adj_to_spec_ord_list(const Args* __restrict__ list, const int* __restrict__ cta_starts,
+                           int nprob) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ uint32_t s_tmem;
+  pdl_trigger();
+  int lo = 0, hi = nprob - 1;  // the last problem whose first CTA is <= blockIdx.x
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(cta_starts + mid) <= (int)blockIdx.x)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const Args a = list[lo];
+  const int64_t b0 = __ldg(cta_starts + lo), G = __ldg(cta_starts + lo + 1) - b0;
+  ord_adjoint<T, P>(a, (int64_t)blockIdx.x - b0, G, a.M * a.E * a.n * a.n, smem_raw, &s_tmem);
+}
+
+// ... then, per (energy, patch), one inverse transform -> window -> gradient:
+// the patch's module sum plus the continuing CTAs' spill slots (in CTA order),
+// and the gradient accumulates exactly in two words (each problem with its own
+// bound).  Without spill slots the accumulator was summed by reductions, and it
+// is cleared as it is read.
 template <typename T, int P, typename Src>
 __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_from_spec(Src src) {
   using R = Tr<T, P>;
-  constexpr bool ORD = std::is_same<Src, OneProblem>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned long long s_slot;
   Unit<T, P> U;
@@ -1751,7 +1796,10 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_from_spec(Src src) {
   int item;
   const Args& a = src.at((int)blockIdx.x, item);
   U.init(a, smem_raw, false, item);
-  if constexpr (ORD) {
+  // the module sums come from the ordered adjoint (spill slots set) or, in a
+  // list of problems without it, from reductions into a cleared accumulator
+  const bool ordered = a.spill != nullptr;
+  if (ordered) {
     // CTAs of the ordered adjoint whose tail range starts inside this patch:
     // tail_lo(b) in (u0, u0 + M) (none for the patches of the full rounds)
     const int64_t G = a.loop_grid, patches = (int64_t)a.E * a.n * a.n;
@@ -1767,16 +1815,15 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_from_spec(Src src) {
     U.nsp = n;
   }
   pdl_wait();
-  Split2<T> sp{};
-  if constexpr (ORD) sp = output_splitter<T>(a, &s_slot);
+  const Split2<T> sp = output_splitter<T>(a, &s_slot);  // the gradient is exact in two words
   stage_mid<T, P, MID_FROM_ACC, true>(U);
   __syncthreads();
   stage_invB<T, P, 0>(U, U.tid, R::NT);
   __syncthreads();
   stage_combine<T, P>(U, U.mg / 2, (U.mg + U.K + 1) / 2);
   __syncthreads();
-  stage_output<T, P, true, ORD>(U, a, sp);
-  if constexpr (!ORD) {
+  stage_output<T, P, true, true>(U, a, sp);
+  if (!ordered) {
     // leave this patch's accumulator zero for the next call (read in the first stage)
     float4* z = reinterpret_cast<float4*>(U.spec);
     constexpr int n16 = (int)(sizeof(cx<T>) * P * R::H / 16);
@@ -1924,6 +1971,7 @@ int ensure_smem_attrs() {
     JUBIK_TRY(set_smem(k_adj_to_spec<T, P, ProblemList>, smem));
     JUBIK_TRY(set_smem(k_fwd_from_spec<T, P, ProblemList>, smem));
     JUBIK_TRY(set_smem(k_adj_to_spec_ord<T, P>, ord_smem_bytes<T, P>()));
+    JUBIK_TRY(set_smem(k_adj_to_spec_ord_list<T, P>, ord_smem_bytes<T, P>()));
     if constexpr (sizeof(T) == 4 && P == 192) JUBIK_TRY(set_smem(k_fwd_run<T, P>, smem));
     attr_set[dev] = true;
   }
@@ -2106,10 +2154,9 @@ int launch_group_shared(const void* list, const int* starts, int nprob, int64_t 
       return launch_pdl<T, P>(k_fwd_from_spec<T, P, ProblemList>,
                               loop_grid<T, P>(k_fwd_from_spec<T, P, ProblemList>, count), pdl, s,
                               src, (int)count);
-    case FUSED_ADJ_TO_SPEC:
-      return launch_pdl<T, P>(k_adj_to_spec<T, P, ProblemList>,
-                              loop_grid<T, P>(k_adj_to_spec<T, P, ProblemList>, count), pdl, s,
-                              src, (int)count);
+    case FUSED_ADJ_TO_SPEC:  // starts: each problem's CTA range; count: all CTAs
+      return launch_pdl_smem<T, P>(k_adj_to_spec_ord_list<T, P>, count, ord_smem_bytes<T, P>(),
+                                   pdl, s, (const Args*)list, starts, nprob);
     case FUSED_ADJ_FROM_SPEC:
       return launch_pdl<T, P>(k_adj_from_spec<T, P, ProblemList>, count, pdl, s, src);
     default:
@@ -2270,6 +2317,18 @@ int fused_fwd_run_len(const Geom& g, int dtype, int requested) {
   if (requested == 0) return fits ? auto_run_len(g) : 1;
   if (requested == 1) return 1;
   return fits && run_geometry(g, requested) ? requested : -1;
+}
+
+// CTAs of the ordered adjoint at FFT side P that the GPU holds at once (0 where
+// the fused path does not cover P).
+int64_t fused_ord_capacity(int P, int dtype) {
+  if (!fused_supported(P, dtype)) return 0;
+  Geom g{};
+  g.P = P;
+  g.M = 1;
+  g.E = 1;
+  g.n = 1 << 15;  // more units than any GPU holds CTAs
+  return fused_adj_grid(g, dtype);
 }
 
 int fused_run(const Geom& g, int dtype, const FusedLaunch& a, int which, cudaStream_t s) {

@@ -122,6 +122,9 @@ int64_t fused_adj_grid(const Geom& g, int dtype);
 // Run length of the module-shared forward for a request (0 = the library's
 // choice): 1, 2 or 4, or -1 where geometry g cannot take the request.
 int fused_fwd_run_len(const Geom& g, int dtype, int requested);
+// CTAs of the ordered module-shared adjoint at FFT side P that fit on the GPU
+// at once (0 where the fused path does not cover P).
+int64_t fused_ord_capacity(int P, int dtype);
 size_t fused_spec_bytes(const Geom& g, int dtype);
 // Grouped per-unit launches over independent problems of one FFT side: the
 // kernel-argument block of one problem's stage (fused_args_size() bytes,
@@ -131,6 +134,7 @@ size_t fused_spec_bytes(const Geom& g, int dtype);
 // Grouped likelihood pass and grouped clearing over independent problems.
 struct PoissonJob {
   const void* conv;
+  const void* conv_lo;  // low words of the exact overlap-add (the image is conv + conv_lo)
   const void* eps;
   const int32_t* dimg;
   int64_t npix;
@@ -139,11 +143,30 @@ struct PoissonJob {
   double* partials;
   unsigned int* counter;
   double* energy;
+  unsigned long long* rmax;  // per-block maxima of |resid| (the adjoint's bound), or nullptr
 };
 struct ZeroJob {
   void* ptr;
   int64_t bytes;
 };
+// Grouped maxima of |in[0 .. n)| into one slot per job (atomicMax of the bits).
+struct AbsmaxJob {
+  const void* in;
+  int64_t n;
+  unsigned long long* slot;
+};
+// Grouped two-word combine: hi[i] += lo[i], i < n.
+struct CombineJob {
+  void* hi;
+  const void* lo;
+  int64_t n;
+};
+// Blocks of one job of the grouped maxima and combine passes (<= 1024).
+int group_blocks(int64_t n);
+int absmax_group_run(int dtype, const AbsmaxJob* jobs, const int* starts, int njobs,
+                     int64_t blocks, bool pdl, cudaStream_t s);
+int combine_group_run(int dtype, const CombineJob* jobs, const int* starts, int njobs,
+                      int64_t blocks, bool pdl, cudaStream_t s);
 int poisson_group_blocks(int64_t npix);
 int poisson_group_run(int dtype, const PoissonJob* jobs, const int* starts, int njobs,
                       int64_t blocks, bool pdl, cudaStream_t s);

@@ -711,9 +711,94 @@ __global__ void __launch_bounds__(kBlock)
   }
   __syncthreads();
   const PoissonJob jb = jobs[s_job];
-  poisson_image_body<T>((const T*)jb.conv, nullptr, (const T*)jb.eps, jb.dimg, jb.npix, (T*)jb.wts,
-                        (T*)jb.resid, jb.partials, jb.counter, jb.energy,
-                        blockIdx.x - starts[s_job], starts[s_job + 1] - starts[s_job], nullptr);
+  poisson_image_body<T>((const T*)jb.conv, (const T*)jb.conv_lo, (const T*)jb.eps, jb.dimg,
+                        jb.npix, (T*)jb.wts, (T*)jb.resid, jb.partials, jb.counter, jb.energy,
+                        blockIdx.x - starts[s_job], starts[s_job + 1] - starts[s_job], jb.rmax);
+}
+
+// The job that owns this block (the last whose first block is <= blockIdx.x).
+__device__ __forceinline__ int block_job(const int* __restrict__ starts, int njobs) {
+  __shared__ int s_job;
+  __syncthreads();  // a previous call's readers are done with s_job
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (starts[mid] <= (int)blockIdx.x)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    s_job = lo;
+  }
+  __syncthreads();
+  return s_job;
+}
+
+// Grouped magnitude maxima: job j (one problem's sky) owns blocks [starts[j],
+// starts[j + 1]).  Each block takes the largest |value| of its share and raises
+// the job's slot to it by atomicMax on the bits of a non-negative double, which
+// order as the values do (a NaN, stored as the canonical quiet NaN, sorts above
+// +inf): the slot ends at the same value in any order of the blocks.
+template <typename T>
+__global__ void __launch_bounds__(kBlock)
+    k_absmax_group(const AbsmaxJob* __restrict__ jobs, const int* __restrict__ starts,
+                   int njobs) {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  const int j = block_job(starts, njobs);
+  const AbsmaxJob jb = jobs[j];
+  const int64_t nb = starts[j + 1] - starts[j], b = blockIdx.x - starts[j];
+  const int64_t stride = nb * blockDim.x;
+  const T* in = (const T*)jb.in;
+  MagMax<T> mm;
+  int64_t i0 = 0;
+  if constexpr (sizeof(T) == 4) {
+    if ((reinterpret_cast<uintptr_t>(in) & 15) == 0) {
+      const int64_t n4 = jb.n / 4;
+      const float4* in4 = reinterpret_cast<const float4*>(in);
+      for (int64_t i = b * blockDim.x + threadIdx.x; i < n4; i += stride) {
+        const float4 q = __ldcs(in4 + i);
+        mm.add(q.x);
+        mm.add(q.y);
+        mm.add(q.z);
+        mm.add(q.w);
+      }
+      i0 = n4 * 4;
+    }
+  }
+  for (int64_t i = i0 + b * blockDim.x + threadIdx.x; i < jb.n; i += stride) mm.add(in[i]);
+  __shared__ unsigned long long red[1];
+  store_block_max(mm.bits(), red, 0);
+  if (threadIdx.x == 0) atomicMax(jb.slot, red[0]);
+}
+
+// Grouped two-word combine: hi[i] += lo[i] over every job's n values.
+template <typename T>
+__global__ void __launch_bounds__(kBlock)
+    k_combine_group(const CombineJob* __restrict__ jobs, const int* __restrict__ starts,
+                    int njobs) {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  const int j = block_job(starts, njobs);
+  const CombineJob jb = jobs[j];
+  const int64_t nb = starts[j + 1] - starts[j], b = blockIdx.x - starts[j];
+  const int64_t stride = nb * blockDim.x;
+  T* hi = (T*)jb.hi;
+  const T* lo = (const T*)jb.lo;
+  int64_t i0 = 0;
+  if constexpr (sizeof(T) == 4) {  // plan and batch buffers are 16-byte aligned
+    const int64_t n4 = jb.n / 4;
+    float4* h4 = reinterpret_cast<float4*>(hi);
+    const float4* l4 = reinterpret_cast<const float4*>(lo);
+    for (int64_t i = b * blockDim.x + threadIdx.x; i < n4; i += stride) {
+      const float4 h = h4[i], l = __ldcs(l4 + i);
+      h4[i] = make_float4(h.x + l.x, h.y + l.y, h.z + l.z, h.w + l.w);
+    }
+    i0 = n4 * 4;
+  }
+  for (int64_t i = i0 + b * blockDim.x + threadIdx.x; i < jb.n; i += stride)
+    hi[i] = hi[i] + lo[i];
 }
 
 // Grouped clearing: job j owns blocks [starts[j], starts[j + 1]) and clears its
@@ -886,6 +971,48 @@ int zero_group_run(const ZeroJob* jobs, const int* starts, int njobs, int64_t bl
   cfg.numAttrs = 1;
   return cuda_status(cudaLaunchKernelEx(&cfg, k_zero_group, jobs, starts, njobs),
                      "k_zero_group");
+}
+
+int group_blocks(int64_t n) {
+  const int64_t b = (n + (int64_t)kBlock * 16 - 1) / ((int64_t)kBlock * 16);
+  return (int)(b < 1 ? 1 : (b > 1024 ? 1024 : b));
+}
+
+namespace {
+cudaLaunchConfig_t group_cfg(int64_t blocks, bool pdl, cudaStream_t s,
+                             cudaLaunchAttribute* attr) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)blocks);
+  cfg.blockDim = dim3(kBlock);
+  cfg.stream = s;
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cfg;
+}
+}  // namespace
+
+int absmax_group_run(int dtype, const AbsmaxJob* jobs, const int* starts, int njobs,
+                     int64_t blocks, bool pdl, cudaStream_t s) {
+  if (blocks <= 0) return JUBIK_OK;
+  cudaLaunchAttribute attr[1];
+  const cudaLaunchConfig_t cfg = group_cfg(blocks, pdl, s, attr);
+  return cuda_status(dtype == JUBIK_F32
+                         ? cudaLaunchKernelEx(&cfg, k_absmax_group<float>, jobs, starts, njobs)
+                         : cudaLaunchKernelEx(&cfg, k_absmax_group<double>, jobs, starts, njobs),
+                     "k_absmax_group");
+}
+
+int combine_group_run(int dtype, const CombineJob* jobs, const int* starts, int njobs,
+                      int64_t blocks, bool pdl, cudaStream_t s) {
+  if (blocks <= 0) return JUBIK_OK;
+  cudaLaunchAttribute attr[1];
+  const cudaLaunchConfig_t cfg = group_cfg(blocks, pdl, s, attr);
+  return cuda_status(dtype == JUBIK_F32
+                         ? cudaLaunchKernelEx(&cfg, k_combine_group<float>, jobs, starts, njobs)
+                         : cudaLaunchKernelEx(&cfg, k_combine_group<double>, jobs, starts, njobs),
+                     "k_combine_group");
 }
 
 // --------------------------------------------------------------- host wrappers

@@ -12,6 +12,10 @@ from jubik_gb300 import synthetic
 pytestmark = pytest.mark.gpu
 
 
+def _bits(t):
+    return t.detach().reshape(-1).contiguous().view(torch.uint8).cpu().numpy().tobytes()
+
+
 def rel(a, b):
     a = a.detach().double().cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
@@ -79,6 +83,9 @@ def test_batch_autotune_picks_a_covering_path(cuda, small_batch):
             b.autotune()
         b.set_data([r["data"] for r in refs])
         chosen = b.autotune(reps=2)
+        # run lengths are tuned on the module-shared FP32 plans at FFT side 192
+        for k, times in b.run_timings.items():
+            assert b.plans[k].forward_run == min(times, key=times.get)
         sides = {2 * (i.shape[0] // i.n_patches) + 2 * i.margin for i in insts}
         assert set(chosen) == sides
         assert all(p in ("fused", "fused_unit", "plain") for p in chosen.values())
@@ -103,11 +110,14 @@ def test_grouped_launches_match_per_problem(cuda, small_batch, dtype):
         g0 = [t.clone() for t in g0]
         assert b.group()
         sides = {2 * (i.shape[0] // i.n_patches) + 2 * i.margin for i in insts}
-        assert b.launches_per_pass() == 2 + 2 * len(sides) < 5 * len(insts)
-        # FP32 images are summed with L2 reductions whose order varies between
-        # runs: energies agree to ~1e-9 (observed up to 1.03e-9), far inside 1e-6
+        assert b.launches_per_pass() == 4 + 2 * len(sides) < 5 * len(insts)
+        # exact two-word sums: every grouped pass gives the same bits.  Against
+        # the per-problem pass, the FP32 energy differs by ~1e-9: the grouped
+        # likelihood pass splits each image into other blocks, whose per-thread
+        # compensated FP32 sums round differently
         etol = 1e-13 if dtype == torch.float64 else 1e-8
-        gtol = 1e-13 if dtype == torch.float64 else 2e-5
+        gtol = 1e-13 if dtype == torch.float64 else 1e-6
+        first = None
         for run in ("eager", "graph", "graph again"):
             if run == "graph":
                 b.capture()
@@ -115,6 +125,9 @@ def test_grouped_launches_match_per_problem(cuda, small_batch, dtype):
                 t.fill_(float("nan"))  # the grouped pass clears and fills every gradient
             e, g = b.replay() if run.startswith("graph") else b.energy_and_grad()
             torch.cuda.synchronize()
+            bits = (_bits(e), [_bits(t) for t in g])
+            first = first or bits
+            assert bits == first, run
             for k, r in enumerate(refs):
                 assert abs(float(e[k]) - float(e0[k])) <= etol * abs(float(e0[k])), (run, k)
                 assert rel(g[k], g0[k].double().cpu().numpy()) < gtol, (run, k)
@@ -151,11 +164,16 @@ def test_grouped_module_shared_and_mixed_problems(cuda, dtype):
         g0 = [t.clone() for t in g0]
         assert b.group()
         # classes: (64, shared), (96, shared), (64, per-unit), (96, per-unit)
-        assert b.launches_per_pass() == 2 + 4 + 4 + 2 + 2
-        # FP32 images are summed with L2 reductions whose order varies between
-        # runs: energies agree to ~1e-9 (observed 1.0e-9), far inside the 1e-6 bar
+        assert b.launches_per_pass() == 4 + 4 + 4 + 2 + 2
+        # the same bits on every grouped pass (module sums in module order, exact
+        # two-word sums).  Against the per-problem pass the FP32 energy differs by
+        # the likelihood pass's other block split (~1e-9), and the gradient by the
+        # ordered adjoint's other CTA count: a patch whose modules are split over
+        # two CTAs adds its FP32 partial sums in another grouping (~1e-6 here,
+        # after the cancellation in 1 - d/lam)
         etol = 1e-13 if dtype == torch.float64 else 1e-8
         gtol = 1e-13 if dtype == torch.float64 else 2e-5
+        first = None
         for run in ("eager", "graph", "graph again"):
             if run == "graph":
                 b.capture()
@@ -163,6 +181,9 @@ def test_grouped_module_shared_and_mixed_problems(cuda, dtype):
                 t.fill_(float("nan"))
             e, g = b.replay() if run.startswith("graph") else b.energy_and_grad()
             torch.cuda.synchronize()
+            bits = (_bits(e), [_bits(t) for t in g])
+            first = first or bits
+            assert bits == first, run
             for k, r in enumerate(refs):
                 assert abs(float(e[k]) - float(e0[k])) <= etol * abs(float(e0[k])), (run, k)
                 assert rel(g[k], g0[k].double().cpu().numpy()) < gtol, (run, k)
