@@ -1378,11 +1378,23 @@ int jubik_group_set_io(jubik_group* g, const void* const* x, void* const* grad,
     // proportion to its units (at most its spill slots), about as many in all as
     // the GPU holds at once
     int64_t per_cta = 1;
+    auto ord_ctas = [&](int i) {
+      const jubik_plan* p = g->plans[i];
+      return std::max<int64_t>(
+          1, std::min<int64_t>(p->adj_grid, (p->g.units() + per_cta - 1) / per_cta));
+    };
     if (c.shared) {
       int64_t total = 0;
       for (int i : c.members) total += g->plans[i]->g.units();
       const int64_t cap = std::max<int64_t>(1, fused_ord_capacity(c.P, g->dtype));
       per_cta = std::max<int64_t>(1, (total + cap - 1) / cap);
+      // all ranges in one wave: a CTA that waits for a free SM doubles the critical path
+      for (;;) {
+        int64_t ctas = 0;
+        for (int i : c.members) ctas += ord_ctas(i);
+        if (ctas <= cap || ctas <= (int64_t)c.members.size()) break;
+        ++per_cta;
+      }
     }
     for (size_t k = 0; k < c.members.size(); ++k) {
       const int i = c.members[k];
@@ -1416,8 +1428,7 @@ int jubik_group_set_io(jubik_group* g, const void* const* x, void* const* grad,
       r.bnd_log2 = adj_terms_log2(pg);
       r.bnd_scale = 2.0 * (double)(int64_t(1) << r.bnd_log2) * p->kmax * area;
       if (c.shared) {  // module sums in module order (ordered adjoint, spill slots)
-        const int64_t G = std::max<int64_t>(
-            1, std::min<int64_t>(p->adj_grid, (pg.units() + per_cta - 1) / per_cta));
+        const int64_t G = ord_ctas(i);
         ord_starts.push_back((int)ob);
         ob += G;
         r.spill = p->spill;

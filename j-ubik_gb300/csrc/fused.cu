@@ -2319,16 +2319,35 @@ int fused_fwd_run_len(const Geom& g, int dtype, int requested) {
   return fits && run_geometry(g, requested) ? requested : -1;
 }
 
-// CTAs of the ordered adjoint at FFT side P that the GPU holds at once (0 where
-// the fused path does not cover P).
+// CTAs of the ordered adjoint over a list of problems at FFT side P that the
+// GPU holds at once (0 where the fused path does not cover P).
+template <typename T>
+int64_t ord_list_capacity(int P) {
+  constexpr int64_t kMany = int64_t(1) << 30;  // more than any GPU holds
+  switch (P) {
+    case 32: return loop_grid<T, 32>(k_adj_to_spec_ord_list<T, 32>, kMany, ord_smem_bytes<T, 32>());
+    case 64: return loop_grid<T, 64>(k_adj_to_spec_ord_list<T, 64>, kMany, ord_smem_bytes<T, 64>());
+    case 96: return loop_grid<T, 96>(k_adj_to_spec_ord_list<T, 96>, kMany, ord_smem_bytes<T, 96>());
+    case 128:
+      return loop_grid<T, 128>(k_adj_to_spec_ord_list<T, 128>, kMany, ord_smem_bytes<T, 128>());
+    case 160:
+      if constexpr (sizeof(T) == 4)
+        return loop_grid<T, 160>(k_adj_to_spec_ord_list<T, 160>, kMany, ord_smem_bytes<T, 160>());
+      break;
+    case 192:
+      if constexpr (sizeof(T) == 4)
+        return loop_grid<T, 192>(k_adj_to_spec_ord_list<T, 192>, kMany, ord_smem_bytes<T, 192>());
+      break;
+    default: break;
+  }
+  return 0;
+}
+
 int64_t fused_ord_capacity(int P, int dtype) {
   if (!fused_supported(P, dtype)) return 0;
-  Geom g{};
-  g.P = P;
-  g.M = 1;
-  g.E = 1;
-  g.n = 1 << 15;  // more units than any GPU holds CTAs
-  return fused_adj_grid(g, dtype);
+  if ((dtype == JUBIK_F32 ? ensure_attrs_dispatch<float>(P) : ensure_attrs_dispatch<double>(P)))
+    return 0;
+  return dtype == JUBIK_F32 ? ord_list_capacity<float>(P) : ord_list_capacity<double>(P);
 }
 
 int fused_run(const Geom& g, int dtype, const FusedLaunch& a, int which, cudaStream_t s) {
