@@ -715,6 +715,10 @@ def main():
         err["metric"] = rel(plan.metric(x, vm.float()), m64)
         err["metric_floor_fp32_lambda"] = rel(plan64.response_vjp(plan64.response(vm) / lam_r),
                                               m64)
+        # the FP32 metric with its weights from the FP64 plan's lam (set once per
+        # linearisation point): only the FP32 products' own rounding remains
+        plan.set_metric_lambda(lam64)
+        err["metric_fp64_lambda"] = rel(plan.metric(None, vm.float()), m64)
         # bitwise reproducibility of the FP32 step
         e_a, g_a = plan.energy_and_grad(x)
         e_a, g_a = float(e_a), g_a.clone()

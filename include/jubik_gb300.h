@@ -179,6 +179,18 @@ JUBIK_API int jubik_plan_set_profiling(jubik_plan* plan, int32_t on);
 /* ms and launch counts per phase accumulated since profiling was switched on. */
 JUBIK_API int jubik_plan_profile(const jubik_plan* plan, double* ms, int64_t* launches);
 
+/* Metric weights from a caller's expected counts (no counterpart in the
+ * reference): lam (device, readout order, readout_total values, dtype
+ * JUBIK_F32 or JUBIK_F64) replaces the plan's cached lam for the next
+ * jubik_metric_apply calls with x = NULL; the weights eps^2 / lam are formed in
+ * FP64 and rounded once.  An FP32 plan's own lam carries the FP32 forward's
+ * error, which the metric's 1/lam amplifies at faint pixels; a lam from an FP64
+ * plan, computed once per linearisation point, leaves the FP32 metric products
+ * only their own rounding.  The next energy or metric call with an x replaces
+ * the weights again. */
+JUBIK_API int jubik_plan_set_metric_lambda(jubik_plan* plan, const void* lam, int32_t lam_dtype,
+                                           void* stream);
+
 /* Stand-alone Poisson likelihood on readout vectors (jft.Poissonian(data)):
  * energy (device double[1]) = sum(lam - d log lam); grad (may be NULL) = 1 - d/lam. */
 JUBIK_API int jubik_poisson_energy(const void* lam, const int32_t* data, int64_t n, int32_t dtype,

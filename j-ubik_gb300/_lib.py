@@ -86,6 +86,7 @@ _SIGS = {
     "jubik_dot": ([_vp, _vp, _i64, _i32, _vp, _vp], C.c_int),
     "jubik_plan_set_dependent_launch": ([_vp, _i32], C.c_int),
     "jubik_plan_set_forward_run": ([_vp, _i32], C.c_int),
+    "jubik_plan_set_metric_lambda": ([_vp, _vp, _i32, _vp], C.c_int),
     "jubik_plan_forward_run": ([_vp, _vp], C.c_int),
     "jubik_group_create": ([_vp, _i32, _vp], C.c_int),
     "jubik_group_set_io": ([_vp, _vp, _vp, _vp], C.c_int),

@@ -1126,6 +1126,23 @@ int jubik_metric_apply(jubik_plan* p, const void* x, const void* v, void* out, v
   return finish_words(p, out, p->grad_lo, (int64_t)p->g.E * p->g.pixels(), s);
 }
 
+int jubik_plan_set_metric_lambda(jubik_plan* p, const void* lam, int32_t lam_dtype,
+                                 void* stream) {
+  NvtxRange nvtx_("jubik_plan_set_metric_lambda");
+  JUBIK_TRY(check_plan(p));
+  if (!lam || (lam_dtype != JUBIK_F32 && lam_dtype != JUBIK_F64)) {
+    set_error("set_metric_lambda: need a device lam vector of dtype JUBIK_F32 or JUBIK_F64");
+    return JUBIK_ERR_INVALID_ARGUMENT;
+  }
+  cudaStream_t s = S(stream);
+  const int64_t img = image_elems(p);
+  JUBIK_TRY(p->dtype == JUBIK_F32
+                ? weights_from_lambda<float>(lam, lam_dtype, p->eps, p->ridx, img, p->wts, s)
+                : weights_from_lambda<double>(lam, lam_dtype, p->eps, p->ridx, img, p->wts, s));
+  p->lam_valid = true;
+  return JUBIK_OK;
+}
+
 int jubik_poisson_energy(const void* lam, const int32_t* data, int64_t n, int32_t dtype,
                          double* energy, void* grad, void* stream) {
   NvtxRange nvtx_("jubik_poisson_energy");

@@ -254,6 +254,11 @@ int count_image(const int32_t* ridx, const int32_t* data, int64_t npix, int32_t*
 template <typename T>
 int metric_weights(const void* conv, const void* conv_lo, const void* eps, const int32_t* ridx,
                    int64_t npix, void* wts, cudaStream_t s);
+// The same from a caller's lam in readout order (lam_dtype JUBIK_F32 or
+// JUBIK_F64): w = eps^2 / lam formed in FP64, rounded once to T.
+template <typename T>
+int weights_from_lambda(const void* lam, int lam_dtype, const void* eps, const int32_t* ridx,
+                        int64_t npix, void* wts, cudaStream_t s);
 // out = w * (hi + lo) (lo nullptr: w * hi), n elements; *nb block maxima of
 // |out| at rmax (nullptr: none)
 template <typename T>

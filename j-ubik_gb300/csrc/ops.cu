@@ -875,6 +875,24 @@ __global__ void k_metric_weights(const T* __restrict__ conv, const T* __restrict
   }
 }
 
+// Metric weights from a caller's expected counts in readout order (FP32 or
+// FP64): w = eps^2 / lam on read-out pixels, formed in FP64 and rounded once.
+template <typename T, typename L>
+__global__ void k_weights_from_lambda(const L* __restrict__ lam, const T* __restrict__ eps,
+                                      const int32_t* __restrict__ ridx, int64_t npix,
+                                      T* __restrict__ wts) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < npix;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t r = ridx[p];
+    if (r < 0) {
+      wts[p] = (T)0;
+      continue;
+    }
+    const double ep = eps ? (double)eps[p] : 1.0;
+    wts[p] = (T)((ep * ep) / (double)lam[r]);
+  }
+}
+
 // resid = w * (hi + lo): the weighted image a metric product hands to the
 // adjoint, made in the same pass that adds the two words of R v.
 template <typename T>
@@ -1169,6 +1187,18 @@ int metric_weights(const void* conv, const void* conv_lo, const void* eps, const
 }
 
 template <typename T>
+int weights_from_lambda(const void* lam, int lam_dtype, const void* eps, const int32_t* ridx,
+                        int64_t npix, void* wts, cudaStream_t s) {
+  if (lam_dtype == JUBIK_F64)
+    k_weights_from_lambda<T, double><<<grid_for(npix), kBlock, 0, s>>>(
+        (const double*)lam, (const T*)eps, ridx, npix, (T*)wts);
+  else
+    k_weights_from_lambda<T, float><<<grid_for(npix), kBlock, 0, s>>>(
+        (const float*)lam, (const T*)eps, ridx, npix, (T*)wts);
+  return cuda_status(cudaGetLastError(), "k_weights_from_lambda");
+}
+
+template <typename T>
 int apply_weights(const void* hi, const void* lo, const void* w, int64_t n, void* out, bool pdl,
                   cudaStream_t s, void* rmax, int* nb) {
   const unsigned grid = (unsigned)std::min<int64_t>(
@@ -1360,6 +1390,8 @@ int combine_words(void* hi, const void* lo, int64_t n, bool pdl, cudaStream_t s)
   template int combine_words<T>(void*, const void*, int64_t, bool, cudaStream_t);                \
   template int metric_weights<T>(const void*, const void*, const void*, const int32_t*, int64_t, \
                                  void*, cudaStream_t);                                           \
+  template int weights_from_lambda<T>(const void*, int, const void*, const int32_t*, int64_t,    \
+                                      void*, cudaStream_t);                                      \
   template int apply_weights<T>(const void*, const void*, const void*, int64_t, void*, bool,     \
                                 cudaStream_t, void*, int*);                                      \
   template int poisson_vec<T>(const void*, const int32_t*, int64_t, double*, unsigned int*,      \

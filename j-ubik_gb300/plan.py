@@ -392,6 +392,22 @@ class ResponsePlan:
                   ptr(grad if need_grad else None), self._s())
         return energy, (grad if need_grad else None)
 
+    def set_metric_lambda(self, lam) -> "ResponsePlan":
+        """Take the metric weights eps^2/lam from ``lam`` (expected counts in
+        readout order, float32 or float64; e.g. the response of a float64 plan of
+        the same instrument) for the next ``metric(None, v)`` calls.  An FP32
+        plan's own lam carries the FP32 forward's error, which 1/lam amplifies at
+        faint pixels; a float64 lam leaves the FP32 metric only its own rounding."""
+        t = lam if isinstance(lam, torch.Tensor) else torch.as_tensor(np.asarray(lam))
+        if t.dtype not in (torch.float32, torch.float64):
+            t = t.to(torch.float64)
+        t = t.to(self.device).contiguous().reshape(-1)
+        if t.numel() != self.readout_total:
+            raise ValueError("lam size does not match the readout")
+        self._metric_lam = t  # read by a kernel queued on the current stream
+        _lib.call("jubik_plan_set_metric_lambda", self._h, ptr(t), dtype_code(t.dtype), self._s())
+        return self
+
     def metric(self, x, v, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         """R^T diag(1/lam) R v with lam = R(x); x=None reuses the last lam."""
         xx = None if x is None else self._sky(x)

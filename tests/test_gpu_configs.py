@@ -247,6 +247,11 @@ def test_benchmark_workload_properties(cuda, bench_case):
                                   inst.margin, precut=True)
         assert rel(img64[0, 0], ref[0]) < 1e-12
         assert rel(img32[0, 0], ref[0]) < 1e-6
+        # the metric product at the workload's size: FP32 with the FP64 plan's lam
+        t = torch.as_tensor(rng.normal(size=inst.sky.shape), device=cuda)
+        m64 = p64.metric(x, t)
+        p32.set_metric_lambda(p64.response(x))
+        assert rel(p32.metric(None, t.float()), m64.double().cpu().numpy()) < 1e-6
     finally:
         p32.close()
         p64.close()
@@ -309,3 +314,28 @@ def test_fp32_gradient_and_metric_errors_come_from_the_fp32_forward(cuda, deriv_
         assert em <= m_lam + 1e-6
     finally:
         plan.close()
+
+
+def test_fp32_metric_with_fp64_lambda_meets_1e6(cuda, deriv_case):
+    """The metric weights 1/lam taken from a float64 plan's lam (once per
+    linearisation point) leave the FP32 metric product only its own rounding."""
+    c = deriv_case
+    inst = c["inst"]
+    p32 = make_plan(inst, F32)
+    p64 = make_plan(inst, F64, path="plain")
+    try:
+        lam64 = p64.response(inst.sky)
+        p32.set_metric_lambda(lam64)
+        m = p32.metric(None, c["t"])
+        em = rel(m, c["metric"])
+        own = rel(p32.metric(inst.sky, c["t"]), c["metric"])  # weights from the FP32 lam
+        print(f"FP32 metric: FP64 lam {em:.3e}, own FP32 lam {own:.3e}")
+        assert em < 1e-6
+        # a float32 copy of the float64 lam works the same
+        p32.set_metric_lambda(lam64.float())
+        assert rel(p32.metric(None, c["t"]), c["metric"]) < 1e-6
+        with pytest.raises(ValueError):
+            p32.set_metric_lambda(lam64[:-1])
+    finally:
+        p32.close()
+        p64.close()
