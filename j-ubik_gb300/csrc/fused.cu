@@ -660,8 +660,8 @@ __device__ __forceinline__ void stage_split(Unit<T, P>& U) {
 }
 
 // ---- column phase 1 (variant A forward): items (c, n2), DFT-L1 over n1;
-// rows outside [ylo, yhi) are known zeros
-template <typename T, int P>
+// rows outside [ylo, yhi) are known zeros (FULL: none are)
+template <typename T, int P, bool FULL = false>
 __device__ __forceinline__ void stage_col1(Unit<T, P>& U, int ylo, int yhi) {
   using R = Tr<T, P>;
   constexpr int L1 = R::L1, H = R::H, NT = R::NT;
@@ -672,7 +672,7 @@ __device__ __forceinline__ void stage_col1(Unit<T, P>& U, int ylo, int yhi) {
 #pragma unroll
     for (int i = 0; i < L1; ++i) {
       const int y = n2 + 16 * i;
-      v[i] = (y >= ylo && y < yhi) ? base[8 * i * (P + 1)] : mkc<T>((T)0, (T)0);
+      v[i] = (FULL || (y >= ylo && y < yhi)) ? base[8 * i * (P + 1)] : mkc<T>((T)0, (T)0);
     }
     Dft<L1, false, T>::run(v);
 #pragma unroll
@@ -1723,7 +1723,7 @@ __device__ __forceinline__ void ord_adjoint(const Args& a, int64_t b, int64_t G,
     stage_input<T, P, true>(U, a, pre);
     stage_split<T, P>(U);
     __syncthreads();
-    stage_col1<T, P>(U, 0, P);
+    stage_col1<T, P, true>(U, 0, P);
     __syncthreads();
     OrdCursor nx = cur;
     nx.advance(sch, b, tlo);
@@ -1815,6 +1815,13 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_from_spec(Src src) {
     U.nsp = n;
   }
   pdl_wait();
+  // the module sum (written by the previous kernel, mostly evicted from L2 by its
+  // PSF stream) is read in three rounds of loads: fetch all of it into L2 at once
+  if (threadIdx.x == 0) {
+    prefetch_l2(U.spec, sizeof(cx<T>) * P * R::H);
+    for (int j = 0; j < U.nsp; ++j)
+      prefetch_l2(U.sp0 + (int64_t)j * (P * R::H), sizeof(cx<T>) * P * R::H);
+  }
   const Split2<T> sp = output_splitter<T>(a, &s_slot);  // the gradient is exact in two words
   stage_mid<T, P, MID_FROM_ACC, true>(U);
   __syncthreads();
