@@ -159,15 +159,6 @@ __device__ __forceinline__ void red_add_v4(float* p, float a, float b, float c, 
                : "memory");
 }
 
-__device__ __forceinline__ void red_add_v2(float* p, float a, float b) {
-  asm volatile("red.global.add.v2.f32 [%0], {%1,%2};" ::"l"(p), "f"(a), "f"(b) : "memory");
-}
-__device__ __forceinline__ void red_add_cx(float2* p, float2 v) { red_add_v2((float*)p, v.x, v.y); }
-__device__ __forceinline__ void red_add_cx(double2* p, double2 v) {
-  atomicAdd(&p->x, v.x);
-  atomicAdd(&p->y, v.y);
-}
-
 // ---- exact, order-independent accumulation in two words
 // Atomic reductions add in whatever order the patches arrive, and floating
 // point addition rounds differently in different orders.  Each term v of an
@@ -681,7 +672,7 @@ __device__ __forceinline__ void stage_col1(Unit<T, P>& U, int ylo, int yhi) {
 }
 
 // ---- column phase 2 (class k1 = warp): the spectrum-side step
-enum Mid { MID_FULL, MID_TO_SPEC, MID_FROM_SPEC, MID_TO_ACC, MID_FROM_ACC };
+enum Mid { MID_FULL, MID_TO_SPEC, MID_FROM_SPEC, MID_FROM_ACC };
 
 template <typename T, int P, int MODE, bool ADJ>
 __device__ __forceinline__ void stage_mid(Unit<T, P>& U) {
@@ -690,9 +681,9 @@ __device__ __forceinline__ void stage_mid(Unit<T, P>& U) {
   for (int c = U.lane; c < H; c += 32) {
     cx<T> v[16];
     cx<T> hv[16];
-    const bool prod = MODE == MID_FULL || MODE == MID_FROM_SPEC || MODE == MID_TO_ACC;
+    const bool prod = MODE == MID_FULL || MODE == MID_FROM_SPEC;
     // column 0 carries the packed kx = 0 / kx = P/2 columns: alpha / beta products
-    const bool col0 = c == 0 && (MODE == MID_FROM_SPEC || MODE == MID_TO_ACC);
+    const bool col0 = c == 0 && MODE == MID_FROM_SPEC;
     if (prod && (c != 0 || col0)) {
 #pragma unroll
       for (int q = 0; q < 16; ++q) hv[q] = ldg2(U.hmain + (16 * cls + q) * H + c);
@@ -732,26 +723,9 @@ __device__ __forceinline__ void stage_mid(Unit<T, P>& U) {
         const cx<T> be = ldg2(U.hnyq + 16 * cls + q);
         v[q] = cadd<T>(cmul<T>(v[q], hv[q]), cmul<T>(cconj<T>(wm), be));
       }
-    } else if (col0 && MODE == MID_TO_ACC) {
-      // scatter form of the conjugate product: W(ky) adds conj(alpha(ky)) W(ky) to
-      // ky and conj(beta(-ky)) conj(W(ky)) to -ky
-#pragma unroll
-      for (int q = 0; q < 16; ++q) {
-        const int ky = cls + L1 * q, km = (P - ky) % P;
-        const int sm = 16 * (km % L1) + km / L1;
-        const cx<T> bm = ldg2(U.hnyq + sm);
-        red_add_cx(U.spec + (16 * cls + q) * H, cmulc<T>(v[q], hv[q]));
-        red_add_cx(U.spec + sm * H, cconj<T>(cmul<T>(v[q], bm)));
-      }
-      continue;
     } else if (prod && c != 0) {
 #pragma unroll
       for (int q = 0; q < 16; ++q) v[q] = ADJ ? cmulc<T>(v[q], hv[q]) : cmul<T>(v[q], hv[q]);
-    }
-    if (MODE == MID_TO_ACC) {
-#pragma unroll
-      for (int q = 0; q < 16; ++q) red_add_cx(U.spec + (16 * cls + q) * H + c, v[q]);
-      continue;
     }
     // inverse variant-B step A; in MID_FULL column 0 waits for its product (stage_col0)
     if (c != 0 || MODE != MID_FULL) {
@@ -1579,63 +1553,6 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_fwd_run(Args a, int items) {
   if (U.warp == 0) tmem_dealloc(tbase, 2 * kRunCols <= 256 ? 256 : 512);
 }
 
-// Adjoint, module-shared, over a list of problems: per unit, cotangent spectrum
-// * conj(PSF spectrum) added into the patch's (zero) accumulator by L2
-// reductions ...
-// A loop over units: CTA b takes units b, b + G, b + 2G, ... (G = gridDim.x,
-// as many CTAs as fit on the GPU at once; one per SM at P = 192).  The next unit's first input chunk is issued into the
-// staging area before this unit's spectrum stage, which leaves the staging
-// area alone: those loads overlap the stage instead of opening the next unit.
-// The next unit's PSF spectrum is prefetched into L2 only once this unit is
-// done (earlier, it competes with this unit's spectrum loads).
-template <typename T, int P, typename Src>
-__global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_to_spec(Src src, int units) {
-  using R = Tr<T, P>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  Unit<T, P> U;
-  pdl_trigger();
-  int g = blockIdx.x;
-  {
-    int lu;
-    U.init(src.at(g, lu), smem_raw, true, lu);
-  }
-  prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
-  pdl_wait();
-  {
-    int lu;
-    const Args& a = src.at(g, lu);
-    if (a.zero_out)
-      zero_slice(a.out, (int64_t)a.E * a.nx * a.ny * (int64_t)sizeof(T), a.zchunk);
-  }
-  bool pre = false;
-  for (;;) {
-    {
-      int lu;
-      stage_input<T, P, true>(U, src.at(g, lu), pre);
-    }
-    stage_split<T, P>(U);
-    __syncthreads();
-    stage_col1<T, P>(U, 0, P);
-    __syncthreads();
-    const int gn = g + (int)gridDim.x;
-    if (gn < units) {
-      int lun;
-      const Args& an = src.at(gn, lun);
-      Unit<T, P> N;
-      N.geom(an, smem_raw, true, lun);
-      input_issue<T, P, true>(N, an, InChunks<T, P, true>(N), 0);
-    }
-    stage_mid<T, P, MID_TO_ACC, true>(U);
-    if (gn >= units) break;
-    __syncthreads();  // the tile's last reads before the next unit's input stage writes it
-    g = gn;
-    int lu;
-    U.geom(src.at(g, lu), smem_raw, true, lu);
-    prefetch_unit(U.hmain, sizeof(cx<T>) * P * R::H, U.hnyq, sizeof(cx<T>) * P);
-    pre = true;
-  }
-}
-
 // Shared memory of the ordered adjoint beyond the tile: column 0's two terms
 // and running sum (3 P complex values).
 template <typename T, int P>
@@ -1784,8 +1701,7 @@ __global__ void __launch_bounds__(Tr<T, P>::NT)
 // ... then, per (energy, patch), one inverse transform -> window -> gradient:
 // the patch's module sum plus the continuing CTAs' spill slots (in CTA order),
 // and the gradient accumulates exactly in two words (each problem with its own
-// bound).  Without spill slots the accumulator was summed by reductions, and it
-// is cleared as it is read.
+// bound).
 template <typename T, int P, typename Src>
 __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_from_spec(Src src) {
   using R = Tr<T, P>;
@@ -1796,10 +1712,7 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_from_spec(Src src) {
   int item;
   const Args& a = src.at((int)blockIdx.x, item);
   U.init(a, smem_raw, false, item);
-  // the module sums come from the ordered adjoint (spill slots set) or, in a
-  // list of problems without it, from reductions into a cleared accumulator
-  const bool ordered = a.spill != nullptr;
-  if (ordered) {
+  {  // the module sums of the ordered adjoint: this patch's plus any spill slots
     // CTAs of the ordered adjoint whose tail range starts inside this patch:
     // tail_lo(b) in (u0, u0 + M) (none for the patches of the full rounds)
     const int64_t G = a.loop_grid, patches = (int64_t)a.E * a.n * a.n;
@@ -1830,12 +1743,6 @@ __global__ void __launch_bounds__(Tr<T, P>::NT) k_adj_from_spec(Src src) {
   stage_combine<T, P>(U, U.mg / 2, (U.mg + U.K + 1) / 2);
   __syncthreads();
   stage_output<T, P, true, true>(U, a, sp);
-  if (!ordered) {
-    // leave this patch's accumulator zero for the next call (read in the first stage)
-    float4* z = reinterpret_cast<float4*>(U.spec);
-    constexpr int n16 = (int)(sizeof(cx<T>) * P * R::H / 16);
-    for (int i = threadIdx.x; i < n16; i += R::NT) z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-  }
 }
 
 template <typename KernelT>
@@ -1975,7 +1882,6 @@ int ensure_smem_attrs() {
     JUBIK_TRY(set_smem(k_fwd_from_spec<T, P, OneProblem>, smem));
     JUBIK_TRY(set_smem(k_sky_spec<T, P, ProblemList>, smem));
     JUBIK_TRY(set_smem(k_adj_from_spec<T, P, ProblemList>, smem));
-    JUBIK_TRY(set_smem(k_adj_to_spec<T, P, ProblemList>, smem));
     JUBIK_TRY(set_smem(k_fwd_from_spec<T, P, ProblemList>, smem));
     JUBIK_TRY(set_smem(k_adj_to_spec_ord<T, P>, ord_smem_bytes<T, P>()));
     JUBIK_TRY(set_smem(k_adj_to_spec_ord_list<T, P>, ord_smem_bytes<T, P>()));
