@@ -55,12 +55,13 @@ def parse():
                     help="skip the FP64 comparison and the CPU baseline")
     ap.add_argument("--profile-only", action="store_true",
                     help="one warm-up and two steps (for a launch list under a profiler)")
-    ap.add_argument("--leg", choices=["step", "sky", "batch", "fp64", "psf", "sampling"],
+    ap.add_argument("--leg", choices=["step", "sky", "batch", "fp64", "psf", "sampling", "p384"],
                     default="step",
                     help="with --profile-only: the response step, the correlated-field sky "
                          "(log-sky and VJP), the grouped uneven batch, the FP64 unfused step, "
-                         "the PSF-patch interpolation, or the sampling kernels (FP64 dot "
-                         "products, Poisson draws)")
+                         "the PSF-patch interpolation, the sampling kernels (dot products, "
+                         "Poisson draws), or the FP32 step at FFT side 384 (1024^2 x 7 x 3, "
+                         "8 x 8 patches, margin 64: the unfused path)")
     return ap.parse_args()
 
 
@@ -453,6 +454,27 @@ def profile_psf_leg(dev, nx, passes=2):
     torch.cuda.synchronize()
 
 
+def profile_p384_leg(dev, passes=2):
+    """The FP32 energy+gradient step at FFT side 384 (1024^2 x 7 modules x 3
+    energies, 8 x 8 patches of stride 128, margin 64), which the fused tile does
+    not hold: the unfused path, ``passes`` times."""
+    import torch
+
+    import jubik_gb300 as ju
+    from jubik_gb300 import synthetic
+    inst = synthetic.config2(nx=1024, dx=128, margin=64, dtype=np.float32)
+    plan = ju.ResponsePlan(inst.n_modules, inst.n_energies, inst.shape, inst.n_patches,
+                           inst.margin, dtype=torch.float32, device=dev)
+    plan.set_psf(inst.psf)
+    plan.set_exposure(inst.exposure, inst.readmask)
+    x = torch.as_tensor(inst.sky, device=dev)
+    plan.set_data(synthetic.poisson_data(plan.response(x).double().cpu().numpy(), seed=1))
+    for _ in range(passes):
+        plan.energy_and_grad(x)
+    torch.cuda.synchronize()
+    plan.close()
+
+
 def ju_domain(shape, distances):
     import jubik_gb300 as ju
     return ju.Domain(shape, distances)
@@ -520,6 +542,8 @@ def main():
             profile_psf_leg(dev, nx)
         elif args.leg == "sampling":
             profile_sampling_leg(dev, plan.response(x))
+        elif args.leg == "p384":
+            profile_p384_leg(dev)
         else:
             step()
             step()

@@ -140,73 +140,101 @@ __global__ void k_spectra_store(const double2* __restrict__ buf, int P, int64_t 
 // both real results as its real and imaginary parts.
 // PSF spectrum value at flat frequency index rem of unit hu, from the stored
 // half plane kx <= P/2 (the spectrum of a real kernel is Hermitian).
-template <typename T>
-__device__ __forceinline__ cx<T> h_at(const cx<T>* __restrict__ hh, int64_t hu, int64_t rem,
-                                      int P) {
-  const int H1 = P / 2 + 1;
-  const int ky = (int)(rem / P), kx = (int)(rem - (int64_t)ky * P);
-  if (kx < H1) return hh[(hu * P + ky) * H1 + kx];
-  return cconj<T>(hh[(hu * P + (P - ky) % P) * H1 + (P - kx)]);
+
+// The unfused path's element-wise kernels run on 3-D grids -- z: a unit pair or
+// an image plane, y: a row, x: the threads along it -- so that no element
+// index is divided back into its coordinates.  Every element is computed with
+// the same operations, in the same order, as a flat index would give.
+constexpr int kRowBlock = 128;
+constexpr int kRowsPerBlock = 8;  // rows a block takes (every gridDim.y-th): fewer, fuller blocks
+
+inline dim3 row_grid(int64_t Z, int64_t Y, int64_t X) {
+  return dim3((unsigned)std::min<int64_t>(64, std::max<int64_t>(1, (X + kRowBlock - 1) / kRowBlock)),
+              (unsigned)std::min<int64_t>(
+                  65535, std::max<int64_t>(1, (Y + kRowsPerBlock - 1) / kRowsPerBlock)),
+              (unsigned)std::min<int64_t>(65535, std::max<int64_t>(1, Z)));
 }
 
-__device__ __forceinline__ int64_t mirror_index(int64_t rem, int P) {
-  const int ky = (int)(rem / P), kx = (int)(rem - (int64_t)ky * P);
-  return (int64_t)((P - ky) % P) * P + (P - kx) % P;
-}
+#define JUBIK_FOR_Z(var_, n_) for (int64_t var_ = blockIdx.z; var_ < (n_); var_ += gridDim.z)
+#define JUBIK_FOR_Y(var_, n_) \
+  for (int var_ = (int)blockIdx.y; var_ < (n_); var_ += (int)gridDim.y)
+#define JUBIK_FOR_X(var_, n_)                                                  \
+  for (int var_ = (int)(blockIdx.x * blockDim.x + threadIdx.x); var_ < (n_); \
+       var_ += (int)(gridDim.x * blockDim.x))
 
 template <typename T>
-__global__ void k_plain_sky_patches(const T* __restrict__ x, const T* __restrict__ wt, int E,
-                                    int n, int nx, int ny, int dx, int margin, int half,
-                                    int sr_max, int sc_max, int P, cx<T>* __restrict__ zs) {
+__global__ void __launch_bounds__(kRowBlock)
+    k_plain_sky_patches(const T* __restrict__ x, const T* __restrict__ wt, int E, int n, int nx,
+                        int ny, int dx, int margin, int half, int sr_max, int sc_max, int P,
+                        cx<T>* __restrict__ zs) {
   const int n2p = n * n;
   const int np = E * n2p, nph = (np + 1) / 2;
-  const int64_t total = (int64_t)nph * P * P;
   const int K = 2 * dx;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t j = i / ((int64_t)P * P);
-    const int rem = (int)(i - j * P * P);
-    const int y = rem / P, xx = rem % P;
-    T v[2] = {(T)0, (T)0};
-    for (int part = 0; part < 2; ++part) {
+  JUBIK_FOR_Z(j, nph) {
+    bool ok[2];
+    int e2[2], rb[2], cb[2];
+    for (int part = 0; part < 2; ++part) {  // the pair's two patches
       const int p = (int)(2 * j + part);
-      if (p >= np) break;
-      const int k = p % n2p, e = p / n2p;
-      const int rb = img_row_base(k % n, dx, sr_max, half, margin);
-      const int cb = img_row_base(k / n, dx, sc_max, half, margin);
-      const int ya = y - margin, xa = xx - margin, row = rb + y, col = cb + xx;
-      if (ya >= 0 && ya < K && xa >= 0 && xa < K && row >= 0 && row < nx && col >= 0 &&
-          col < ny)
-        v[part] = (wt[ya] * wt[xa]) * x[((int64_t)e * nx + row) * ny + col];
+      ok[part] = p < np;
+      const int k = ok[part] ? p % n2p : 0;
+      e2[part] = ok[part] ? p / n2p : 0;
+      rb[part] = img_row_base(k % n, dx, sr_max, half, margin);
+      cb[part] = img_row_base(k / n, dx, sc_max, half, margin);
     }
-    zs[i] = mkc<T>(v[0], v[1]);
+    JUBIK_FOR_Y(y, P) {
+      const int ya = y - margin;
+      cx<T>* __restrict__ zrow = zs + (j * P + y) * (int64_t)P;
+      JUBIK_FOR_X(xx, P) {
+        T v[2] = {(T)0, (T)0};
+        for (int part = 0; part < 2; ++part) {
+          if (!ok[part]) break;
+          const int xa = xx - margin, row = rb[part] + y, col = cb[part] + xx;
+          if (ya >= 0 && ya < K && xa >= 0 && xa < K && row >= 0 && row < nx && col >= 0 &&
+              col < ny)
+            v[part] = (wt[ya] * wt[xa]) * x[((int64_t)e2[part] * nx + row) * ny + col];
+        }
+        zrow[xx] = mkc<T>(v[0], v[1]);
+      }
+    }
   }
 }
 
+// H at spectrum position (ky, kx) of unit hu from the Hermitian half plane
+// (kx <= P/2); kym = (P - ky) mod P
 template <typename T>
-__global__ void k_plain_mul_modules(const cx<T>* __restrict__ zs, const cx<T>* __restrict__ hfull,
-                                    int m0, int nm, int E, int n2p, int P,
-                                    cx<T>* __restrict__ zu) {
+__device__ __forceinline__ cx<T> h_row(const cx<T>* __restrict__ hh, int64_t hu, int ky, int kym,
+                                       int kx, int P) {
+  const int H1 = P / 2 + 1;
+  if (kx < H1) return hh[(hu * P + ky) * H1 + kx];
+  return cconj<T>(hh[(hu * P + kym) * H1 + (P - kx)]);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRowBlock)
+    k_plain_mul_modules(const cx<T>* __restrict__ zs, const cx<T>* __restrict__ hfull, int m0,
+                        int nm, int E, int n2p, int P, cx<T>* __restrict__ zu) {
   const int64_t pp = (int64_t)P * P;
   const int np = E * n2p, nph = (np + 1) / 2;
-  const int64_t total = (int64_t)nm * nph * pp;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t up = i / pp;
-    const int64_t rem = i - up * pp;
+  JUBIK_FOR_Z(up, (int64_t)nm * nph) {
     const int64_t j = up % nph;
     const int m = m0 + (int)(up / nph);
-    const cx<T> z = zs[j * pp + rem], zm = cconj<T>(zs[j * pp + mirror_index(rem, P)]);
-    const cx<T> a = cscale<T>(cadd<T>(z, zm), (T)0.5);   // spectrum of patch 2j
-    const cx<T> ib = cscale<T>(csub<T>(z, zm), (T)0.5);  // i x spectrum of patch 2j + 1
     const int pa = (int)(2 * j), pb = pa + 1;
     const int64_t ha = ((int64_t)m * n2p + pa % n2p) * E + pa / n2p;
-    cx<T> w = cmul<T>(a, h_at<T>(hfull, ha, rem, P));
-    if (pb < np) {
-      const int64_t hb = ((int64_t)m * n2p + pb % n2p) * E + pb / n2p;
-      w = cadd<T>(w, cmul<T>(ib, h_at<T>(hfull, hb, rem, P)));
+    const int64_t hb = pb < np ? ((int64_t)m * n2p + pb % n2p) * E + pb / n2p : 0;
+    const cx<T>* __restrict__ zj = zs + j * pp;
+    JUBIK_FOR_Y(ky, P) {
+      const int kym = ky == 0 ? 0 : P - ky;
+      cx<T>* __restrict__ zrow = zu + up * pp + (int64_t)ky * P;
+      JUBIK_FOR_X(kx, P) {
+        const int kxm = kx == 0 ? 0 : P - kx;
+        const cx<T> z = zj[(int64_t)ky * P + kx], zm = cconj<T>(zj[(int64_t)kym * P + kxm]);
+        const cx<T> a = cscale<T>(cadd<T>(z, zm), (T)0.5);   // spectrum of patch 2j
+        const cx<T> ib = cscale<T>(csub<T>(z, zm), (T)0.5);  // i x spectrum of patch 2j + 1
+        cx<T> w = cmul<T>(a, h_row<T>(hfull, ha, ky, kym, kx, P));
+        if (pb < np) w = cadd<T>(w, cmul<T>(ib, h_row<T>(hfull, hb, ky, kym, kx, P)));
+        zrow[kx] = w;
+      }
     }
-    zu[i] = w;
   }
 }
 
@@ -214,154 +242,169 @@ __global__ void k_plain_mul_modules(const cx<T>* __restrict__ zs, const cx<T>* _
 // every output pixel sums the <= 9 patch outputs that cover it, in patch
 // order, with Kahan compensation.
 template <typename T>
-__global__ void k_plain_overlap_gather(const cx<T>* __restrict__ zu, int m0, int nm, int E,
-                                       int n, int nx, int ny, int dx, int margin, int half,
-                                       int sr_max, int sc_max, int P, T scale,
-                                       T* __restrict__ out) {
+__global__ void __launch_bounds__(kRowBlock)
+    k_plain_overlap_gather(const cx<T>* __restrict__ zu, int m0, int nm, int E, int n, int nx,
+                           int ny, int dx, int margin, int half, int sr_max, int sc_max, int P,
+                           T scale, T* __restrict__ out) {
   const int n2p = n * n;
   const int nph = (E * n2p + 1) / 2;
   const int64_t pp = (int64_t)P * P;
-  const int64_t total = (int64_t)nm * E * nx * ny;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int c = (int)(i % ny);
-    const int64_t t = i / ny;
-    const int r = (int)(t % nx);
-    const int64_t me = t / nx;  // (m - m0) * E + e
+  JUBIK_FOR_Z(me, (int64_t)nm * E) {  // (m - m0) * E + e
     const int64_t mm = me / E;
     const int e = (int)(me % E);
-    const int tr = r + half + margin, tc = c + half + margin;
-    const int ri_hi = min(n - 1, tr / dx), ci_hi = min(n - 1, tc / dx);
-    const int ri_lo = tr - P + 1 <= 0 ? 0 : (tr - P + 1 + dx - 1) / dx;
-    const int ci_lo = tc - P + 1 <= 0 ? 0 : (tc - P + 1 + dx - 1) / dx;
-    T s = (T)0, comp = (T)0;
-    auto visit = [&](int pi, int pj) {
-      const int rb = img_row_base(pi, dx, sr_max, half, margin);
-      const int cb = img_row_base(pj, dx, sc_max, half, margin);
-      const int y = r - rb, xx = c - cb;
-      if (y < 0 || y >= P || xx < 0 || xx >= P) return;
-      const int p = e * n2p + pj * n + pi;
-      const cx<T> z = zu[(mm * nph + (p >> 1)) * pp + (int64_t)y * P + xx];
-      const T v = (p & 1) ? z.y : z.x;
-      const T yk = v - comp;
-      const T tt = s + yk;
-      comp = (tt - s) - yk;
-      s = tt;
-    };
-    for (int pj = ci_lo; pj <= ci_hi; ++pj) {
-      for (int pi = ri_lo; pi <= ri_hi; ++pi) visit(pi, pj);
-      if (ri_hi < n - 1) visit(n - 1, pj);
-    }
-    if (ci_hi < n - 1) {
-      for (int pi = ri_lo; pi <= ri_hi; ++pi) visit(pi, n - 1);
-      if (ri_hi < n - 1) visit(n - 1, n - 1);
-    }
     const int64_t m = m0 + mm;
-    out[((m * E + e) * nx + r) * (int64_t)ny + c] = scale * s;
+    JUBIK_FOR_Y(r, nx) {
+      const int tr = r + half + margin;
+      const int ri_hi = min(n - 1, tr / dx);
+      const int ri_lo = tr - P + 1 <= 0 ? 0 : (tr - P + 1 + dx - 1) / dx;
+      T* __restrict__ orow = out + ((m * E + e) * nx + r) * (int64_t)ny;
+      JUBIK_FOR_X(c, ny) {
+        const int tc = c + half + margin;
+        const int ci_hi = min(n - 1, tc / dx);
+        const int ci_lo = tc - P + 1 <= 0 ? 0 : (tc - P + 1 + dx - 1) / dx;
+        T s = (T)0, comp = (T)0;
+        auto visit = [&](int pi, int pj) {
+          const int rb = img_row_base(pi, dx, sr_max, half, margin);
+          const int cb = img_row_base(pj, dx, sc_max, half, margin);
+          const int y = r - rb, xx = c - cb;
+          if (y < 0 || y >= P || xx < 0 || xx >= P) return;
+          const int p = e * n2p + pj * n + pi;
+          const cx<T> z = zu[(mm * nph + (p >> 1)) * pp + (int64_t)y * P + xx];
+          const T v = (p & 1) ? z.y : z.x;
+          const T yk = v - comp;
+          const T tt = s + yk;
+          comp = (tt - s) - yk;
+          s = tt;
+        };
+        for (int pj = ci_lo; pj <= ci_hi; ++pj) {
+          for (int pi = ri_lo; pi <= ri_hi; ++pi) visit(pi, pj);
+          if (ri_hi < n - 1) visit(n - 1, pj);
+        }
+        if (ci_hi < n - 1) {
+          for (int pi = ri_lo; pi <= ri_hi; ++pi) visit(pi, n - 1);
+          if (ri_hi < n - 1) visit(n - 1, n - 1);
+        }
+        orow[c] = scale * s;
+      }
+    }
   }
 }
 
 template <typename T>
-__global__ void k_plain_cot_patches(const T* __restrict__ cot, int m0, int nm, int E, int n,
-                                    int nx, int ny, int dx, int margin, int half, int sr_max,
-                                    int sc_max, int P, cx<T>* __restrict__ zu) {
+__global__ void __launch_bounds__(kRowBlock)
+    k_plain_cot_patches(const T* __restrict__ cot, int m0, int nm, int E, int n, int nx, int ny,
+                        int dx, int margin, int half, int sr_max, int sc_max, int P,
+                        cx<T>* __restrict__ zu) {
   const int n2p = n * n;
   const int np = E * n2p, nph = (np + 1) / 2;
   const int64_t pp = (int64_t)P * P;
-  const int64_t total = (int64_t)nm * nph * pp;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t up = i / pp;
-    const int rem = (int)(i - up * pp);
-    const int y = rem / P, xx = rem % P;
+  JUBIK_FOR_Z(up, (int64_t)nm * nph) {
     const int64_t j = up % nph;
     const int64_t m = m0 + up / nph;
-    T v[2] = {(T)0, (T)0};
+    bool ok[2];
+    int e2[2], rb[2], cb[2];
     for (int part = 0; part < 2; ++part) {
       const int p = (int)(2 * j + part);
-      if (p >= np) break;
-      const int k = p % n2p, e = p / n2p;
-      const int rb = img_row_base(k % n, dx, sr_max, half, margin);
-      const int cb = img_row_base(k / n, dx, sc_max, half, margin);
-      const int row = rb + y, col = cb + xx;
-      if (row >= 0 && row < nx && col >= 0 && col < ny)
-        v[part] = cot[((m * E + e) * nx + row) * (int64_t)ny + col];
+      ok[part] = p < np;
+      const int k = ok[part] ? p % n2p : 0;
+      e2[part] = ok[part] ? p / n2p : 0;
+      rb[part] = img_row_base(k % n, dx, sr_max, half, margin);
+      cb[part] = img_row_base(k / n, dx, sc_max, half, margin);
     }
-    zu[i] = mkc<T>(v[0], v[1]);
-  }
-}
-
-template <typename T>
-__global__ void k_plain_mulconj_accum(const cx<T>* __restrict__ zu, const cx<T>* __restrict__ hfull,
-                                      int m0, int nm, int E, int n2p, int P, int first,
-                                      cx<T>* __restrict__ zs) {
-  const int64_t pp = (int64_t)P * P;
-  const int np = E * n2p, nph = (np + 1) / 2;
-  const int64_t total = (int64_t)nph * pp;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t j = i / pp;
-    const int64_t rem = i - j * pp;
-    const int64_t mrem = mirror_index(rem, P);
-    const int pa = (int)(2 * j), pb = pa + 1;
-    cx<T> acc = first ? mkc<T>((T)0, (T)0) : zs[i];
-    for (int mm = 0; mm < nm; ++mm) {
-      const int64_t base = ((int64_t)mm * nph + j) * pp;
-      const cx<T> z = zu[base + rem], zm = cconj<T>(zu[base + mrem]);
-      const cx<T> a = cscale<T>(cadd<T>(z, zm), (T)0.5);
-      const cx<T> ib = cscale<T>(csub<T>(z, zm), (T)0.5);
-      const int64_t ha = ((int64_t)(m0 + mm) * n2p + pa % n2p) * E + pa / n2p;
-      acc = cadd<T>(acc, cmulc<T>(a, h_at<T>(hfull, ha, rem, P)));
-      if (pb < np) {
-        const int64_t hb = ((int64_t)(m0 + mm) * n2p + pb % n2p) * E + pb / n2p;
-        acc = cadd<T>(acc, cmulc<T>(ib, h_at<T>(hfull, hb, rem, P)));
+    JUBIK_FOR_Y(y, P) {
+      cx<T>* __restrict__ zrow = zu + up * pp + (int64_t)y * P;
+      JUBIK_FOR_X(xx, P) {
+        T v[2] = {(T)0, (T)0};
+        for (int part = 0; part < 2; ++part) {
+          if (!ok[part]) break;
+          const int row = rb[part] + y, col = cb[part] + xx;
+          if (row >= 0 && row < nx && col >= 0 && col < ny)
+            v[part] = cot[((m * E + e2[part]) * nx + row) * (int64_t)ny + col];
+        }
+        zrow[xx] = mkc<T>(v[0], v[1]);
       }
     }
-    zs[i] = acc;
   }
 }
 
 template <typename T>
-__global__ void k_plain_grad_gather(const cx<T>* __restrict__ zs, const T* __restrict__ wt, int E,
-                                    int n, int nx, int ny, int dx, int margin, int half,
-                                    int sr_max, int sc_max, int P, T scale, T* __restrict__ out) {
+__global__ void __launch_bounds__(kRowBlock)
+    k_plain_mulconj_accum(const cx<T>* __restrict__ zu, const cx<T>* __restrict__ hfull, int m0,
+                          int nm, int E, int n2p, int P, int first, cx<T>* __restrict__ zs) {
+  const int64_t pp = (int64_t)P * P;
+  const int np = E * n2p, nph = (np + 1) / 2;
+  JUBIK_FOR_Z(j, nph) {
+    const int pa = (int)(2 * j), pb = pa + 1;
+    const int ka = pa % n2p, ea = pa / n2p, kb = pb % n2p, eb = pb / n2p;
+    JUBIK_FOR_Y(ky, P) {
+      const int kym = ky == 0 ? 0 : P - ky;
+      JUBIK_FOR_X(kx, P) {
+        const int kxm = kx == 0 ? 0 : P - kx;
+        const int64_t rem = (int64_t)ky * P + kx, mrem = (int64_t)kym * P + kxm;
+        const int64_t i = j * pp + rem;
+        cx<T> acc = first ? mkc<T>((T)0, (T)0) : zs[i];
+        for (int mm = 0; mm < nm; ++mm) {
+          const int64_t base = ((int64_t)mm * nph + j) * pp;
+          const cx<T> z = zu[base + rem], zm = cconj<T>(zu[base + mrem]);
+          const cx<T> a = cscale<T>(cadd<T>(z, zm), (T)0.5);
+          const cx<T> ib = cscale<T>(csub<T>(z, zm), (T)0.5);
+          const int64_t ha = ((int64_t)(m0 + mm) * n2p + ka) * E + ea;
+          acc = cadd<T>(acc, cmulc<T>(a, h_row<T>(hfull, ha, ky, kym, kx, P)));
+          if (pb < np) {
+            const int64_t hb = ((int64_t)(m0 + mm) * n2p + kb) * E + eb;
+            acc = cadd<T>(acc, cmulc<T>(ib, h_row<T>(hfull, hb, ky, kym, kx, P)));
+          }
+        }
+        zs[i] = acc;
+      }
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRowBlock)
+    k_plain_grad_gather(const cx<T>* __restrict__ zs, const T* __restrict__ wt, int E, int n,
+                        int nx, int ny, int dx, int margin, int half, int sr_max, int sc_max,
+                        int P, T scale, T* __restrict__ out) {
   const int n2p = n * n;
   const int64_t pp = (int64_t)P * P;
   const int K = 2 * dx;
-  const int64_t total = (int64_t)E * nx * ny;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int c = (int)(i % ny);
-    const int64_t t = i / ny;
-    const int r = (int)(t % nx);
-    const int e = (int)(t / nx);
-    const int tr = r + half + margin, tc = c + half + margin;
-    const int ri_hi = min(n - 1, tr / dx), ci_hi = min(n - 1, tc / dx);
-    const int ri_lo = tr - P + 1 <= 0 ? 0 : (tr - P + 1 + dx - 1) / dx;
-    const int ci_lo = tc - P + 1 <= 0 ? 0 : (tc - P + 1 + dx - 1) / dx;
-    T s = (T)0, comp = (T)0;
-    auto visit = [&](int pi, int pj) {
-      const int rb = img_row_base(pi, dx, sr_max, half, margin);
-      const int cb = img_row_base(pj, dx, sc_max, half, margin);
-      const int ya = r - rb - margin, xa = c - cb - margin;
-      if (ya < 0 || ya >= K || xa < 0 || xa >= K) return;
-      const int p = e * n2p + pj * n + pi;
-      const cx<T> z = zs[(int64_t)(p >> 1) * pp + (int64_t)(ya + margin) * P + (xa + margin)];
-      const T v = (wt[ya] * wt[xa]) * ((p & 1) ? z.y : z.x);
-      const T yk = v - comp;
-      const T tt = s + yk;
-      comp = (tt - s) - yk;
-      s = tt;
-    };
-    for (int pj = ci_lo; pj <= ci_hi; ++pj) {
-      for (int pi = ri_lo; pi <= ri_hi; ++pi) visit(pi, pj);
-      if (ri_hi < n - 1) visit(n - 1, pj);
+  JUBIK_FOR_Z(ez, (int64_t)E) {
+    const int e = (int)ez;
+    JUBIK_FOR_Y(r, nx) {
+      const int tr = r + half + margin;
+      const int ri_hi = min(n - 1, tr / dx);
+      const int ri_lo = tr - P + 1 <= 0 ? 0 : (tr - P + 1 + dx - 1) / dx;
+      T* __restrict__ orow = out + ((int64_t)e * nx + r) * ny;
+      JUBIK_FOR_X(c, ny) {
+        const int tc = c + half + margin;
+        const int ci_hi = min(n - 1, tc / dx);
+        const int ci_lo = tc - P + 1 <= 0 ? 0 : (tc - P + 1 + dx - 1) / dx;
+        T s = (T)0, comp = (T)0;
+        auto visit = [&](int pi, int pj) {
+          const int rb = img_row_base(pi, dx, sr_max, half, margin);
+          const int cb = img_row_base(pj, dx, sc_max, half, margin);
+          const int ya = r - rb - margin, xa = c - cb - margin;
+          if (ya < 0 || ya >= K || xa < 0 || xa >= K) return;
+          const int p = e * n2p + pj * n + pi;
+          const cx<T> z = zs[(int64_t)(p >> 1) * pp + (int64_t)(ya + margin) * P + (xa + margin)];
+          const T v = (wt[ya] * wt[xa]) * ((p & 1) ? z.y : z.x);
+          const T yk = v - comp;
+          const T tt = s + yk;
+          comp = (tt - s) - yk;
+          s = tt;
+        };
+        for (int pj = ci_lo; pj <= ci_hi; ++pj) {
+          for (int pi = ri_lo; pi <= ri_hi; ++pi) visit(pi, pj);
+          if (ri_hi < n - 1) visit(n - 1, pj);
+        }
+        if (ci_hi < n - 1) {
+          for (int pi = ri_lo; pi <= ri_hi; ++pi) visit(pi, n - 1);
+          if (ri_hi < n - 1) visit(n - 1, n - 1);
+        }
+        orow[c] = scale * s;
+      }
     }
-    if (ci_hi < n - 1) {
-      for (int pi = ri_lo; pi <= ri_hi; ++pi) visit(pi, n - 1);
-      if (ri_hi < n - 1) visit(n - 1, n - 1);
-    }
-    out[i] = scale * s;
   }
 }
 
@@ -1056,8 +1099,7 @@ int spectra_store(const Geom& g, const void* buf, int64_t u0, int64_t nu, void* 
 
 template <typename T>
 int plain_sky_patches(const Geom& g, const void* x, const void* wt, void* zs, cudaStream_t s) {
-  const int64_t total = plain_pairs(g) * g.P * g.P;
-  k_plain_sky_patches<T><<<grid_for(total), kBlock, 0, s>>>(
+  k_plain_sky_patches<T><<<row_grid(plain_pairs(g), g.P, g.P), kRowBlock, 0, s>>>(
       (const T*)x, (const T*)wt, g.E, g.n, g.nx, g.ny, g.dx, g.margin, g.half, g.sr_max, g.sc_max,
       g.P, (cx<T>*)zs);
   return cuda_status(cudaGetLastError(), "k_plain_sky_patches");
@@ -1066,8 +1108,7 @@ int plain_sky_patches(const Geom& g, const void* x, const void* wt, void* zs, cu
 template <typename T>
 int plain_mul_modules(const Geom& g, const void* zs, const void* hfull, int m0, int nm, void* zu,
                       cudaStream_t s) {
-  const int64_t total = (int64_t)nm * plain_pairs(g) * g.P * g.P;
-  k_plain_mul_modules<T><<<grid_for(total), kBlock, 0, s>>>(
+  k_plain_mul_modules<T><<<row_grid((int64_t)nm * plain_pairs(g), g.P, g.P), kRowBlock, 0, s>>>(
       (const cx<T>*)zs, (const cx<T>*)hfull, m0, nm, g.E, g.n * g.n, g.P, (cx<T>*)zu);
   return cuda_status(cudaGetLastError(), "k_plain_mul_modules");
 }
@@ -1075,8 +1116,7 @@ int plain_mul_modules(const Geom& g, const void* zs, const void* hfull, int m0, 
 template <typename T>
 int plain_overlap_gather(const Geom& g, const void* zu, int m0, int nm, double scale, void* out,
                          cudaStream_t s) {
-  const int64_t total = (int64_t)nm * g.E * g.nx * g.ny;
-  k_plain_overlap_gather<T><<<grid_for(total), kBlock, 0, s>>>(
+  k_plain_overlap_gather<T><<<row_grid((int64_t)nm * g.E, g.nx, g.ny), kRowBlock, 0, s>>>(
       (const cx<T>*)zu, m0, nm, g.E, g.n, g.nx, g.ny, g.dx, g.margin, g.half, g.sr_max, g.sc_max,
       g.P, (T)scale, (T*)out);
   return cuda_status(cudaGetLastError(), "k_plain_overlap_gather");
@@ -1084,8 +1124,7 @@ int plain_overlap_gather(const Geom& g, const void* zu, int m0, int nm, double s
 
 template <typename T>
 int plain_cot_patches(const Geom& g, const void* cot, int m0, int nm, void* zu, cudaStream_t s) {
-  const int64_t total = (int64_t)nm * plain_pairs(g) * g.P * g.P;
-  k_plain_cot_patches<T><<<grid_for(total), kBlock, 0, s>>>(
+  k_plain_cot_patches<T><<<row_grid((int64_t)nm * plain_pairs(g), g.P, g.P), kRowBlock, 0, s>>>(
       (const T*)cot, m0, nm, g.E, g.n, g.nx, g.ny, g.dx, g.margin, g.half, g.sr_max, g.sc_max,
       g.P, (cx<T>*)zu);
   return cuda_status(cudaGetLastError(), "k_plain_cot_patches");
@@ -1094,8 +1133,7 @@ int plain_cot_patches(const Geom& g, const void* cot, int m0, int nm, void* zu, 
 template <typename T>
 int plain_mulconj_accum(const Geom& g, const void* zu, const void* hfull, int m0, int nm,
                         bool first, void* zs, cudaStream_t s) {
-  const int64_t total = plain_pairs(g) * g.P * g.P;
-  k_plain_mulconj_accum<T><<<grid_for(total), kBlock, 0, s>>>(
+  k_plain_mulconj_accum<T><<<row_grid(plain_pairs(g), g.P, g.P), kRowBlock, 0, s>>>(
       (const cx<T>*)zu, (const cx<T>*)hfull, m0, nm, g.E, g.n * g.n, g.P, first ? 1 : 0,
       (cx<T>*)zs);
   return cuda_status(cudaGetLastError(), "k_plain_mulconj_accum");
@@ -1104,8 +1142,7 @@ int plain_mulconj_accum(const Geom& g, const void* zu, const void* hfull, int m0
 template <typename T>
 int plain_grad_gather(const Geom& g, const void* zs, const void* wt, double scale, void* out,
                       cudaStream_t s) {
-  const int64_t total = (int64_t)g.E * g.nx * g.ny;
-  k_plain_grad_gather<T><<<grid_for(total), kBlock, 0, s>>>(
+  k_plain_grad_gather<T><<<row_grid(g.E, g.nx, g.ny), kRowBlock, 0, s>>>(
       (const cx<T>*)zs, (const T*)wt, g.E, g.n, g.nx, g.ny, g.dx, g.margin, g.half, g.sr_max,
       g.sc_max, g.P, (T)scale, (T*)out);
   return cuda_status(cudaGetLastError(), "k_plain_grad_gather");
