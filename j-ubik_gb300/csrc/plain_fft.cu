@@ -80,8 +80,11 @@ __global__ void __launch_bounds__(kThreads)
                   int64_t se, const cx<T>* __restrict__ tw, FftStages st, int inv, T scale,
                   int spc) {
   extern __shared__ unsigned char smem_raw[];
+  // odd pitch per sequence: staging strided sequences one lane per sequence
+  // has no bank conflicts
+  const int LP = L | 1;
   cx<T>* b0 = reinterpret_cast<cx<T>*>(smem_raw);
-  cx<T>* b1 = b0 + (size_t)spc * L;
+  cx<T>* b1 = b0 + (size_t)spc * LP;
   const int64_t s0 = (int64_t)blockIdx.x * spc;
   const int ns = (int)min((int64_t)spc, nseq - s0);
   const bool seq_fast = (se != 1);
@@ -101,7 +104,7 @@ __global__ void __launch_bounds__(kThreads)
       i = idx % L;
       s = idx / L;
     }
-    b0[s * L + i] = data[seq_base[s] + (int64_t)i * se];
+    b0[s * LP + i] = data[seq_base[s] + (int64_t)i * se];
   }
   __syncthreads();
   cx<T>* in = b0;
@@ -114,8 +117,8 @@ __global__ void __launch_bounds__(kThreads)
     for (int b = threadIdx.x; b < ns * Lr; b += blockDim.x) {
       const int s = b / Lr;
       const int j = b - s * Lr;
-      const cx<T>* src = in + s * L;
-      cx<T>* dst = out + s * L;
+      const cx<T>* src = in + s * LP;
+      cx<T>* dst = out + s * LP;
       switch (r) {
         case 2: bfly<2, T>(src, dst, j, Lr, Ns, tstep, tw, inv); break;
         case 3: bfly<3, T>(src, dst, j, Lr, Ns, tstep, tw, inv); break;
@@ -143,7 +146,7 @@ __global__ void __launch_bounds__(kThreads)
       i = idx % L;
       s = idx / L;
     }
-    cx<T> v = in[s * L + i];
+    cx<T> v = in[s * LP + i];
     data[seq_base[s] + (int64_t)i * se] = mkc<T>(v.x * scale, v.y * scale);
   }
 }
@@ -160,11 +163,13 @@ __global__ void __launch_bounds__(kThreads)
     k_fft4(cx<T>* __restrict__ data, int64_t nseq, int nb, int64_t sa, int64_t sb, int64_t se,
            const cx<T>* __restrict__ tw, T scale, int spc) {
   constexpr int L = 16 * L1;
+  constexpr int LP = L + 1;  // odd pitch of a sequence in bx: the column-major staging of
+                             // strided sequences (one lane per sequence) has no bank conflicts
   constexpr int Q = (L1 % 2 == 0) ? L1 + 1 : L1 + 2;
   constexpr int LY = 16 * Q;
   extern __shared__ unsigned char smem_raw[];
   cx<T>* bx = reinterpret_cast<cx<T>*>(smem_raw);
-  cx<T>* by = bx + (size_t)spc * L;
+  cx<T>* by = bx + (size_t)spc * LP;
   const int64_t s0 = (int64_t)blockIdx.x * spc;
   const int ns = (int)min((int64_t)spc, nseq - s0);
   const bool seq_fast = (se != 1);
@@ -183,12 +188,12 @@ __global__ void __launch_bounds__(kThreads)
       i = idx % L;
       sq = idx / L;
     }
-    bx[sq * L + i] = data[seq_base[sq] + (int64_t)i * se];
+    bx[sq * LP + i] = data[seq_base[sq] + (int64_t)i * se];
   }
   __syncthreads();
   for (int it = threadIdx.x; it < ns * L1; it += blockDim.x) {
     const int sq = it / L1, n1 = it - sq * L1;
-    const cx<T>* src = bx + sq * L + n1;
+    const cx<T>* src = bx + sq * LP + n1;
     cx<T> v[16];
 #pragma unroll
     for (int n2 = 0; n2 < 16; ++n2) v[n2] = src[L1 * n2];
@@ -209,7 +214,7 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
     for (int n1 = 0; n1 < L1; ++n1) v[n1] = src[n1];
     Dft<L1, INV, T>::run(v);
-    cx<T>* dst = bx + sq * L + k2;
+    cx<T>* dst = bx + sq * LP + k2;
 #pragma unroll
     for (int k1 = 0; k1 < L1; ++k1) dst[16 * k1] = v[k1];
   }
@@ -223,7 +228,7 @@ __global__ void __launch_bounds__(kThreads)
       i = idx % L;
       sq = idx / L;
     }
-    const cx<T> v = bx[sq * L + i];
+    const cx<T> v = bx[sq * LP + i];
     data[seq_base[sq] + (int64_t)i * se] = mkc<T>(v.x * scale, v.y * scale);
   }
 }
@@ -233,7 +238,7 @@ int launch_fft4(void* data, int64_t nseq, int nb, int64_t sa, int64_t sb, int64_
                 const cx<T>* tw, double scale, int smax, cudaStream_t s) {
   constexpr int L = 16 * L1;
   constexpr int Q = (L1 % 2 == 0) ? L1 + 1 : L1 + 2;
-  const size_t per = sizeof(cx<T>) * (size_t)(L + 16 * Q);
+  const size_t per = sizeof(cx<T>) * (size_t)(L + 1 + 16 * Q);
   // (1 KB of the block's shared memory stays for the static sequence offsets)
   int spc = (int)std::min<size_t>(16, (size_t)(smax - 1024) / per);
   if (spc < 1) {
@@ -421,7 +426,7 @@ int fft_batched(const Fft1D& f, void* data, int64_t nseq, int nb, int64_t sa, in
                                                 s, &done);
     if (done) return st;
   }
-  const size_t per = 2 * sizeof(cx<T>) * (size_t)L;
+  const size_t per = 2 * sizeof(cx<T>) * (size_t)(L | 1);
   // (1 KB of the block's shared memory stays for the static sequence offsets)
   int spc = (int)std::max<size_t>(1, std::min<size_t>(64, (size_t)(47 * 1024) / per));
   if (per + 1024 > (size_t)smax) {
