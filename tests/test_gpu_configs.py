@@ -257,6 +257,34 @@ def test_benchmark_workload_properties(cuda, bench_case):
         p64.close()
 
 
+# --------------------------- FFT side 384: 8 x 8 eROSITA patches at 1024^2 (margin 64)
+@pytest.mark.parametrize("dtype", [F64, F32], ids=["f64", "f32"])
+def test_fft_side_384_unfused(cuda, dtype):
+    """Patches of stride 128 with a 64-pixel margin (the margin rule of
+    erosita_response.py:207 at 1024^2 with 8 x 8 patches) give P = 384, which
+    runs the unfused path: here on a 256^2 field with 2 x 2 patches, two modules
+    and two energies, against the oracle."""
+    nx, dx, m, M, E = 256, 128, 64, 2, 2
+    inst = synthetic.config2(nx=nx, dx=dx, margin=m, n_modules=M, n_energies=E, seed=5)
+    dom = O.Domain((E, nx, nx), (1.0, 1.0, 1.0))
+    R = O.Response(dom, inst.psf, nx // dx, m, inst.exposure, inst.readmask)
+    lam = R(inst.sky)
+    data = [synthetic.poisson_data(l, 9 + i) for i, l in enumerate(lam)]
+    e_ref, g_ref = R.energy_and_grad(inst.sky, data)
+    plan = make_plan(inst, dtype)
+    try:
+        assert plan.path == "plain" and plan.P == 384
+        plan.set_data(np.concatenate(data))
+        tol = 1e-12 if dtype == F64 else 1e-6
+        assert rel(plan.response(inst.sky), np.concatenate(lam)) < tol
+        e, g = plan.energy_and_grad(inst.sky)
+        assert abs(float(e) - e_ref) / abs(e_ref) < tol
+        cancel = R.adjoint([d / l for d, l in zip(data, lam)])
+        assert grad_err(g, g_ref, cancel, dtype) < (1e-11 if dtype == F64 else 3e-6)
+    finally:
+        plan.close()
+
+
 # --------------------------- the demo geometries beyond the fused tile (P = 320)
 @pytest.mark.parametrize("dtype", [F64, F32], ids=["f64", "f32"])
 def test_chandra_demo_geometry_unfused(cuda, dtype):
