@@ -55,10 +55,12 @@ def parse():
                     help="skip the FP64 comparison and the CPU baseline")
     ap.add_argument("--profile-only", action="store_true",
                     help="one warm-up and two steps (for a launch list under a profiler)")
-    ap.add_argument("--leg", choices=["step", "sky", "batch", "fp64", "psf", "sampling", "p384"],
+    ap.add_argument("--leg", choices=["step", "sky", "batch", "batch7", "fp64", "psf", "sampling",
+                                      "p384"],
                     default="step",
                     help="with --profile-only: the response step, the correlated-field sky "
-                         "(log-sky and VJP), the grouped uneven batch, the FP64 unfused step, "
+                         "(log-sky and VJP), the grouped uneven batch (one module per field, "
+                         "or batch7: seven), the FP64 unfused step, "
                          "the PSF-patch interpolation, the sampling kernels (dot products, "
                          "Poisson draws), or the FP32 step at FFT side 384 (1024^2 x 7 x 3, "
                          "8 x 8 patches, margin 64: the unfused path)")
@@ -404,15 +406,23 @@ def profile_sky_leg(dev, nx, E, passes=3):
     sky.close()
 
 
-def profile_batch_leg(dev, passes=3):
-    """The grouped pass over the config-5 uneven batch, ``passes`` times (for ncu)."""
+def profile_batch_leg(dev, passes=3, modules=1):
+    """The grouped pass over the config-5 uneven batch, ``passes`` times (for ncu):
+    64 one-module fields on the per-unit kernels, or (modules = 7) 16 fields of
+    seven modules on the module-shared kernels."""
     import torch
 
     import jubik_gb300 as ju
     from jubik_gb300 import synthetic
-    insts = synthetic.config5()
-    b = ju.ProblemBatch(insts, dtype=torch.float32, device=dev,
-                        paths={32: "fused_unit", 64: "fused_unit", 128: "fused_unit"})
+    if modules == 1:
+        insts = synthetic.config5()
+        paths = {32: "fused_unit", 64: "fused_unit", 128: "fused_unit"}
+    else:
+        insts = [synthetic.config2(nx=g["nx"], dx=g["dx"], margin=g["margin"],
+                                   n_modules=modules, n_energies=g["E"], seed=g["seed"])
+                 for g in synthetic.config5_geometry(count=16)]
+        paths = {64: "fused", 128: "fused"}
+    b = ju.ProblemBatch(insts, dtype=torch.float32, device=dev, paths=paths)
     b.set_data([synthetic.poisson_data(l, 1) for l in b.expected_counts()])
     if not b.group():
         raise RuntimeError("the config-5 batch did not group")
@@ -536,6 +546,8 @@ def main():
             profile_sky_leg(dev, nx, E)
         elif args.leg == "batch":
             profile_batch_leg(dev)
+        elif args.leg == "batch7":
+            profile_batch_leg(dev, modules=7)
         elif args.leg == "fp64":
             profile_fp64_leg(dev, inst, data)
         elif args.leg == "psf":
