@@ -24,6 +24,20 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kMaxSeqPerBlock = 64;  // sequences one block transforms (spc <= 64)
 
+// Asynchronous global -> shared copy of one complex value (8 or 16 bytes): the
+// staging loops issue every load of a thread before any of them is waited for.
+template <typename T>
+__device__ __forceinline__ void cp_async_cx(cx<T>* smem, const cx<T>* gmem) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
+  if constexpr (sizeof(cx<T>) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
+}
+
 template <int R, typename T>
 __device__ __forceinline__ void bfly(const cx<T>* __restrict__ src, cx<T>* __restrict__ dst,
                                      int j, int Lr, int Ns, int tstep,
@@ -104,8 +118,9 @@ __global__ void __launch_bounds__(kThreads)
       i = idx % L;
       s = idx / L;
     }
-    b0[s * LP + i] = data[seq_base[s] + (int64_t)i * se];
+    cp_async_cx<T>(b0 + s * LP + i, data + seq_base[s] + (int64_t)i * se);
   }
+  cp_async_wait_all();
   __syncthreads();
   cx<T>* in = b0;
   cx<T>* out = b1;
@@ -188,8 +203,9 @@ __global__ void __launch_bounds__(kThreads)
       i = idx % L;
       sq = idx / L;
     }
-    bx[sq * LP + i] = data[seq_base[sq] + (int64_t)i * se];
+    cp_async_cx<T>(bx + sq * LP + i, data + seq_base[sq] + (int64_t)i * se);
   }
+  cp_async_wait_all();
   __syncthreads();
   for (int it = threadIdx.x; it < ns * L1; it += blockDim.x) {
     const int sq = it / L1, n1 = it - sq * L1;
