@@ -286,6 +286,46 @@ def uneven_batch_leg(dev, n_streams=8, passes=10, modules=1, count=64):
         b.close()
 
 
+def chandra_demo_leg(dev, passes=20):
+    """The geometry of the reference's Chandra demo (demos/configs/chandra_demo.yaml:
+    a 512^2 sky, one observation, 3 energy bins, 4 x 4 patches and margin fraction
+    0.062, i.e. margin 32 and FFT side 320, beyond the fused tile) on synthetic
+    inputs: energy + gradient steps on the unfused path."""
+    import torch
+
+    import jubik_gb300 as ju
+    from jubik_gb300 import synthetic
+
+    inst = synthetic.config2(nx=512, dx=128, margin=32, n_modules=1, n_energies=3,
+                             dtype=np.float32)
+    mpix = inst.n_modules * inst.n_energies * inst.shape[0] * inst.shape[1] / 1e6
+    plan = ju.ResponsePlan(1, 3, inst.shape, inst.n_patches, inst.margin, dtype=torch.float32,
+                           device=dev)
+    try:
+        plan.set_psf(inst.psf)
+        plan.set_exposure(inst.exposure, inst.readmask)
+        x = torch.as_tensor(inst.sky, device=dev)
+        plan.set_data(synthetic.poisson_data(plan.response(x).double().cpu().numpy(), seed=1))
+        energy = torch.empty((), dtype=torch.float64, device=dev)
+        grad = torch.empty_like(x)
+        s = torch.cuda.current_stream(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        for _ in range(5):
+            plan.energy_and_grad(x, energy=energy, grad=grad)
+        torch.cuda.synchronize(dev)
+        e0.record(s)
+        for _ in range(passes):
+            plan.energy_and_grad(x, energy=energy, grad=grad)
+        e1.record(s)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / passes
+        return {"geometry": "512^2 x 1 observation x 3 energies, 4 x 4 patches, margin 32, P 320",
+                "path": plan.path, "mpix": mpix, "ms": ms, "mpix_s": mpix / (ms / 1e3)}
+    finally:
+        plan.close()
+
+
 def erosita_demo_leg(dev, passes=20):
     """The geometry of the reference's eROSITA demo (demos/configs/eROSITA_demo.yaml:
     a 512^2 sky, telescope modules 1 and 2, 3 energy bins, 8 x 8 patches and margin
@@ -794,6 +834,7 @@ def main():
         # the same geometry with the 7 modules of an eROSITA field, 16 fields
         line["uneven_batch_7_modules"] = uneven_batch_leg(dev, modules=7, count=16)
         line["erosita_demo"] = erosita_demo_leg(dev)
+        line["chandra_demo"] = chandra_demo_leg(dev)
         line["sky_model"] = sky_model_leg(plan, dev, nx, E, mpix)
         line["rel_err_vs_fp64_gpu"] = err
         line["fp64_plain_ms_per_step"] = fp64_ms
