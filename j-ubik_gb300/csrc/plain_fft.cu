@@ -24,6 +24,16 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kMaxSeqPerBlock = 64;  // sequences one block transforms (spc <= 64)
 
+// Division by a divisor d fixed for the kernel, as one multiply-high: with
+// m = floor(2^32 / d) + 1, floor(n / d) = (n m) >> 32 exactly whenever n d < 2^32
+// (here n < 2^18 and d <= 4096).  d = 1 passes n through.
+struct Divider {
+  uint32_t d, m;
+  __device__ __forceinline__ explicit Divider(uint32_t div)
+      : d(div), m(div > 1 ? (uint32_t)(0x100000000ull / div + 1) : 0u) {}
+  __device__ __forceinline__ uint32_t div(uint32_t n) const { return d > 1 ? __umulhi(n, m) : n; }
+};
+
 // Asynchronous global -> shared copy of one complex value (8 or 16 bytes): the
 // staging loops issue every load of a thread before any of them is waited for.
 template <typename T>
@@ -102,6 +112,7 @@ __global__ void __launch_bounds__(kThreads)
   const int64_t s0 = (int64_t)blockIdx.x * spc;
   const int ns = (int)min((int64_t)spc, nseq - s0);
   const bool seq_fast = (se != 1);
+  const Divider dns((uint32_t)ns), dL((uint32_t)L);
   // start offset of each of the block's sequences (one 64-bit division per sequence)
   __shared__ int64_t seq_base[kMaxSeqPerBlock];
   for (int sq = threadIdx.x; sq < ns; sq += blockDim.x) {
@@ -112,11 +123,11 @@ __global__ void __launch_bounds__(kThreads)
   for (int idx = threadIdx.x; idx < ns * L; idx += blockDim.x) {
     int s, i;
     if (seq_fast) {
-      s = idx % ns;
-      i = idx / ns;
+      i = (int)dns.div((uint32_t)idx);
+      s = idx - i * ns;
     } else {
-      i = idx % L;
-      s = idx / L;
+      s = (int)dL.div((uint32_t)idx);
+      i = idx - s * L;
     }
     cp_async_cx<T>(b0 + s * LP + i, data + seq_base[s] + (int64_t)i * se);
   }
@@ -129,8 +140,9 @@ __global__ void __launch_bounds__(kThreads)
     const int r = st.r[stg];
     const int Lr = L / r;
     const int tstep = L / (Ns * r);
+    const Divider dLr((uint32_t)Lr);
     for (int b = threadIdx.x; b < ns * Lr; b += blockDim.x) {
-      const int s = b / Lr;
+      const int s = (int)dLr.div((uint32_t)b);
       const int j = b - s * Lr;
       const cx<T>* src = in + s * LP;
       cx<T>* dst = out + s * LP;
@@ -155,11 +167,11 @@ __global__ void __launch_bounds__(kThreads)
   for (int idx = threadIdx.x; idx < ns * L; idx += blockDim.x) {
     int s, i;
     if (seq_fast) {
-      s = idx % ns;
-      i = idx / ns;
+      i = (int)dns.div((uint32_t)idx);
+      s = idx - i * ns;
     } else {
-      i = idx % L;
-      s = idx / L;
+      s = (int)dL.div((uint32_t)idx);
+      i = idx - s * L;
     }
     cx<T> v = in[s * LP + i];
     data[seq_base[s] + (int64_t)i * se] = mkc<T>(v.x * scale, v.y * scale);
@@ -188,6 +200,7 @@ __global__ void __launch_bounds__(kThreads)
   const int64_t s0 = (int64_t)blockIdx.x * spc;
   const int ns = (int)min((int64_t)spc, nseq - s0);
   const bool seq_fast = (se != 1);
+  const Divider dns((uint32_t)ns), dL((uint32_t)L);
   __shared__ int64_t seq_base[kMaxSeqPerBlock];
   for (int sq = threadIdx.x; sq < ns; sq += blockDim.x) {
     const int64_t q = s0 + sq;
@@ -197,11 +210,11 @@ __global__ void __launch_bounds__(kThreads)
   for (int idx = threadIdx.x; idx < ns * L; idx += blockDim.x) {
     int sq, i;
     if (seq_fast) {
-      sq = idx % ns;
-      i = idx / ns;
+      i = (int)dns.div((uint32_t)idx);
+      sq = idx - i * ns;
     } else {
-      i = idx % L;
-      sq = idx / L;
+      sq = (int)dL.div((uint32_t)idx);
+      i = idx - sq * L;
     }
     cp_async_cx<T>(bx + sq * LP + i, data + seq_base[sq] + (int64_t)i * se);
   }
@@ -238,11 +251,11 @@ __global__ void __launch_bounds__(kThreads)
   for (int idx = threadIdx.x; idx < ns * L; idx += blockDim.x) {
     int sq, i;
     if (seq_fast) {
-      sq = idx % ns;
-      i = idx / ns;
+      i = (int)dns.div((uint32_t)idx);
+      sq = idx - i * ns;
     } else {
-      i = idx % L;
-      sq = idx / L;
+      sq = (int)dL.div((uint32_t)idx);
+      i = idx - sq * L;
     }
     const cx<T> v = bx[sq * LP + i];
     data[seq_base[sq] + (int64_t)i * se] = mkc<T>(v.x * scale, v.y * scale);
