@@ -92,7 +92,25 @@ class ClockSampler:
         except OSError:
             self.proc = None
 
-    def stop(self):
+    def _rows(self):
+        with open(self.file.name) as f:
+            return [r.split(",") for r in f.read().splitlines() if r.count(",") >= 8]
+
+    def wait_first(self, limit_s: float = 5.0):
+        """Wait (at most limit_s) until nvidia-smi has written its first row, so
+        that its samples cover what runs next."""
+        t0 = time.time()
+        while self.proc is not None and time.time() - t0 < limit_s and not self._rows():
+            time.sleep(0.02)
+
+    def mark(self) -> int:
+        """Number of rows written so far: brackets a region of the run."""
+        return len(self._rows()) if self.proc is not None else 0
+
+    def stop(self, window=None):
+        """Median SM clock and the throttle reasons seen over the rows written
+        inside window = (mark at start, mark at end); the whole run when no row
+        fell inside it."""
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -101,9 +119,11 @@ class ClockSampler:
         except subprocess.TimeoutExpired:
             self.proc.kill()
         self.file.flush()
-        self.file.seek(0)
-        rows = [r.split(",") for r in self.file.read().strip().splitlines() if r.count(",") >= 8]
+        rows = self._rows()
         os.unlink(self.file.name)
+        scope = "whole run"
+        if window is not None and window[1] > window[0]:
+            rows, scope = rows[window[0]:window[1]], "timed region"
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for r in rows:
@@ -117,7 +137,7 @@ class ClockSampler:
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "scope": scope}
 
 
 def replica_throughput(ms_local: float, mpix_per_rank: float, pg=None, device=None):
@@ -286,21 +306,19 @@ def uneven_batch_leg(dev, n_streams=8, passes=10, modules=1, count=64):
         b.close()
 
 
-def chandra_demo_leg(dev, passes=20):
-    """The geometry of the reference's Chandra demo (demos/configs/chandra_demo.yaml:
-    a 512^2 sky, one observation, 3 energy bins, 4 x 4 patches and margin fraction
-    0.062, i.e. margin 32 and FFT side 320, beyond the fused tile) on synthetic
-    inputs: energy + gradient steps on the unfused path."""
+def unfused_leg(dev, nx, dx, margin, n_modules, n_energies, geometry, passes=20):
+    """Energy + gradient steps (FP32) of a geometry whose FFT side is beyond the
+    fused tile, on synthetic inputs: the unfused path, event-timed."""
     import torch
 
     import jubik_gb300 as ju
     from jubik_gb300 import synthetic
 
-    inst = synthetic.config2(nx=512, dx=128, margin=32, n_modules=1, n_energies=3,
-                             dtype=np.float32)
+    inst = synthetic.config2(nx=nx, dx=dx, margin=margin, n_modules=n_modules,
+                             n_energies=n_energies, dtype=np.float32)
     mpix = inst.n_modules * inst.n_energies * inst.shape[0] * inst.shape[1] / 1e6
-    plan = ju.ResponsePlan(1, 3, inst.shape, inst.n_patches, inst.margin, dtype=torch.float32,
-                           device=dev)
+    plan = ju.ResponsePlan(n_modules, n_energies, inst.shape, inst.n_patches, inst.margin,
+                           dtype=torch.float32, device=dev)
     try:
         plan.set_psf(inst.psf)
         plan.set_exposure(inst.exposure, inst.readmask)
@@ -320,10 +338,27 @@ def chandra_demo_leg(dev, passes=20):
         e1.record(s)
         torch.cuda.synchronize(dev)
         ms = e0.elapsed_time(e1) / passes
-        return {"geometry": "512^2 x 1 observation x 3 energies, 4 x 4 patches, margin 32, P 320",
-                "path": plan.path, "mpix": mpix, "ms": ms, "mpix_s": mpix / (ms / 1e3)}
+        return {"geometry": geometry, "path": plan.path, "mpix": mpix, "ms": ms,
+                "mpix_s": mpix / (ms / 1e3)}
     finally:
         plan.close()
+
+
+def chandra_demo_leg(dev, passes=20):
+    """The geometry of the reference's Chandra demo (demos/configs/chandra_demo.yaml:
+    a 512^2 sky, one observation, 3 energy bins, 4 x 4 patches and margin fraction
+    0.062, i.e. margin 32 and FFT side 320, beyond the fused tile)."""
+    return unfused_leg(dev, 512, 128, 32, 1, 3,
+                       "512^2 x 1 observation x 3 energies, 4 x 4 patches, margin 32, P 320",
+                       passes)
+
+
+def p384_leg(dev, passes=10):
+    """The benchmark field (1024^2 x 7 modules x 3 energies) cut into 8 x 8
+    patches: margin 64 (erosita_response.py:207's rule) and FFT side 384."""
+    return unfused_leg(dev, 1024, 128, 64, 7, 3,
+                       "1024^2 x 7 modules x 3 energies, 8 x 8 patches, margin 64, P 384",
+                       passes)
 
 
 def erosita_demo_leg(dev, passes=20):
@@ -504,15 +539,15 @@ def profile_psf_leg(dev, nx, passes=2):
     torch.cuda.synchronize()
 
 
-def profile_p384_leg(dev, passes=2):
-    """The FP32 energy+gradient step at FFT side 384 (1024^2 x 7 modules x 3
-    energies, 8 x 8 patches of stride 128, margin 64), which the fused tile does
-    not hold: the unfused path, ``passes`` times."""
+def profile_p384_leg(dev, nx=1024, passes=2):
+    """The FP32 energy+gradient step at FFT side 384 (nx^2 x 7 modules x 3
+    energies, patches of stride 128, margin 64: 8 x 8 patches at 1024^2), which
+    the fused tile does not hold: the unfused path, ``passes`` times."""
     import torch
 
     import jubik_gb300 as ju
     from jubik_gb300 import synthetic
-    inst = synthetic.config2(nx=1024, dx=128, margin=64, dtype=np.float32)
+    inst = synthetic.config2(nx=nx, dx=128, margin=64, dtype=np.float32)
     plan = ju.ResponsePlan(inst.n_modules, inst.n_energies, inst.shape, inst.n_patches,
                            inst.margin, dtype=torch.float32, device=dev)
     plan.set_psf(inst.psf)
@@ -595,7 +630,7 @@ def main():
         elif args.leg == "sampling":
             profile_sampling_leg(dev, plan.response(x))
         elif args.leg == "p384":
-            profile_p384_leg(dev)
+            profile_p384_leg(dev, nx)
         else:
             step()
             step()
@@ -608,6 +643,7 @@ def main():
     index = os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[local if world > 1
                                                                           else 0]
     sampler = ClockSampler(index.strip() or "0")
+    sampler.wait_first()
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -617,14 +653,16 @@ def main():
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    row0 = sampler.mark()
     ev0.record(stream)
     for _ in range(args.steps):
         step()
     ev1.record(stream)
     torch.cuda.synchronize()
+    row1 = sampler.mark()
     if pg:
         pg.barrier()
-    clocks = sampler.stop()
+    clocks = sampler.stop((row0, row1))
     ms, value = replica_throughput(ev0.elapsed_time(ev1) / args.steps, mpix, pg, dev)
 
     # per-kernel durations (events on the launch stream, inside the library)
@@ -835,6 +873,7 @@ def main():
         line["uneven_batch_7_modules"] = uneven_batch_leg(dev, modules=7, count=16)
         line["erosita_demo"] = erosita_demo_leg(dev)
         line["chandra_demo"] = chandra_demo_leg(dev)
+        line["p384_8x8"] = p384_leg(dev)
         line["sky_model"] = sky_model_leg(plan, dev, nx, E, mpix)
         line["rel_err_vs_fp64_gpu"] = err
         line["fp64_plain_ms_per_step"] = fp64_ms

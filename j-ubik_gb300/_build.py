@@ -20,8 +20,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libjubik_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["fused.cu", "plain_fft.cu", "ops.cu", "api.cu", "noalloc.cu", "sampling.cu",
-           "psf_interp.cu", "sky_cf.cu"]
+SOURCES = ["fused.cu", "plain_fft.cu", "plain_cols.cu", "ops.cu", "api.cu", "noalloc.cu",
+           "sampling.cu", "psf_interp.cu", "sky_cf.cu"]
 
 
 def _nvcc():

@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -373,6 +374,13 @@ int adj_terms_log2(const Geom& g) {
   return terms_log2(per * per * g.M);
 }
 
+// row pass of the unfused path's 2-D transforms over batch P x P arrays
+template <typename T>
+int plain_rows(jubik_plan* p, void* data, int64_t batch, bool inverse, cudaStream_t s) {
+  const int64_t P = p->g.P;
+  return fft_batched<T>(p->fft, data, batch * P, (int)P, P * P, P, 1, inverse, 1.0, s);
+}
+
 int do_forward(jubik_plan* p, const void* x, void* out, void* out_lo, double scale,
                cudaStream_t s, void* also_zero = nullptr, int64_t also_zero_bytes = 0,
                bool* zeroed = nullptr, SkyView view = SkyView()) {
@@ -441,6 +449,24 @@ int do_forward(jubik_plan* p, const void* x, void* out, void* out_lo, double sca
   const bool f32 = p->dtype == JUBIK_F32;
   JUBIK_TRY(f32 ? plain_sky_patches<float>(g, x, p->wt, p->zs, s)
                 : plain_sky_patches<double>(g, x, p->wt, p->zs, s));
+  if (plain_cols_supported(g.P)) {
+    // row pass; per module chunk: column stage with the PSF product, inverse row
+    // pass, overlap gather
+    const void* tw = f32 ? p->fft.tw32 : p->fft.tw64;
+    JUBIK_TRY(f32 ? plain_rows<float>(p, p->zs, plain_pairs(g), false, s)
+                  : plain_rows<double>(p, p->zs, plain_pairs(g), false, s));
+    for (int m0 = 0; m0 < g.M; m0 += p->zu_modules) {
+      const int nm = std::min(p->zu_modules, g.M - m0);
+      JUBIK_TRY(f32 ? plain_cols_forward<float>(g, p->zs, p->hfull, tw, m0, nm, p->zu, s)
+                    : plain_cols_forward<double>(g, p->zs, p->hfull, tw, m0, nm, p->zu, s));
+      const int64_t batch = (int64_t)nm * plain_pairs(g);
+      JUBIK_TRY(f32 ? plain_rows<float>(p, p->zu, batch, true, s)
+                    : plain_rows<double>(p, p->zu, batch, true, s));
+      JUBIK_TRY(f32 ? plain_overlap_gather<float>(g, p->zu, m0, nm, scale, out, s)
+                    : plain_overlap_gather<double>(g, p->zu, m0, nm, scale, out, s));
+    }
+    return JUBIK_OK;
+  }
   JUBIK_TRY(f32 ? fft2_batched<float>(p->fft, p->fft, p->zs, plain_pairs(g), false, s)
                 : fft2_batched<double>(p->fft, p->fft, p->zs, plain_pairs(g), false, s));
   for (int m0 = 0; m0 < g.M; m0 += p->zu_modules) {
@@ -514,6 +540,29 @@ int do_adjoint(jubik_plan* p, const void* cot, void* out_x, void* out_lo, double
   }
   Phase ph(p, 1, s);
   const bool f32 = p->dtype == JUBIK_F32;
+  if (plain_cols_supported(g.P)) {
+    // per module chunk: cotangent windows, row pass, column stage summing the
+    // conjugate-PSF products over modules; then the inverse row pass and the
+    // gradient gather
+    const void* tw = f32 ? p->fft.tw32 : p->fft.tw64;
+    for (int m0 = 0; m0 < g.M; m0 += p->zu_modules) {
+      const int nm = std::min(p->zu_modules, g.M - m0);
+      const bool first = m0 == 0, last = m0 + nm == g.M;
+      JUBIK_TRY(f32 ? plain_cot_patches<float>(g, cot, m0, nm, p->zu, s)
+                    : plain_cot_patches<double>(g, cot, m0, nm, p->zu, s));
+      const int64_t batch = (int64_t)nm * plain_pairs(g);
+      JUBIK_TRY(f32 ? plain_rows<float>(p, p->zu, batch, false, s)
+                    : plain_rows<double>(p, p->zu, batch, false, s));
+      JUBIK_TRY(f32 ? plain_cols_adjoint<float>(g, p->zu, p->hfull, tw, m0, nm, first, last,
+                                                p->zs, s)
+                    : plain_cols_adjoint<double>(g, p->zu, p->hfull, tw, m0, nm, first, last,
+                                                 p->zs, s));
+    }
+    JUBIK_TRY(f32 ? plain_rows<float>(p, p->zs, plain_pairs(g), true, s)
+                  : plain_rows<double>(p, p->zs, plain_pairs(g), true, s));
+    return f32 ? plain_grad_gather<float>(g, p->zs, p->wt, scale, out_x, s)
+               : plain_grad_gather<double>(g, p->zs, p->wt, scale, out_x, s);
+  }
   for (int m0 = 0; m0 < g.M; m0 += p->zu_modules) {
     const int nm = std::min(p->zu_modules, g.M - m0);
     JUBIK_TRY(f32 ? plain_cot_patches<float>(g, cot, m0, nm, p->zu, s)
@@ -690,9 +739,15 @@ int jubik_plan_create(const jubik_plan_desc* d, jubik_plan** out) {
   } else {
     if ((st = p->alloc(&p->hfull, (size_t)units * g.P * (g.P / 2 + 1) * csz))) return fail(st);
     if ((st = p->alloc(&p->zs, (size_t)plain_pairs(g) * g.P * g.P * csz))) return fail(st);
-    // bound the per-chunk unit buffer to ~2 GiB
+    // bound the per-chunk unit buffer to ~2 GiB; JUBIK_PLAIN_CHUNK_MODULES, when
+    // set to a positive count, bounds the modules per chunk further
     const size_t per_module = (size_t)plain_pairs(g) * g.P * g.P * csz;
-    p->zu_modules = (int)std::max<size_t>(1, std::min<size_t>(g.M, (2ull << 30) / per_module));
+    size_t chunk = std::min<size_t>(g.M, (2ull << 30) / per_module);
+    if (const char* env = std::getenv("JUBIK_PLAIN_CHUNK_MODULES")) {
+      const long v = std::strtol(env, nullptr, 10);
+      if (v >= 1) chunk = std::min<size_t>(chunk, (size_t)v);
+    }
+    p->zu_modules = (int)std::max<size_t>(1, chunk);
     if ((st = p->alloc(&p->zu, per_module * p->zu_modules))) return fail(st);
   }
   if ((st = p->alloc(&p->conv, img * p->esz))) return fail(st);

@@ -216,6 +216,21 @@ template <typename T>
 int plain_grad_gather(const Geom& g, const void* zs, const void* wt, double scale, void* out,
                       cudaStream_t s);
 
+// Column stage of the unfused path fused with the PSF product (plain_cols.cu),
+// for FFT sides P = 16 L1 with L1 in {10, 12, 16, 20, 24, 32}.  Forward: zs
+// holds the row-transformed sky pairs; zu gets, per module of the chunk
+// [m0, m0 + nm), the products with their columns transformed back (the inverse
+// row pass follows).  Adjoint: zu holds the chunk's row-transformed cotangent
+// pairs; zs gets their conjugate-PSF products summed over modules, added to
+// the sum of earlier chunks (first: none) and transformed back (last).
+bool plain_cols_supported(int P);
+template <typename T>
+int plain_cols_forward(const Geom& g, const void* zs, const void* hfull, const void* tw, int m0,
+                       int nm, void* zu, cudaStream_t s);
+template <typename T>
+int plain_cols_adjoint(const Geom& g, const void* zu, const void* hfull, const void* tw, int m0,
+                       int nm, bool first, bool last, void* zs, cudaStream_t s);
+
 template <typename T>
 int slice_patches_op(const void* x, int64_t batch, int nx, int ny, int n, int dr, void* out,
                      cudaStream_t s);
