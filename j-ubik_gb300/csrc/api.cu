@@ -447,14 +447,12 @@ int do_forward(jubik_plan* p, const void* x, void* out, void* out_lo, double sca
   }
   Phase ph(p, 0, s);
   const bool f32 = p->dtype == JUBIK_F32;
-  JUBIK_TRY(f32 ? plain_sky_patches<float>(g, x, p->wt, p->zs, s)
-                : plain_sky_patches<double>(g, x, p->wt, p->zs, s));
   if (plain_cols_supported(g.P)) {
-    // row pass; per module chunk: column stage with the PSF product, inverse row
-    // pass, overlap gather
+    // row pass over the weighted sky windows; per module chunk: column stage
+    // with the PSF product, inverse row pass, overlap gather
     const void* tw = f32 ? p->fft.tw32 : p->fft.tw64;
-    JUBIK_TRY(f32 ? plain_rows<float>(p, p->zs, plain_pairs(g), false, s)
-                  : plain_rows<double>(p, p->zs, plain_pairs(g), false, s));
+    JUBIK_TRY(f32 ? fft_rows_windows<float>(p->fft, g, x, false, p->wt, 0, 1, p->zs, s)
+                  : fft_rows_windows<double>(p->fft, g, x, false, p->wt, 0, 1, p->zs, s));
     for (int m0 = 0; m0 < g.M; m0 += p->zu_modules) {
       const int nm = std::min(p->zu_modules, g.M - m0);
       JUBIK_TRY(f32 ? plain_cols_forward<float>(g, p->zs, p->hfull, tw, m0, nm, p->zu, s)
@@ -467,6 +465,8 @@ int do_forward(jubik_plan* p, const void* x, void* out, void* out_lo, double sca
     }
     return JUBIK_OK;
   }
+  JUBIK_TRY(f32 ? plain_sky_patches<float>(g, x, p->wt, p->zs, s)
+                : plain_sky_patches<double>(g, x, p->wt, p->zs, s));
   JUBIK_TRY(f32 ? fft2_batched<float>(p->fft, p->fft, p->zs, plain_pairs(g), false, s)
                 : fft2_batched<double>(p->fft, p->fft, p->zs, plain_pairs(g), false, s));
   for (int m0 = 0; m0 < g.M; m0 += p->zu_modules) {
@@ -541,18 +541,15 @@ int do_adjoint(jubik_plan* p, const void* cot, void* out_x, void* out_lo, double
   Phase ph(p, 1, s);
   const bool f32 = p->dtype == JUBIK_F32;
   if (plain_cols_supported(g.P)) {
-    // per module chunk: cotangent windows, row pass, column stage summing the
-    // conjugate-PSF products over modules; then the inverse row pass and the
+    // per module chunk: row pass over the cotangent windows, column stage summing
+    // the conjugate-PSF products over modules; then the inverse row pass and the
     // gradient gather
     const void* tw = f32 ? p->fft.tw32 : p->fft.tw64;
     for (int m0 = 0; m0 < g.M; m0 += p->zu_modules) {
       const int nm = std::min(p->zu_modules, g.M - m0);
       const bool first = m0 == 0, last = m0 + nm == g.M;
-      JUBIK_TRY(f32 ? plain_cot_patches<float>(g, cot, m0, nm, p->zu, s)
-                    : plain_cot_patches<double>(g, cot, m0, nm, p->zu, s));
-      const int64_t batch = (int64_t)nm * plain_pairs(g);
-      JUBIK_TRY(f32 ? plain_rows<float>(p, p->zu, batch, false, s)
-                    : plain_rows<double>(p, p->zu, batch, false, s));
+      JUBIK_TRY(f32 ? fft_rows_windows<float>(p->fft, g, cot, true, nullptr, m0, nm, p->zu, s)
+                    : fft_rows_windows<double>(p->fft, g, cot, true, nullptr, m0, nm, p->zu, s));
       JUBIK_TRY(f32 ? plain_cols_adjoint<float>(g, p->zu, p->hfull, tw, m0, nm, first, last,
                                                 p->zs, s)
                     : plain_cols_adjoint<double>(g, p->zu, p->hfull, tw, m0, nm, first, last,

@@ -76,6 +76,16 @@ template <typename T>
 int fft2_batched(const Fft1D& fh, const Fft1D& fw, void* data, int64_t batch, bool inverse,
                  cudaStream_t s);
 
+// Forward row pass of the unfused path reading its rows from the images: pair
+// j's row y holds row y of patch 2j's and 2j+1's P x P windows (real and
+// imaginary parts), zero outside the field.  module_axis: img is (M, E, nx, ny)
+// and the nm modules from m0 are transformed; else img is (E, nx, ny) (nm = 1).
+// wt != nullptr applies the sky's window weights.  out: (nm, pairs, P, P).
+// FFT sides P = 16 L1 with L1 in {10, 12, 16, 20, 24, 32}.
+template <typename T>
+int fft_rows_windows(const Fft1D& f, const Geom& g, const void* img, bool module_axis,
+                     const void* wt, int m0, int nm, void* out, cudaStream_t s);
+
 // ------------------------------------------------------------------ fused path
 bool fused_supported(int P, int dtype);
 size_t fused_smem_bytes(int P, int dtype);

@@ -178,6 +178,46 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// The two register passes of the four-step length-16 L1 transform of ns
+// sequences staged at pitch L + 1 in bx (by: scratch of 16 Q per sequence);
+// the result is back in bx, in natural order.
+template <typename T, int L1, bool INV>
+__device__ __forceinline__ void fft4_passes(cx<T>* bx, cx<T>* by, int ns,
+                                            const cx<T>* __restrict__ tw) {
+  constexpr int L = 16 * L1;
+  constexpr int LP = L + 1;
+  constexpr int Q = (L1 % 2 == 0) ? L1 + 1 : L1 + 2;
+  constexpr int LY = 16 * Q;
+  for (int it = threadIdx.x; it < ns * L1; it += blockDim.x) {
+    const int sq = it / L1, n1 = it - sq * L1;
+    const cx<T>* src = bx + sq * LP + n1;
+    cx<T> v[16];
+#pragma unroll
+    for (int n2 = 0; n2 < 16; ++n2) v[n2] = src[L1 * n2];
+    Dft<16, INV, T>::run(v);
+    cx<T>* dst = by + sq * LY + n1;
+    dst[0] = v[0];
+#pragma unroll
+    for (int k2 = 1; k2 < 16; ++k2) {
+      const cx<T> w = tw[n1 * k2];
+      dst[Q * k2] = INV ? cmulc<T>(v[k2], w) : cmul<T>(v[k2], w);
+    }
+  }
+  __syncthreads();
+  for (int it = threadIdx.x; it < ns * 16; it += blockDim.x) {
+    const int sq = it >> 4, k2 = it & 15;
+    const cx<T>* src = by + sq * LY + Q * k2;
+    cx<T> v[L1];
+#pragma unroll
+    for (int n1 = 0; n1 < L1; ++n1) v[n1] = src[n1];
+    Dft<L1, INV, T>::run(v);
+    cx<T>* dst = bx + sq * LP + k2;
+#pragma unroll
+    for (int k1 = 0; k1 < L1; ++k1) dst[16 * k1] = v[k1];
+  }
+  __syncthreads();
+}
+
 // Batched complex FFTs of length L = 16 L1 in two register passes (four-step),
 // x[n1 + L1 n2]:
 //   pass 1, per (sequence, n1): DFT-16 over n2, times w_L^(n1 k2)
@@ -220,34 +260,7 @@ __global__ void __launch_bounds__(kThreads)
   }
   cp_async_wait_all();
   __syncthreads();
-  for (int it = threadIdx.x; it < ns * L1; it += blockDim.x) {
-    const int sq = it / L1, n1 = it - sq * L1;
-    const cx<T>* src = bx + sq * LP + n1;
-    cx<T> v[16];
-#pragma unroll
-    for (int n2 = 0; n2 < 16; ++n2) v[n2] = src[L1 * n2];
-    Dft<16, INV, T>::run(v);
-    cx<T>* dst = by + sq * LY + n1;
-    dst[0] = v[0];
-#pragma unroll
-    for (int k2 = 1; k2 < 16; ++k2) {
-      const cx<T> w = tw[n1 * k2];
-      dst[Q * k2] = INV ? cmulc<T>(v[k2], w) : cmul<T>(v[k2], w);
-    }
-  }
-  __syncthreads();
-  for (int it = threadIdx.x; it < ns * 16; it += blockDim.x) {
-    const int sq = it >> 4, k2 = it & 15;
-    const cx<T>* src = by + sq * LY + Q * k2;
-    cx<T> v[L1];
-#pragma unroll
-    for (int n1 = 0; n1 < L1; ++n1) v[n1] = src[n1];
-    Dft<L1, INV, T>::run(v);
-    cx<T>* dst = bx + sq * LP + k2;
-#pragma unroll
-    for (int k1 = 0; k1 < L1; ++k1) dst[16 * k1] = v[k1];
-  }
-  __syncthreads();
+  fft4_passes<T, L1, INV>(bx, by, ns, tw);
   for (int idx = threadIdx.x; idx < ns * L; idx += blockDim.x) {
     int sq, i;
     if (seq_fast) {
@@ -287,6 +300,144 @@ int launch_fft4(void* data, int64_t nseq, int nb, int64_t sa, int64_t sb, int64_
   kern<<<(unsigned)blocks, kThreads, smem, s>>>((cx<T>*)data, nseq, nb, sa, sb, se, tw, (T)scale,
                                                 spc);
   return cuda_status(cudaGetLastError(), "k_fft4 launch");
+}
+
+// Forward row pass of the unfused path with its rows read straight from the
+// images (the windows k_plain_sky_patches and k_plain_cot_patches write, without
+// the round trip through a pair buffer).  Sequence q = (chunk module mm, pair j,
+// row y): its real part is row y of patch 2j's P x P window, its imaginary part
+// that of patch 2j + 1 (zero if there is none), both zero outside the field.
+// Windows are cut as in convolve.py:86-104: the window of patch (r, c) starts at
+// (min(r dx, sr_max) - half - margin, min(c dx, sc_max) - half - margin).
+// module_axis: the image is (M, E, nx, ny) and the chunk starts at module m0;
+// else (E, nx, ny).  wt != nullptr: the sky's window weights, (wt[ya] wt[xa]) x
+// inside the 2dx window at offset margin (ya = y - margin, xa = x - margin), 0
+// outside it.  Output: (nm, pairs, P, P), row-transformed.
+struct RowWindows {
+  int E, n, nx, ny, dx, margin, half, sr_max, sc_max, K;
+  int m0, module_axis;
+  int64_t nph;
+};
+
+template <typename T>
+__device__ __forceinline__ void cp_async_real(T* smem, const T* gmem, bool ok) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
+  const int n = ok ? (int)sizeof(T) : 0;  // 0: zero fill, nothing read
+  if constexpr (sizeof(T) == 4)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(gmem), "r"(n)
+                 : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(d), "l"(gmem), "r"(n)
+                 : "memory");
+}
+
+template <typename T, int L1>
+__global__ void __launch_bounds__(kThreads)
+    k_fft4_rows_win(const T* __restrict__ img, const T* __restrict__ wt, RowWindows w,
+                    int64_t nseq, const cx<T>* __restrict__ tw, int spc,
+                    cx<T>* __restrict__ out) {
+  constexpr int L = 16 * L1;
+  constexpr int LP = L + 1;
+  extern __shared__ unsigned char smem_raw[];
+  cx<T>* bx = reinterpret_cast<cx<T>*>(smem_raw);
+  cx<T>* by = bx + (size_t)spc * LP;
+  __shared__ int64_t row_off[2][kMaxSeqPerBlock];  // element offset of the image row, -1: zero
+  __shared__ int col0[2][kMaxSeqPerBlock];         // image column of window column 0
+  __shared__ T row_w[kMaxSeqPerBlock];             // wt[y - margin] (weighted rows)
+  const int64_t s0 = (int64_t)blockIdx.x * spc;
+  const int ns = (int)min((int64_t)spc, nseq - s0);
+  const int n2p = w.n * w.n, np = w.E * n2p;
+  for (int sq = threadIdx.x; sq < ns; sq += blockDim.x) {
+    const int64_t q = s0 + sq;
+    const int y = (int)(q % L);
+    const int64_t up = q / L;
+    const int64_t j = up % w.nph;
+    const int64_t mm = up / w.nph;
+    const int ya = y - w.margin;
+    const bool row_in = wt == nullptr || (ya >= 0 && ya < w.K);
+    row_w[sq] = (wt != nullptr && row_in) ? wt[ya] : (T)1;
+    for (int part = 0; part < 2; ++part) {
+      const int p = (int)(2 * j + part);
+      int64_t off = -1;
+      int c0 = 0;
+      if (p < np && row_in) {
+        const int k = p % n2p, e = p / n2p;
+        const int rb = min((k % w.n) * w.dx, w.sr_max) - w.half - w.margin;
+        c0 = min((k / w.n) * w.dx, w.sc_max) - w.half - w.margin;
+        const int row = rb + y;
+        if (row >= 0 && row < w.nx) {
+          const int64_t plane = w.module_axis ? (int64_t)(w.m0 + mm) * w.E + e : (int64_t)e;
+          off = (plane * w.nx + row) * (int64_t)w.ny;
+        }
+      }
+      row_off[part][sq] = off;
+      col0[part][sq] = c0;
+    }
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < ns * L; idx += blockDim.x) {
+    const int sq = idx / L, x = idx - sq * L;
+    const bool col_in = wt == nullptr || (x - w.margin >= 0 && x - w.margin < w.K);
+    T* dst = reinterpret_cast<T*>(bx + sq * LP + x);
+#pragma unroll
+    for (int part = 0; part < 2; ++part) {
+      const int64_t off = row_off[part][sq];
+      const int col = col0[part][sq] + x;
+      const bool ok = off >= 0 && col_in && col >= 0 && col < w.ny;
+      cp_async_real<T>(dst + part, ok ? img + off + col : img, ok);
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  if (wt != nullptr) {
+    for (int idx = threadIdx.x; idx < ns * L; idx += blockDim.x) {
+      const int sq = idx / L, x = idx - sq * L;
+      const int xa = x - w.margin;
+      cx<T>& v = bx[sq * LP + x];
+      if (xa >= 0 && xa < w.K) {
+        const T wgt = row_w[sq] * wt[xa];
+        v = mkc<T>(wgt * v.x, wgt * v.y);
+      } else {
+        v = mkc<T>((T)0, (T)0);
+      }
+    }
+    __syncthreads();
+  }
+  fft4_passes<T, L1, false>(bx, by, ns, tw);
+  for (int idx = threadIdx.x; idx < ns * L; idx += blockDim.x) {
+    const int sq = idx / L, x = idx - sq * L;
+    out[(s0 + sq) * L + x] = bx[sq * LP + x];
+  }
+}
+
+template <typename T, int L1>
+int launch_rows_win(const Geom& g, const void* img, bool module_axis, const void* wt, int m0,
+                    int nm, const cx<T>* tw, int smax, void* out, cudaStream_t s) {
+  constexpr int L = 16 * L1;
+  constexpr int Q = (L1 % 2 == 0) ? L1 + 1 : L1 + 2;
+  const size_t per = sizeof(cx<T>) * (size_t)(L + 1 + 16 * Q);
+  // (2 KB of the block's shared memory stay for the static per-sequence tables)
+  const int spc = (int)std::min<size_t>(16, (size_t)(smax - 2048) / per);
+  if (spc < 1) {
+    set_error("FFT length %d needs %zu bytes of shared memory", L, per);
+    return JUBIK_ERR_UNSUPPORTED;
+  }
+  RowWindows w{g.E, g.n, g.nx, g.ny, g.dx, g.margin, g.half, g.sr_max, g.sc_max, g.K,
+               m0, module_axis ? 1 : 0, plain_pairs(g)};
+  const int64_t nseq = (int64_t)nm * w.nph * L;
+  const size_t smem = per * spc;
+  auto kern = k_fft4_rows_win<T, L1>;
+  if (smem > 47 * 1024)
+    JUBIK_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+  const int64_t blocks = (nseq + spc - 1) / spc;
+  if (blocks > 0x7fffffffLL) {
+    set_error("too many FFT sequences");
+    return JUBIK_ERR_UNSUPPORTED;
+  }
+  kern<<<(unsigned)blocks, kThreads, smem, s>>>((const T*)img, (const T*)wt, w, nseq, tw, spc,
+                                                (cx<T>*)out);
+  return cuda_status(cudaGetLastError(), "k_fft4_rows_win launch");
 }
 
 // lengths 16 L1 with a DFT-L1 codelet take the two-pass kernel; 0 = not covered
@@ -490,6 +641,28 @@ int fft2_batched(const Fft1D& fh, const Fft1D& fw, void* data, int64_t batch, bo
   return JUBIK_OK;
 }
 
+template <typename T>
+int fft_rows_windows(const Fft1D& f, const Geom& g, const void* img, bool module_axis,
+                     const void* wt, int m0, int nm, void* out, cudaStream_t s) {
+  const cx<T>* tw = (const cx<T>*)(sizeof(T) == 4 ? f.tw32 : f.tw64);
+  const int smax = max_smem_optin();
+  switch (f.L) {
+    case 160: return launch_rows_win<T, 10>(g, img, module_axis, wt, m0, nm, tw, smax, out, s);
+    case 192: return launch_rows_win<T, 12>(g, img, module_axis, wt, m0, nm, tw, smax, out, s);
+    case 256: return launch_rows_win<T, 16>(g, img, module_axis, wt, m0, nm, tw, smax, out, s);
+    case 320: return launch_rows_win<T, 20>(g, img, module_axis, wt, m0, nm, tw, smax, out, s);
+    case 384: return launch_rows_win<T, 24>(g, img, module_axis, wt, m0, nm, tw, smax, out, s);
+    case 512: return launch_rows_win<T, 32>(g, img, module_axis, wt, m0, nm, tw, smax, out, s);
+    default:
+      set_error("no windowed row pass for FFT side %d", f.L);
+      return JUBIK_ERR_UNSUPPORTED;
+  }
+}
+
+template int fft_rows_windows<float>(const Fft1D&, const Geom&, const void*, bool, const void*,
+                                     int, int, void*, cudaStream_t);
+template int fft_rows_windows<double>(const Fft1D&, const Geom&, const void*, bool, const void*,
+                                      int, int, void*, cudaStream_t);
 template int fft_batched<float>(const Fft1D&, void*, int64_t, int, int64_t, int64_t, int64_t,
                                 bool, double, cudaStream_t);
 template int fft_batched<double>(const Fft1D&, void*, int64_t, int, int64_t, int64_t, int64_t,
