@@ -461,14 +461,21 @@ __device__ __forceinline__ void input_issue(const Unit<T, P>& U, const Args& a,
   const bool interior = ADJ && U.rb >= 0 && U.rb + P <= a.nx && U.cb >= 0 && U.cb + P <= a.ny;
   const int j0 = ch.jlo + c * CH;
   const int nch = min(CH, ch.jhi - j0);
-  if (ADJ && interior && NT % width == 0) {
-    const int xs = U.tid % width, jstep = NT / width;
-    const T* gcol = src + (int64_t)U.rb * rs + U.cb + xs;
-    for (int jj = U.tid / width; jj < nch; jj += jstep) {
-      const T* g0 = gcol + (int64_t)(2 * (j0 + jj)) * rs;
-      T* d = reinterpret_cast<T*>(ch.buf(U, c, jj) + xs);
-      cp_async_in<T>(d, g0);
-      cp_async_in<T>(d + 1, g0 + rs);
+  if (ADJ && interior && NT % P == 0) {
+    // a chunk's buffer is linear in its pair rows: walk both addresses by
+    // increments instead of recomputing them per pair row
+    constexpr int JSTEP = NT / P;
+    const int xs = U.tid % P;
+    int jj = U.tid / P;
+    const T* g = src + (int64_t)(U.rb + 2 * (j0 + jj)) * rs + U.cb + xs;
+    const int64_t gstep = 2 * JSTEP * rs;
+    T* d = reinterpret_cast<T*>(ch.buf(U, c, jj) + xs);
+#pragma unroll 4
+    for (; jj < nch; jj += JSTEP) {
+      cp_async_in<T>(d, g);
+      cp_async_in<T>(d + 1, g + rs);
+      g += gstep;
+      d += 2 * JSTEP * R::TP;
     }
   } else if (NT % width == 0) {
     // each thread owns one staged column and every (NT / width)-th pair row
