@@ -478,20 +478,29 @@ __device__ __forceinline__ void input_issue(const Unit<T, P>& U, const Args& a,
       d += 2 * JSTEP * R::TP;
     }
   } else if (NT % width == 0) {
-    // each thread owns one staged column and every (NT / width)-th pair row
+    // each thread owns one staged column and every (NT / width)-th pair row;
+    // the row, its element offset and the buffer address advance by increments
     const int xs = U.tid % width, jstep = NT / width;
     const int col = U.cb + xoff + xs;
     const bool cok = col >= 0 && col < a.ny;
     const T* gcol = src + (cok ? col : 0);
-    for (int jj = U.tid / width; jj < nch; jj += jstep) {
-      const int y0 = 2 * (j0 + jj);
+    int jj = U.tid / width;
+    int y0 = 2 * (j0 + jj);
+    int64_t off = (int64_t)(U.rb + y0) * rs;
+    const int64_t ostep = 2 * (int64_t)jstep * rs;
+    T* d = reinterpret_cast<T*>(ch.buf(U, c, jj) + xs);
+    const int dstep = 2 * jstep * R::TP;
+    // the forward's odd chunk in a second buffer skips the window's pair rows:
+    // its buffer is not linear in jj
+    const bool lin = ADJ || !(ch.db && (c & 1));
+    for (; jj < nch; jj += jstep, y0 += 2 * jstep, off += ostep, d += dstep) {
       const int row = U.rb + y0;
       const bool ok0 = cok && row >= 0 && row < a.nx && (ADJ || (y0 - mg >= 0 && y0 - mg < K));
       const bool ok1 = cok && row + 1 >= 0 && row + 1 < a.nx &&
                        (ADJ || (y0 + 1 - mg >= 0 && y0 + 1 - mg < K));
-      T* d = reinterpret_cast<T*>(ch.buf(U, c, jj) + xs);
-      cp_async<T>(d, ok0 ? gcol + (int64_t)row * rs : src, ok0);
-      cp_async<T>(d + 1, ok1 ? gcol + (int64_t)(row + 1) * rs : src, ok1);
+      T* dd = lin ? d : reinterpret_cast<T*>(ch.buf(U, c, jj) + xs);
+      cp_async<T>(dd, ok0 ? gcol + off : src, ok0);
+      cp_async<T>(dd + 1, ok1 ? gcol + off + rs : src, ok1);
     }
   } else {
     for (int i = U.tid; i < nch * width; i += NT) {
