@@ -582,7 +582,8 @@ __device__ __forceinline__ void stage_input(Unit<T, P>& U, const Args& a,
 #pragma unroll
       for (int q = 0; q < 16; ++q) {
         const int xs = U.cls + L1 * q - xoff;
-        if (xs >= 0 && xs < width) {
+        // the adjoint stages whole P-wide rows: cls + L1 q is always inside
+        if (ADJ || (xs >= 0 && xs < width)) {
           cx<T> t = bsrc[xs];
           if (!ADJ && a.in_exp) t = mkc<T>(exp(t.x), exp(t.y));
           // (w_row * w_col) * x, the order of weights * slices in convolve.py:89-90
@@ -1277,7 +1278,7 @@ __device__ __forceinline__ void fused_unit_body(const Args& a, int ub, unsigned 
   stage_input<T, P, ADJ>(U, a);
   stage_split<T, P>(U);
   __syncthreads();
-  stage_col1<T, P>(U, ADJ ? 0 : 2 * (U.mg / 2), ADJ ? P : 2 * ((U.mg + U.K + 1) / 2));
+  stage_col1<T, P, ADJ>(U, ADJ ? 0 : 2 * (U.mg / 2), ADJ ? P : 2 * ((U.mg + U.K + 1) / 2));
   __syncthreads();
   stage_mid<T, P, MID_FULL, ADJ>(U);
   __syncthreads();
