@@ -121,6 +121,15 @@ __device__ __forceinline__ void cp_async_in(T* dst, const T* src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
   }
 }
+// The same copy to a shared-memory address already in the shared window.
+template <typename T>
+__device__ __forceinline__ void cp_async_in_s(unsigned d, const T* src) {
+  if constexpr (sizeof(T) == 4) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+  } else {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+  }
+}
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
 }
@@ -469,13 +478,13 @@ __device__ __forceinline__ void input_issue(const Unit<T, P>& U, const Args& a,
     int jj = U.tid / P;
     const T* g = src + (int64_t)(U.rb + 2 * (j0 + jj)) * rs + U.cb + xs;
     const int64_t gstep = 2 * JSTEP * rs;
-    T* d = reinterpret_cast<T*>(ch.buf(U, c, jj) + xs);
+    unsigned d = (unsigned)__cvta_generic_to_shared(ch.buf(U, c, jj) + xs);
 #pragma unroll 4
     for (; jj < nch; jj += JSTEP) {
-      cp_async_in<T>(d, g);
-      cp_async_in<T>(d + 1, g + rs);
+      cp_async_in_s<T>(d, g);
+      cp_async_in_s<T>(d + (unsigned)sizeof(T), g + rs);
       g += gstep;
-      d += 2 * JSTEP * R::TP;
+      d += (unsigned)(JSTEP * R::TP * sizeof(cx<T>));
     }
   } else if (NT % width == 0) {
     // each thread owns one staged column and every (NT / width)-th pair row;
