@@ -741,8 +741,9 @@ def main():
            and inst.n_patches % 4 == 0 and M >= 2)
     fwd_kernel = "k_fwd_run<float,192>" if run else "k_fwd_from_spec<float,192>"
     kinfo = {  # phase -> (kernel, bytes, flops)
+        # the forward leaves both words of the exact two-word image sum
         "forward": (fwd_kernel if shared else "k_fused<float,192,fwd>",
-                    spec + (pspec if shared else sky) + img,
+                    spec + (pspec if shared else sky) + 2 * img,
                     U * (fft_unit * (1 if shared else 2) + mul_unit)),
         "adjoint": ("k_adj_to_spec_ord<float,192>" if shared else "k_fused<float,192,adj>",
                     spec + img + (pspec if shared else sky),
