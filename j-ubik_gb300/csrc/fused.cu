@@ -130,9 +130,6 @@ __device__ __forceinline__ void cp_async_in_s(unsigned d, const T* src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
   }
 }
-__device__ __forceinline__ void cp_async_wait_all() {
-  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory");
-}
 
 // Programmatic dependent launch: every kernel of a step lets the next one be
 // scheduled as soon as all of its CTAs run (launch_dependents), and waits for
@@ -542,7 +539,7 @@ template <typename T, int P, bool ADJ, bool TRACK = false>
 __device__ __forceinline__ void stage_input(Unit<T, P>& U, const Args& a,
                                             bool chunk0_issued = false) {
   using R = Tr<T, P>;
-  constexpr int L1 = R::L1, H = R::H, NT = R::NT, TP = R::TP, CH = R::CH;
+  constexpr int L1 = R::L1, NT = R::NT, TP = R::TP, CH = R::CH;
   cx<T>* tile = U.tile;
   const int mg = U.mg, K = U.K;
   const InChunks<T, P, ADJ> ch(U);

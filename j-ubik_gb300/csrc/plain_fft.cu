@@ -232,8 +232,6 @@ __global__ void __launch_bounds__(kThreads)
   constexpr int L = 16 * L1;
   constexpr int LP = L + 1;  // odd pitch of a sequence in bx: the column-major staging of
                              // strided sequences (one lane per sequence) has no bank conflicts
-  constexpr int Q = (L1 % 2 == 0) ? L1 + 1 : L1 + 2;
-  constexpr int LY = 16 * Q;
   extern __shared__ unsigned char smem_raw[];
   cx<T>* bx = reinterpret_cast<cx<T>*>(smem_raw);
   cx<T>* by = bx + (size_t)spc * LP;
