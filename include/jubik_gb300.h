@@ -46,7 +46,14 @@ enum jubik_dtype { JUBIK_F32 = 0, JUBIK_F64 = 1 };
 enum jubik_path {
   JUBIK_PATH_AUTO = 0,  /* fused when the FFT side and dtype allow it */
   JUBIK_PATH_FUSED = 1, /* one kernel per patch unit: FFT, PSF product, overlap-add */
-  JUBIK_PATH_PLAIN = 2, /* unfused: batched FFT kernels + gather kernels */
+  JUBIK_PATH_PLAIN = 2, /* unfused: batched FFT kernels + gather kernels.  For FFT sides
+                           160, 192, 256, 320, 384 and 512 the row passes read the
+                           windows from the images and one kernel does the column
+                           passes with the PSF product.  The per-module buffer is cut
+                           into module chunks of at most ~2 GiB; the environment
+                           variable JUBIK_PLAIN_CHUNK_MODULES (a positive count, read
+                           at plan creation) bounds the modules per chunk further.
+                           Results do not depend on the chunking. */
   JUBIK_PATH_FUSED_UNIT = 3 /* fused, one kernel per (module, energy, patch) unit with no
                                sharing of patch spectra across modules */
 };
