@@ -88,7 +88,17 @@ struct Args {
   void* spill;
   int loop_grid;
   int run_len;  // run-ordered forward: patches per run (2 or 4)
+  // floor(u / d) for d = M, n^2, n and n / run_len as one multiply-high by these
+  // constants (div_const); 0: divide
+  uint32_t div_M, div_n2, div_n, div_nq;
 };
+
+// floor(u / d) for 0 <= u: with mul = floor(2^32 / d) + 1 the high word of u mul
+// is exact while u d < 2^32 (mul d exceeds 2^32 by at most d, so u mul / 2^32
+// exceeds u / d by less than 1 / d).  mul = 0 divides.
+__device__ __forceinline__ int div_by(int u, int d, uint32_t mul) {
+  return mul ? (int)__umulhi((uint32_t)u, mul) : u / d;
+}
 
 __device__ __forceinline__ float2 ldg2(const float2* p) { return __ldg(p); }
 __device__ __forceinline__ double2 ldg2(const double2* p) { return __ldg(p); }
@@ -389,13 +399,15 @@ struct Unit {
     int u = ub >= 0 ? ub : (int)blockIdx.x;
     m = 0;
     if (per_module) {
-      m = u % a.M;
-      u /= a.M;
+      const int q = div_by(u, a.M, a.div_M);
+      m = u - q * a.M;
+      u = q;
     }
-    k = u % n2p;
-    e = u / n2p;
-    const int sr = min((k % a.n) * a.dx, a.sr_max);
-    const int sc = min((k / a.n) * a.dx, a.sc_max);
+    e = div_by(u, n2p, a.div_n2);
+    k = u - e * n2p;
+    const int kc = div_by(k, a.n, a.div_n);
+    const int sr = min((k - kc * a.n) * a.dx, a.sr_max);
+    const int sc = min(kc * a.dx, a.sc_max);
     rb = sr - a.half - a.margin;
     cb = sc - a.half - a.margin;
     K = 2 * a.dx;
@@ -1519,11 +1531,12 @@ __device__ __forceinline__ void stage_output_run(Unit<T, P>& U, const Args& a,
 // run_len patch rows, the patch column j, the energy e.  Returns unit (w, s).
 __device__ __forceinline__ int run_unit(const Args& a, int w, int s) {
   const int nq = a.n / a.run_len;
-  const int m = w % a.M;
-  int t = w / a.M;
-  const int q = t % nq;
-  t /= nq;
-  const int j = t % a.n, e = t / a.n;
+  int t = div_by(w, a.M, a.div_M);
+  const int m = w - t * a.M;
+  const int t2 = div_by(t, nq, a.div_nq);
+  const int q = t - t2 * nq;
+  t = t2;
+  const int e = div_by(t, a.n, a.div_n), j = t - e * a.n;
   const int k = a.run_len * q + s + a.n * j;
   return ((e * a.n * a.n + k) * a.M + m);
 }
@@ -1810,6 +1823,21 @@ int64_t loop_grid(KernelT kern, int64_t count, size_t smem = Tr<T, P>::SMEM) {
 }
 
 // Kernel arguments of one stage of one plan (sizes in bytes use esz).
+// multiply-high constant of div_by for divisor d and numerators below `bound`
+uint32_t div_const(int64_t d, int64_t bound) {
+  if (d < 2 || bound <= 0 || bound * d >= (int64_t(1) << 32)) return 0;
+  return (uint32_t)((uint64_t(1) << 32) / (uint64_t)d + 1);
+}
+
+// numerators of the unit decompositions stay below the unit count
+void set_div_consts(Args& a, int64_t units) {
+  const int64_t bound = units + 1;
+  a.div_M = div_const(a.M, bound);
+  a.div_n2 = div_const((int64_t)a.n * a.n, bound);
+  a.div_n = div_const(a.n, bound);
+  a.div_nq = a.run_len > 0 ? div_const(a.n / a.run_len, bound) : 0;
+}
+
 Args make_args(const Geom& g, const FusedLaunch& f, int which, size_t esz) {
   Args a;
   a.in = f.in;
@@ -1859,6 +1887,7 @@ Args make_args(const Geom& g, const FusedLaunch& f, int which, size_t esz) {
   a.spill = f.spill;
   a.loop_grid = (int)f.loop_grid;
   a.run_len = 0;
+  set_div_consts(a, g.units());
   return a;
 }
 
@@ -2027,6 +2056,7 @@ int launch_one(const Geom& g, const FusedLaunch& f, int which, cudaStream_t s) {
           const int64_t items = units / r;
           Args ar = a;
           ar.run_len = r;
+          set_div_consts(ar, units);
           return launch_pdl<T, P>(k_fwd_run<T, P>, loop_grid<T, P>(k_fwd_run<T, P>, items),
                                   f.pdl, s, ar, (int)items);
         }
