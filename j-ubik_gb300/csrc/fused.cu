@@ -89,7 +89,7 @@ struct Args {
   int loop_grid;
   int run_len;  // run-ordered forward: patches per run (2 or 4)
   // floor(u / d) for d = M, n^2, n and n / run_len as one multiply-high by these
-  // constants (div_const); 0: divide
+  // constants (mulhi_divisor); 0: divide
   uint32_t div_M, div_n2, div_n, div_nq;
 };
 
@@ -1823,19 +1823,13 @@ int64_t loop_grid(KernelT kern, int64_t count, size_t smem = Tr<T, P>::SMEM) {
 }
 
 // Kernel arguments of one stage of one plan (sizes in bytes use esz).
-// multiply-high constant of div_by for divisor d and numerators below `bound`
-uint32_t div_const(int64_t d, int64_t bound) {
-  if (d < 2 || bound <= 0 || bound * d >= (int64_t(1) << 32)) return 0;
-  return (uint32_t)((uint64_t(1) << 32) / (uint64_t)d + 1);
-}
-
 // numerators of the unit decompositions stay below the unit count
 void set_div_consts(Args& a, int64_t units) {
   const int64_t bound = units + 1;
-  a.div_M = div_const(a.M, bound);
-  a.div_n2 = div_const((int64_t)a.n * a.n, bound);
-  a.div_n = div_const(a.n, bound);
-  a.div_nq = a.run_len > 0 ? div_const(a.n / a.run_len, bound) : 0;
+  a.div_M = mulhi_divisor(a.M, bound);
+  a.div_n2 = mulhi_divisor((int64_t)a.n * a.n, bound);
+  a.div_n = mulhi_divisor(a.n, bound);
+  a.div_nq = a.run_len > 0 ? mulhi_divisor(a.n / a.run_len, bound) : 0;
 }
 
 Args make_args(const Geom& g, const FusedLaunch& f, int which, size_t esz) {

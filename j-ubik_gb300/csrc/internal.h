@@ -40,6 +40,15 @@ struct Geom {
 // unfused path: real patches are transformed two per complex array
 inline int64_t plain_pairs(const Geom& g) { return ((int64_t)g.E * g.n * g.n + 1) / 2; }
 
+// Multiply-high constant for dividing numerators 0 <= u < bound by d on the
+// device: floor(u / d) = high word of u * (floor(2^32 / d) + 1), exact while
+// u d < 2^32 (the product exceeds u / d by less than 1 / d).  0 when d < 2 or
+// the bound is too large: the kernel then divides.
+inline uint32_t mulhi_divisor(int64_t d, int64_t bound) {
+  if (d < 2 || bound <= 0 || bound * d >= (int64_t(1) << 32)) return 0;
+  return (uint32_t)((uint64_t(1) << 32) / (uint64_t)d + 1);
+}
+
 
 // ------------------------------------------------------------------ plain FFT
 constexpr int kMaxStages = 24;
