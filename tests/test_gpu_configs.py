@@ -4,8 +4,9 @@
   (FFT side 96): response and Poisson likelihood in FP64 and FP32, and the
   literal full-field kernel path.
 - 1024^2 x 3 energies, correlated-field sky, 16x16 patches, margin 32:
-  JVP, VJP and MGVI metric, and central finite differences (eps = 1e-4) of
-  the Poisson energy along 32 random directions.
+  JVP, VJP and MGVI metric, and central finite differences of the Poisson
+  energy (FP64: eps = 1e-4, 32 random directions; FP32: 4 directions that
+  follow the gradient, where the derivative rises above the FP32 rounding).
 - 2048^2 x 3 energies with 0.1 % point sources (flux 1e1 .. 1e5) and
   power-law PSF wings, 32x32 patches: FP32 against FP64 per energy.
 - 1024^2 x 7 modules x 3 energies (the benchmark workload) at full size:
@@ -175,6 +176,51 @@ def test_derivatives_central_finite_differences(cuda, deriv_case):
             scale = float(torch.linalg.norm(g) * torch.linalg.norm(v)) / np.sqrt(x.numel())
             worst = max(worst, abs(fd - an) / scale)
         assert worst < 2e-4, worst
+    finally:
+        plan.close()
+
+
+def test_fp32_gradient_central_finite_differences(cuda, deriv_case):
+    """The FP32 tier's gradient against central differences of its own energy.
+
+    An FP32 energy carries rounding of a few tens in absolute terms (here |H|
+    is about 2e11, and lam rounds at about 1e-7 of a patch's brightest values,
+    with errors correlated across pixels).  Along a random direction v the
+    derivative <grad, v> is only about |grad| = 5e3, so that rounding, divided
+    by 2 eps, swamps it.  The directions here follow the gradient: sign(grad),
+    sign(grad) with random weights in [0.5, 1.5], and grad itself.  Along them
+    the derivative is sqrt(n) times larger, 1e4 to 2e5 per 2 eps.  The
+    perturbed points are rounded to FP32, so H(x+) - H(x-) is compared with
+    <grad, x+ - x-> over the points actually evaluated.  The float64 oracle
+    puts the truncation error of these central differences at 3e-5 (sign,
+    eps = 1e-2) and 1.5e-4 (grad, eps = 3e-3); the FP32 gradient is within
+    6.5e-4 of FP64.  The bound 1e-2 leaves a margin over all of them; a wrong
+    derivative (a missing factor) is off by O(1)."""
+    c = deriv_case
+    plan = make_plan(c["inst"], F32)
+    try:
+        plan.set_data(c["data"])
+        x64 = torch.as_tensor(c["inst"].sky, device=cuda)
+        x = x64.float()
+        _, g = plan.energy_and_grad(x)
+        g = g.double()
+        n = g.numel()
+        rng = np.random.default_rng(35)
+        sg = torch.sign(g)
+        dirs = [(sg, 1e-2)]
+        for _ in range(2):
+            dirs.append((sg * torch.as_tensor(rng.uniform(0.5, 1.5, size=x.shape), device=cuda),
+                         1e-2))
+        dirs.append((g / torch.linalg.norm(g) * np.sqrt(n), 3e-3))
+        worst = 0.0
+        for d, eps in dirs:
+            xp = (x64 + eps * d).float()
+            xm = (x64 - eps * d).float()
+            ep = float(plan.energy_and_grad(xp, need_grad=False)[0])
+            em = float(plan.energy_and_grad(xm, need_grad=False)[0])
+            an = float((g * (xp.double() - xm.double())).sum())
+            worst = max(worst, abs((ep - em) - an) / abs(an))
+        assert worst < 1e-2, worst
     finally:
         plan.close()
 
